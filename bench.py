@@ -1,0 +1,381 @@
+#!/usr/bin/env python
+"""Raster Join benchmark on GB300.
+
+Default workload (benchmark configuration 2, the one the headline metric is
+quoted for that fits one GPU): 100M points resident in HBM with columns
+x, y (float32), t (uint32, one year), a (float32 lognormal), f1, f2 (int32
+0..9); 260 Voronoi neighbourhoods over a 40 x 40 km box; the hybrid join
+(exact) with the time range = first 6 months, f1 > 2, f2 < 8, a < 50 and
+avg(a), polygon grid index 256 x 256.
+
+A step is one query answered from scratch: grid index, outline mask and
+polygon labels rebuilt (RJ_FLAG_NO_CACHE), one streaming pass over the
+points, results read back.  `value` is points joined per second with the
+table resident; `e2e` adds, every step, the host->device copy of all six
+columns from pinned memory and the result read-back.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--join hybrid|index|raster] [--points N]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (os.path.join(ROOT, "raster-join_gb300"), os.path.join(ROOT, "oracle"), ROOT):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+BYTES_PER_POINT = 24          # x, y, t, a, f1, f2: 4 bytes each, all read by the query
+WORKLOAD = "config2: 100M pts (x,y,t,a,f1,f2), 260 Voronoi polys, 40x40 km, t in first 6 months & f1>2 & f2<8 & a<50, avg(a), grid 256"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--join", default="hybrid", choices=["hybrid", "index", "raster"])
+    ap.add_argument("--points", type=int, default=100_000_000)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_workload(n, seed):
+    from rasterjoin import synth
+    pts = synth.points(n, seed=seed, columns=True)
+    verts, pidx = synth.voronoi_polygons(260, seed=20261203)
+    return pts, verts, pidx
+
+
+def query_constraints():
+    import rasterjoin as rj
+    from rasterjoin import synth
+    cons = [(4, rj.GT, 2), (5, rj.LT, 8), (3, rj.LT, 50.0)]
+    trange = (2, synth.T0, synth.T0 + synth.YEAR // 2)
+    return cons, trange
+
+
+def fn_of(join):
+    import rasterjoin as rj
+    return {"hybrid": rj.HybridJoinFn, "index": rj.IndexJoinFn, "raster": rj.RasterJoinFn}[join]
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed loop runs."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu_id):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu_id), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append((time.time(), ln.strip()))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+
+    def summary(self, t0=None, t1=None):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ts, ln in self.lines:
+            if t0 is not None and (ts < t0 or ts > t1):
+                continue
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(join, n):
+    """DRAM bytes per launch of the point kernel from the committed ncu summary, scaled to n points."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "point_pass_traffic.json")) as fh:
+            d = json.load(fh)
+        e = d[join]
+        return float(e["dram_bytes_per_point"]) * n
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline(pts, verts, pidx, join, sample_points):
+    """CPUJoin restatement (oracle port, all host threads) on a bounded sample."""
+    import oracle
+    cons, trange = query_constraints()
+    n = min(sample_points, len(pts["xy"]))
+    cols = oracle.Columns({2: (oracle.Uint, pts["t"][:n]), 3: (oracle.Float, pts["a"][:n]),
+                           4: (oracle.Int, pts["f1"][:n]), 5: (oracle.Int, pts["f2"][:n])})
+    f = cols.filt([(a, o, v) for a, o, v in cons], aggr_attrib=3, time_range=trange)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    _, _, tj, tb = oracle.cpujoin(pts["xy"][:n], verts, pidx, 1024, f=f, nthreads=threads)
+    wall = time.perf_counter() - t0
+    return n, wall, tj, tb, threads
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    sample = min(args.points, 20_000_000)
+    pts, verts, pidx = make_workload(sample, seed=20261203)
+    times = []
+    threads = os.cpu_count() or 1
+    for i in range(args.warmup + args.steps):
+        n, wall, tj, tb, threads = cpu_baseline(pts, verts, pidx, args.join, sample)
+        if i >= args.warmup:
+            times.append(wall)
+    step = float(np.mean(times))
+    value = sample / step / 1e9
+    line = {
+        "impl": "reference",
+        "metric": "Gpoints/s joined (exact join, config 2 query)",
+        "value": value, "unit": "Gpoints/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_points": sample, "parallelism": "cpu-threads"},
+        "cpu_baseline": {"value": value, "unit": "Gpoints/s", "cores": threads, "kind": "port",
+                         "sample": "CPUJoin restatement (grid 1024 built each step + join) over the first %d points "
+                                   "of the config-2 table, with the config-2 filters and avg as a labelled "
+                                   "extension (CPUJoin itself counts only)" % sample},
+        "e2e": {"value": value, "unit": "Gpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+def run_gb300(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import __graft_entry__
+    __graft_entry__.build()
+    import rasterjoin as rj
+
+    n = args.points
+    pts, verts, pidx = make_workload(n, seed=20261203 + rank)
+    P = len(pidx) - 1
+    stream = torch.cuda.Stream()
+    h = rj.GLHandler(device=local, stream=stream.cuda_stream)
+    dh = rj.DataHandler()
+    dh.add_column(1, rj.Location, pts["xy"])
+    dh.add_column(2, rj.Uint, pts["t"])
+    dh.add_column(3, rj.Float, pts["a"])
+    dh.add_column(4, rj.Int, pts["f1"])
+    dh.add_column(5, rj.Int, pts["f2"])
+    dh.setPolygons(verts, pidx)
+    cons, trange = query_constraints()
+    dh.setQueryConstraints(cons)
+    dh.setTimeRange(*trange)
+    dh.setAggregation(rj.Avg, 3)
+    h.setDataHandler(dh)
+    h.setAccuracyDistance(10.0 if args.join == "raster" else 100.0)
+    h.setPolyIndexResolution(256)
+    h.flags = rj.FLAG_NO_CACHE | rj.FLAG_PHASE_TIMING
+    fn = fn_of(args.join)
+    h.upload()
+    q = h.make_query(fn)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(max(3, args.warmup)):
+        h.execute(fn, query=q)
+    torch.cuda.synchronize()
+
+    dev_uuid = None
+    try:
+        dev_uuid = torch.cuda.get_device_properties(local).uuid
+        dev_uuid = "GPU-" + str(dev_uuid)
+    except Exception:
+        dev_uuid = local
+    sampler = ClockSampler(dev_uuid)
+    sampler.start()
+    time.sleep(0.3)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    pt_ms, launches = [], []
+    barrier()
+    torch.cuda.synchronize()
+    t_wall0 = time.time()
+    for i in range(args.steps):
+        starts[i].record(stream)
+        h.execute(fn, query=q)
+        ends[i].record(stream)
+        t = h.timings()
+        pt_ms.append(t["pt_render_ms"])
+        launches.append(t["kernel_launches"])
+    torch.cuda.synchronize()
+    barrier()
+    t_wall1 = time.time()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if world > 1:
+        tt = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    # keep sampling a little under the same load if the timed loop was short
+    probe_end = time.time() + max(0.0, 1.5 - (t_wall1 - t_wall0))
+    while time.time() < probe_end:
+        h.execute(fn, query=q)
+    torch.cuda.synchronize()
+    sampler.stop()
+    clocks_timed = sampler.summary(t_wall0, t_wall1)
+    clocks_all = sampler.summary()
+    clocks = dict(clocks_all)
+    clocks["samples_in_timed_region"] = clocks_timed["samples"]
+
+    res = h.last
+    ms_per_step = total_ms / args.steps
+    value = world * n / (total_ms / args.steps / 1e3) / 1e9
+
+    # ---- end to end through the public API with host buffers (pinned) ----
+    pinned = {}
+    for k in ("xy", "t", "a", "f1", "f2"):
+        arr = pts[k]
+        tns = torch.empty(arr.shape, dtype={np.float32: torch.float32, np.uint32: torch.int32,
+                                            np.int32: torch.int32}[arr.dtype.type], pin_memory=True)
+        tns.numpy().view(arr.dtype)[...] = arr
+        pinned[k] = tns.numpy().view(arr.dtype)
+    dh2 = rj.DataHandler()
+    dh2.add_column(1, rj.Location, pinned["xy"])
+    dh2.add_column(2, rj.Uint, pinned["t"])
+    dh2.add_column(3, rj.Float, pinned["a"])
+    dh2.add_column(4, rj.Int, pinned["f1"])
+    dh2.add_column(5, rj.Int, pinned["f2"])
+    dh2.setPolygons(verts, pidx)
+    dh2.setQueryConstraints(cons)
+    dh2.setTimeRange(*trange)
+    dh2.setAggregation(rj.Avg, 3)
+    h.setDataHandler(dh2)
+    h.upload(force=True)
+    e2e_times = []
+    for i in range(args.e2e_steps + 2):
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h.upload(force=True)                 # H2D of all columns (rj_load_points)
+        r = h.execute(fn, query=q)           # join + D2H of the results
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if i >= 2:
+            e2e_times.append(dt)
+    e2e_s = float(np.mean(e2e_times))
+    if world > 1:
+        tt = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    same = bool(np.array_equal(r.count, res.count))
+    h2d = n * BYTES_PER_POINT
+    d2h = P * (8 + 8 + 12 + 16)
+
+    # ---- roofline of the point pass ----
+    peak, peak_kind = measured_peaks()
+    mean_pt = float(np.mean(pt_ms))
+    achieved = (n * BYTES_PER_POINT / 1e9) / (mean_pt / 1e3) if mean_pt > 0 else None
+    traffic = profiled_traffic(args.join, n)
+
+    line = {
+        "metric": "Gpoints/s joined (config 2: %s join; exact, so within any epsilon incl. 10 m)" % args.join,
+        "value": value, "unit": "Gpoints/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded; stands in for the NYC-taxi table)",
+        "config": {"workload": WORKLOAD, "join": args.join, "points_per_gpu": n, "polygons": P,
+                   "grid_res": 256, "l2": "inputs (2.4 GB per step) larger than L2", "parallelism":
+                   "replicas" if world > 1 else "single-gpu"},
+        "e2e": {"value": world * n / e2e_s / 1e9, "unit": "Gpoints/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "same_result": same},
+        "gpu_launches": int(sum(launches)),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "kernel": "k_points (point pass)", "kernel_ms": mean_pt,
+                     "algorithmic_bytes_per_launch": n * BYTES_PER_POINT, "peak_kind": peak_kind},
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sample = min(n, 20_000_000)
+        s_n, wall, tj, tb, threads = cpu_baseline(pts, verts, pidx, args.join, sample)
+        line["cpu_baseline"] = {"value": s_n / wall / 1e9, "unit": "Gpoints/s", "cores": threads, "kind": "port",
+                                "sample": "CPUJoin restatement (grid 1024 build %.2fs + join %.2fs) over the first "
+                                          "%d points of the same table, config-2 filters and avg as a labelled "
+                                          "extension" % (tb, tj, s_n)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    h.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

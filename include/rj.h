@@ -1,0 +1,227 @@
+/*
+ * rj.h -- C ABI of the GB300-native Raster Join library (librj.so).
+ *
+ * This is the drop-in boundary for the reference's join layer.  Every entry
+ * point below names the reference interface it replaces (paths are relative
+ * to the VIDA-NYU/raster-join source tree).  All signatures use plain C types
+ * and pointers; no C++ or CUDA types cross the boundary except an opaque
+ * cudaStream_t passed as void*.
+ *
+ * Ownership: input buffers passed as host pointers are copied into device
+ * memory owned by the context; result buffers are caller-allocated host
+ * memory filled on return.  Functions return RJ_OK (0) or a negative status
+ * and never exit the process (the reference called exit(0) on bad input,
+ * RasterJoin/join/GLData.cpp:18-23, RasterJoin/join/GLFunction.cpp:251-252).
+ */
+#ifndef RJ_H
+#define RJ_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RJ_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define RJ_API __attribute__((visibility("default")))
+#else
+#define RJ_API
+#endif
+
+/* ---- status codes (replace qDebug + empty QVector / exit(0)) ---------- */
+#define RJ_OK                      0
+#define RJ_E_INVALID              -1   /* bad argument / malformed input        */
+#define RJ_E_OOM                  -2   /* device memory budget exceeded         */
+#define RJ_E_TOO_MANY_CONSTRAINTS -3   /* > RJ_MAX_CONSTRAINTS (GLFunction.cpp:416) */
+#define RJ_E_TIMEOUT              -4   /* a bounded device wait ran out          */
+#define RJ_E_CUDA                 -5   /* CUDA runtime error                    */
+#define RJ_E_NO_DATA              -6   /* points or polygons not loaded (GLHandler.cpp:190-193) */
+#define RJ_E_UNSUPPORTED          -7   /* join type / option not supported      */
+#define RJ_E_BUSY                 -8   /* admission refused (serving queue full) */
+
+/* ---- limits ------------------------------------------------------------- */
+#define RJ_MAX_CONSTRAINTS 10   /* std140 vec4 query[10], RasterJoin/shaders/points.vert:8-10 */
+#define RJ_MAX_ATTRIBUTES  16   /* columns a point table may hold (reference: 6, GLFunction.cpp:358) */
+#define RJ_MAX_FBO_SIZE    8192 /* canvas tile side, RasterJoin/join/GLFunction.hpp:14 */
+
+/* ---- enums: values identical to the reference ------------------------- */
+/* GLHandler::FunctionType, RasterJoin/join/GLHandler.hpp:23-29 */
+typedef enum {
+    RJ_RASTER_JOIN = 0,      /* RasterJoinFn      */
+    RJ_INDEX_JOIN = 1,       /* IndexJoinFn       */
+    RJ_HYBRID_JOIN = 2,      /* HybridJoinFn      */
+    RJ_RASTER_JOIN_BOUNDS = 3 /* RasterJoinBoundFn */
+} rj_function_type;
+
+/* Aggregation, RasterJoin/common/Common.h:34 */
+typedef enum { RJ_COUNT = 0, RJ_AVG = 1, RJ_SUM = 2 } rj_aggregation;
+
+/* ConstraintType, RasterJoin/common/Common.h:30 */
+typedef enum { RJ_EQ = 0, RJ_LT = 1, RJ_LTE = 2, RJ_GT = 3, RJ_GTE = 4 } rj_constraint_type;
+
+/* AttributeType, RasterJoin/common/Common.h:28 */
+typedef enum { RJ_LOCATION = 0, RJ_UINT = 1, RJ_INT = 2, RJ_FLOAT = 3 } rj_attribute_type;
+
+/* Value / QueryConstraint, RasterJoin/common/Common.h:36-47: 16 bytes,
+ * same field order (asserted at RasterJoin/main.cpp:376). */
+typedef union { int32_t ival; float fval; uint32_t uval; } rj_value;
+typedef struct {
+    int32_t attrib_id;   /* attribute id of the point table column */
+    int32_t type;        /* rj_constraint_type                      */
+    rj_value val;        /* comparison value, typed by the column   */
+    int32_t dummy;       /* padding, as in the reference            */
+} rj_constraint;
+
+/* Semantic switches (named modes for the reference's quirks).  Zero gives
+ * the default semantics; each flag reproduces one reference behaviour. */
+#define RJ_FLAG_COMPAT_INDEX_CLAMP 0x1u /* GPU grid drops the last column/row:
+                                           create-index.glsl:56-61,69-70 */
+#define RJ_FLAG_COMPAT_FLOAT_EQ    0x2u /* LTE/GTE equality compares the raw
+                                           bit patterns as IEEE floats:
+                                           points.vert:98-107 */
+#define RJ_FLAG_LINE_FILTER        0x4u /* error bounds keep only pixels whose
+                                           centre is within 0.5 px of the edge:
+                                           line-bound.frag:245 */
+#define RJ_FLAG_FORCE_CANVAS       0x8u /* raster/hybrid: always accumulate a
+                                           point canvas (no polygon label map) */
+#define RJ_FLAG_PHASE_TIMING       0x10u /* record CUDA events per phase       */
+#define RJ_FLAG_NO_CELL_CLASSIFY   0x20u /* index/hybrid: PIP against every MBR
+                                           candidate, as index.glsl:389-400 */
+#define RJ_FLAG_NO_CACHE           0x40u /* rebuild every polygon-side structure
+                                           (grid, labels, masks) for this call,
+                                           as each reference execute() does */
+
+/* One query: everything GLHandler + DataHandler held between calls
+ * (setAccuracyDistance GLHandler.cpp:250, setPolyIndexResolution :259,
+ *  setQueryConstraints DataHandler.cpp:64, setAggregation :68). */
+typedef struct {
+    int32_t function_type;          /* rj_function_type                    */
+    int32_t aggregation;            /* rj_aggregation                      */
+    int32_t aggr_attrib;            /* column aggregated when != RJ_COUNT  */
+    int32_t n_constraints;          /* 0..RJ_MAX_CONSTRAINTS               */
+    rj_constraint constraints[RJ_MAX_CONSTRAINTS];
+    double accuracy_m;              /* epsilon: pixel diagonal in metres,
+                                       GLFunction::setMaxCellSize
+                                       GLFunction.cpp:26-30               */
+    double cell_size;               /* > 0: pixel side in world units,
+                                       overrides accuracy_m                */
+    double ground_resolution;       /* metres per world unit (1 for metric
+                                       coordinates; UsefulFuncs.cpp:625)   */
+    int32_t grid_res;               /* polygon grid index resolution       */
+    int32_t max_fbo_size;           /* canvas tile side (0 = 8192)         */
+    int32_t time_attrib;            /* uint32 column of the time range, or -1 */
+    uint32_t t_start, t_end;        /* inclusive range, DataHandler.cpp:107-109 */
+    int32_t hybrid_canvas;          /* hybrid canvas long side (0 = 8192,
+                                       HybridJoin.cpp:65)                  */
+    uint32_t flags;                 /* RJ_FLAG_*                           */
+} rj_query;
+
+/* Results.  Host buffers allocated by the caller, npolys entries each (bounds:
+ * 4*npolys), any pointer may be NULL if not wanted.
+ *   count  : exact per-polygon count            (agg[i], main.cpp:215)
+ *   sum    : per-polygon sum of the aggregate   (exact fp64 accumulation)
+ *   compat3: the reference's int32[3P] layout [count | sum/100 | decimal*10]
+ *            (GLFunction.cpp:42, polygon.frag:17-24), decodable by
+ *            printResults main.cpp:206-208
+ *   bounds : int32[4P] [fn | fp | fn1 | fp1] (line-bound.frag:250-258) for
+ *            RJ_RASTER_JOIN_BOUNDS */
+typedef struct {
+    int32_t npolys;
+    uint64_t *count;
+    double *sum;
+    int32_t *compat3;
+    int32_t *bounds;
+} rj_result;
+
+/* Context configuration: GLHandler::getInstance(gpuMemMB, inMemory),
+ * RasterJoin/join/GLHandler.cpp:43-69. */
+typedef struct {
+    int32_t device;          /* CUDA device ordinal                       */
+    int64_t gpu_mem_mb;      /* device memory budget (0 = no limit)       */
+    void *stream;            /* cudaStream_t to run on (NULL = own stream) */
+} rj_config;
+
+/* One point-table column (QueryResult::addAttributeResult,
+ * RasterJoin/db/QueryResult.hpp:38-47): RJ_LOCATION columns are float (x,y)
+ * pairs, the others 4-byte values. */
+typedef struct {
+    int32_t attrib_id;
+    int32_t type;            /* rj_attribute_type */
+    const void *data;
+} rj_column;
+
+/* Per-call timings in milliseconds, the fields of the reference's timing line
+ * (GLHandler::printTimeStats GLHandler.cpp:214-248, schema
+ * experiments/plot-scripts/result_parser.py:5). */
+typedef struct {
+    uint64_t pts_size;
+    int32_t poly_size;
+    int32_t function;
+    int32_t no_pt_passes;
+    int32_t no_constraints;
+    double execute_ms;        /* whole rj_execute, host wall clock         */
+    double pt_mem_ms;         /* point upload (0 for resident tables)      */
+    double pt_render_ms;      /* point pass kernels (CUDA events)          */
+    double poly_mem_ms;       /* polygon uploads / derived-structure copies */
+    double poly_render_ms;    /* polygon pass kernels (CUDA events)        */
+    double setup_ms;          /* host planning                             */
+    double triangulation_ms;  /* always 0: no triangulation is needed      */
+    double poly_index_ms;     /* grid index build (CUDA events)            */
+    double backend_query_ms;  /* always 0: no backend query                */
+    int32_t accuracy;         /* accuracy_m for raster joins, else 0       */
+    int32_t kernel_launches;  /* kernels this library launched in the call */
+} rj_timings;
+
+typedef struct rj_ctx rj_ctx;
+
+/* ---- context ------------------------------------------------------------ */
+/* replaces GLHandler::getInstance + initializeGL + initFunctions
+ * (GLHandler.cpp:43-69,157-186). */
+RJ_API int rj_create(const rj_config *cfg, rj_ctx **out);
+/* replaces GLHandler::~GLHandler (GLHandler.cpp:56-62) */
+RJ_API void rj_destroy(rj_ctx *ctx);
+/* human-readable text of the last failing call on this context */
+const char *rj_last_error(const rj_ctx *ctx);
+/* run subsequent work on a caller stream (cudaStream_t) */
+RJ_API int rj_set_stream(rj_ctx *ctx, void *stream);
+RJ_API int rj_abi_version(void);
+
+/* ---- point table: DataHandler::initData + executeQuery result columns
+ * (DataHandler.cpp:24-62,86-96); GLFunction::setupPoints GLFunction.cpp:199-344 */
+RJ_API int rj_load_points(rj_ctx *ctx, const rj_column *cols, int32_t ncols,
+                   uint64_t npoints, int32_t loc_attrib);
+/* same, but the data pointers are device pointers (16-byte aligned) that the
+ * caller keeps alive; nothing is copied */
+RJ_API int rj_attach_points_device(rj_ctx *ctx, const rj_column *cols, int32_t ncols,
+                            uint64_t npoints, int32_t loc_attrib);
+RJ_API int rj_free_points(rj_ctx *ctx);
+
+/* ---- polygons: PolyHandler::addPolygonCollection (PolyHandler.cpp:49-80).
+ * xy: float pairs of all polygons back to back (PolyHandler "polys"),
+ * pindex: npolys+1 offsets in vertices ("pindexes").  Polygons are open rings
+ * (last vertex != first, PolyHandler.cpp:165-167).  bbox (minx,miny,maxx,maxy)
+ * may be NULL: it is then the vertex bounds, as readPolygons computes
+ * (PolyHandler.cpp:178-186). */
+RJ_API int rj_set_polygons(rj_ctx *ctx, const float *xy, const int32_t *pindex,
+                    int32_t npolys, const double *bbox);
+
+/* ---- execution: GLHandler::executeFunction (GLHandler.cpp:188-204) and
+ * getErrorBounds (GLHandler.cpp:206-212) in one call. */
+RJ_API int rj_execute(rj_ctx *ctx, const rj_query *q, rj_result *res);
+
+/* Fill q with the reference defaults: count, no constraints, accuracy 100 m
+ * (main.cpp:268), grid 256 (main.cpp:299), canvas tile 8192. */
+RJ_API void rj_query_init(rj_query *q);
+
+/* ---- timings: GLHandler::printTimeStats (GLHandler.cpp:214-248) --------- */
+RJ_API int rj_get_timings(const rj_ctx *ctx, rj_timings *out);
+/* the reference's tab-separated timing line for the last call */
+RJ_API int rj_format_time_stats(const rj_ctx *ctx, char *buf, size_t buflen);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RJ_H */

@@ -1,0 +1,268 @@
+// rj_device.cuh -- device-side building blocks shared by every join kernel.
+//
+// All floating-point arithmetic that decides a result (pixel of a point,
+// crossing-number point-in-polygon) uses explicitly rounded intrinsics so
+// that no multiply-add is contracted: the CPU oracle evaluates the same
+// expressions operation by operation and must agree bit for bit.
+#pragma once
+#include <cstdint>
+#include <cstring>
+#include <cuda_runtime.h>
+
+#include "../../include/rj.h"
+
+namespace rj {
+
+constexpr int kMaxFilters = RJ_MAX_CONSTRAINTS + 2;   // + time range (2 predicates)
+constexpr uint32_t kEmptyLabel = 0xFFFFFFFFu;
+constexpr int kSubpixelBits = 8;                      // GL_SUBPIXEL_BITS on NVIDIA
+constexpr int kSub = 1 << kSubpixelBits;              // 256 fixed-point units per pixel
+constexpr float kWinClamp = 1048576.0f;               // |window coord| clamp (2^20 px)
+
+// ---------------------------------------------------------------------------
+// Filter + aggregate description (GLFunction::setupPoints GLFunction.cpp:199-344
+// gathers constraint columns; points.vert:138-159 evaluates them).
+struct DevFilter {
+    int n;                                   // predicates (constraints + time range)
+    const uint32_t* col[kMaxFilters];        // column of each predicate
+    int op[kMaxFilters];                     // rj_constraint_type
+    int typ[kMaxFilters];                    // rj_attribute_type of the column
+    uint32_t val[kMaxFilters];               // comparison value (bit pattern)
+    uint32_t compat_mask;                    // bit k: predicate k uses RJ_FLAG_COMPAT_FLOAT_EQ
+    int aggr;                                // 0: count only, else sum of aggr_col
+    int aggr_typ;
+    const uint32_t* aggr_col;
+};
+
+// aLessThan / aGreaterThan / aEqual, points.vert:24-85: Uint and Int compare
+// the reinterpreted bits, Float compares as fp32; Location (or anything else)
+// yields true.
+__host__ __device__ __forceinline__ bool pred_less(int typ, uint32_t a, uint32_t f) {
+    switch (typ) {
+        case RJ_UINT: return a < f;
+        case RJ_INT: return (int32_t)a < (int32_t)f;
+        case RJ_FLOAT: {
+            float af, ff;
+            memcpy(&af, &a, 4); memcpy(&ff, &f, 4);
+            return af < ff;
+        }
+        default: return true;
+    }
+}
+__host__ __device__ __forceinline__ bool pred_greater(int typ, uint32_t a, uint32_t f) {
+    switch (typ) {
+        case RJ_UINT: return a > f;
+        case RJ_INT: return (int32_t)a > (int32_t)f;
+        case RJ_FLOAT: {
+            float af, ff;
+            memcpy(&af, &a, 4); memcpy(&ff, &f, 4);
+            return af > ff;
+        }
+        default: return true;
+    }
+}
+__host__ __device__ __forceinline__ bool pred_equal(int typ, uint32_t a, uint32_t f) {
+    switch (typ) {
+        case RJ_UINT: return a == f;
+        case RJ_INT: return (int32_t)a == (int32_t)f;
+        case RJ_FLOAT: {
+            float af, ff;
+            memcpy(&af, &a, 4); memcpy(&ff, &f, 4);
+            return af == ff;
+        }
+        default: return true;
+    }
+}
+// validFilter, points.vert:87-114.  LTE/GTE add an equality test that the
+// reference writes as a float comparison of the raw bits
+// (`filterVal == attributes[aid-1]`, points.vert:99,107); by default the
+// equality is typed, RJ_FLAG_COMPAT_FLOAT_EQ selects the float comparison.
+__host__ __device__ __forceinline__ bool pred_eval(int op, int typ, uint32_t a, uint32_t f, int compat) {
+    bool eq_ext = false;
+    if (op == RJ_LTE || op == RJ_GTE) {
+        if (compat) {
+            float af, ff;
+            memcpy(&af, &a, 4); memcpy(&ff, &f, 4);
+            eq_ext = (ff == af);
+        } else {
+            eq_ext = pred_equal(typ, a, f);
+        }
+    }
+    switch (op) {
+        case RJ_EQ: return pred_equal(typ, a, f);
+        case RJ_LT: return pred_less(typ, a, f);
+        case RJ_LTE: return pred_less(typ, a, f) || eq_ext;
+        case RJ_GT: return pred_greater(typ, a, f);
+        case RJ_GTE: return pred_greater(typ, a, f) || eq_ext;
+        default: return false;
+    }
+}
+
+// floatVal, points.vert:116-136: the aggregate value as fp32.
+__host__ __device__ __forceinline__ float agg_value(int typ, uint32_t a) {
+    switch (typ) {
+        case RJ_UINT: return (float)a;
+        case RJ_INT: return (float)(int32_t)a;
+        case RJ_FLOAT: { float af; memcpy(&af, &a, 4); return af; }
+        default: return 0.0f;
+    }
+}
+
+__device__ __forceinline__ bool filter_point(const DevFilter& f, uint64_t i) {
+    #pragma unroll 1
+    for (int k = 0; k < f.n; ++k) {
+        uint32_t a = __ldg(f.col[k] + i);
+        if (!pred_eval(f.op[k], f.typ[k], a, f.val[k], (int)((f.compat_mask >> k) & 1u))) return false;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Raster canvas geometry (RasterJoin::updateBuffers RasterJoin.cpp:51-78, tile
+// loop :224-231, getMVP Utils.h:36-46).  One tile's model-view-projection is a
+// scale and a translation held in fp32 (QMatrix4x4); the viewport maps NDC to
+// window pixels.
+struct TileXf {
+    float sx, tx, sy, ty;     // ndc = s*world + t
+    float hx, hy;             // res/2 per axis
+};
+
+// world -> window coordinate along one axis: ndc = fl(fl(s*v) + t);
+// window = fl(fl(h*ndc) + h)  (GL viewport transform, origin 0).
+__host__ __device__ __forceinline__ float win_coord(float v, float s, float t, float h) {
+#ifdef __CUDA_ARCH__
+    float ndc = __fadd_rn(__fmul_rn(s, v), t);
+    return __fadd_rn(__fmul_rn(h, ndc), h);
+#else
+    volatile float p = s * v;
+    volatile float ndc = p + t;
+    volatile float q = h * ndc;
+    return q + h;
+#endif
+}
+
+// Snap a window coordinate to the 1/256-pixel lattice, round to nearest even.
+__host__ __device__ __forceinline__ int32_t snap_win(float w) {
+    w = fminf(fmaxf(w, -kWinClamp), kWinClamp);
+#ifdef __CUDA_ARCH__
+    return __float2int_rn(__fmul_rn(w, (float)kSub));
+#else
+    return (int32_t)lrintf(w * (float)kSub);
+#endif
+}
+
+__host__ __device__ __forceinline__ int64_t floordiv64(int64_t a, int64_t b) {
+    // b > 0
+    int64_t q = a / b;
+    if ((a % b != 0) && (a < 0)) --q;
+    return q;
+}
+
+// Pixel column of a snapped point coordinate: floor(X/256).
+__host__ __device__ __forceinline__ int32_t pix_of(int32_t X) {
+    return X >> kSubpixelBits;   // arithmetic shift == floor division by 256
+}
+
+// Exact edge-function crossing for the pixel-centre fill rule.  Vertices are
+// fixed-point window coordinates.  Row centre Cy (fixed point).  The edge
+// (A,B) crosses the row iff (A.y >= Cy) != (B.y >= Cy) (top-closed, as GL's
+// top-left rule).  It then toggles every pixel i whose centre lies strictly
+// left of the exact intersection x; those are the pixels i < L with
+// L = ceil((x_int - 128)/256).  Returns L (may be <0 or >res; caller clamps).
+__host__ __device__ __forceinline__ int32_t cross_L(int32_t ax, int32_t ay, int32_t bx, int32_t by, int32_t cy) {
+    int64_t dy = (int64_t)by - ay;
+    int64_t num = ((int64_t)ax - (kSub / 2)) * dy + ((int64_t)bx - ax) * ((int64_t)cy - ay);
+    int64_t den = dy * kSub;
+    if (den < 0) { num = -num; den = -den; }
+    // ceil(num/den)
+    int64_t q = floordiv64(num, den);
+    if (q * den != num) ++q;
+    if (q > (int64_t)0x3fffffff) q = 0x3fffffff;
+    if (q < -(int64_t)0x3fffffff) q = -0x3fffffff;
+    return (int32_t)q;
+}
+__host__ __device__ __forceinline__ bool cross_row(int32_t ay, int32_t by, int32_t cy) {
+    return (ay >= cy) != (by >= cy);
+}
+
+// ---------------------------------------------------------------------------
+// Crossing-number point-in-polygon, index.glsl:47-67 / GridIndexF.cpp:383-402,
+// evaluated in fp32 with the reference's expression order
+// (vj.x - vi.x) * (testy - vi.y) / (vj.y - vi.y) + vi.x.
+__device__ __forceinline__ bool edge_toggles(float vix, float viy, float vjx, float vjy, float tx, float ty) {
+    if ((viy > ty) != (vjy > ty)) {
+        float xi = __fadd_rn(__fdiv_rn(__fmul_rn(__fsub_rn(vjx, vix), __fsub_rn(ty, viy)), __fsub_rn(vjy, viy)), vix);
+        return tx < xi;
+    }
+    return false;
+}
+
+__device__ __forceinline__ bool pip_f32(const float2* __restrict__ v, int n, float tx, float ty) {
+    bool c = false;
+    float2 vj = __ldg(v + (n - 1));
+    for (int i = 0; i < n; ++i) {
+        float2 vi = __ldg(v + i);
+        if (edge_toggles(vi.x, vi.y, vj.x, vj.y, tx, ty)) c = !c;
+        vj = vi;
+    }
+    return c;
+}
+
+// Grid cell of a point, index.glsl:382-385: int() truncates toward zero.
+__device__ __forceinline__ int grid_cell_1d(float p, float lb, float cs) {
+    return __float2int_rz(__fdiv_rn(__fsub_rn(p, lb), cs));
+}
+
+// ---------------------------------------------------------------------------
+// Hybrid canvas pixel of a point, hybrid.glsl:187-200 (rasterize): half-open
+// [-1,1) in normalised coordinates, fp32 throughout.
+struct HybXf {
+    float ox, oy;      // origin = (rightTop + leftBottom)/2
+    float dx, dy;      // diff = (rightTop - leftBottom)/2
+    int resx, resy;    // fboRes
+};
+__device__ __forceinline__ bool hyb_rasterize(const HybXf& h, float x, float y, int& px, int& py) {
+    float u = __fdiv_rn(__fsub_rn(x, h.ox), h.dx);
+    float v = __fdiv_rn(__fsub_rn(y, h.oy), h.dy);
+    if (u < -1.0f || u >= 1.0f || v < -1.0f || v >= 1.0f) return false;
+    u = __fmul_rn(__fadd_rn(u, 1.0f), 0.5f);
+    v = __fmul_rn(__fadd_rn(v, 1.0f), 0.5f);
+    px = __float2int_rz(__fmul_rn(u, (float)h.resx));
+    py = __float2int_rz(__fmul_rn(v, (float)h.resy));
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Warp helpers
+__device__ __forceinline__ int warp_min(int v) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ int warp_max(int v) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_minf(float v) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_maxf(float v) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_sum_f64(double v) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace rj

@@ -1,0 +1,113 @@
+// rj_launch.h -- kernel argument structs and launcher declarations shared by
+// the kernel translation units and the host runtime.
+#pragma once
+#include <algorithm>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "rj_device.cuh"
+
+namespace rj {
+
+enum { MODE_REDUCE = 0, MODE_LABEL = 1, MODE_BOUNDS = 2 };
+
+// Kernels launched by this thread since the last reset (reported per call).
+extern thread_local int g_kernel_launches;
+
+struct PolyPassArgs {
+    const int2* wv;              // [T][V] fixed-point window coordinates
+    const float2* wf;            // [T][V] fp32 window coordinates (bounds)
+    const int* pindex;           // [P+1]
+    int P, V, T;
+    int resx, resy;
+    const uint32_t* canvas_c;    // [T][resy][resx] point counts
+    const double* canvas_s;      // [T][resy][resx] sums or null
+    uint32_t* label;             // [T][resy][resx] polygon label (MODE_LABEL)
+    const uint32_t* border;      // dilated hybrid border mask (skip) or null
+    int border_words;
+    unsigned long long* out_count;
+    double* out_sum;
+    long long* out_bounds;       // [4P]
+    unsigned int* work_ctr;
+    int* flag;                   // bit0: label conflict (overlapping polygons)
+    int line_filter;
+};
+
+struct GridArgs {
+    const float2* verts;
+    const int* pindex;
+    int P;
+    float lbx, lby, csx, csy;
+    int res;
+    int compat_clamp;
+    int* cell_count;
+    const int* cell_start;
+    int* cursor;
+    int* entries;
+};
+
+// Per-axis tile transforms of a raster canvas.
+struct CanvasXf {
+    const float4* colxf;         // [splitx] (sx, tx, hx, tile_dx)
+    const float4* rowxf;         // [splity] (sy, ty, hy, tile_dy)
+    int splitx, splity;
+    int resx, resy;
+    float lbx, lby;              // canvas lower-left (fp32), for the tile guess
+    float tdx, tdy;              // tile extent (fp32), for the tile guess
+    float4 col0, row0;           // transform of column 0 / row 0 (single-tile fast path)
+};
+
+// Point-table view for the point kernels.
+struct PointArgs {
+    const float2* xy;
+    uint64_t n;
+    DevFilter f;
+    int P;
+    unsigned long long* out_count;
+    double* out_sum;
+};
+
+// Exact point-in-polygon index (CSR over a uniform grid).
+struct IndexArgs {
+    const float2* verts;
+    const int* pindex;
+    const int* cell_start;       // [res*res + 1]
+    const int* entries;
+    float lbx, lby, csx, csy;
+    int res;
+};
+
+struct HybridArgs {
+    HybXf h;
+    const uint32_t* border;      // dilated border mask [resy][words]
+    int words;
+    uint32_t* canvas_c;          // canvas mode: [resy][resx]
+    double* canvas_s;
+    const uint32_t* label;       // label mode: [resy][resx]
+};
+
+// polygon side
+void launch_transform_vertices(const float2* verts, int V, const float4* colxf, const float4* rowxf,
+                               int splitx, int T, int2* wv, float2* wf, int sms, cudaStream_t st);
+void launch_poly_pass(int mode, const PolyPassArgs& a, int sms, cudaStream_t st);
+void launch_grid_count(const GridArgs& g, int sms, cudaStream_t st);
+void launch_grid_fill(const GridArgs& g, int sms, cudaStream_t st);
+void launch_grid_sort(const int* cell_start, int* entries, int ncells, int sms, cudaStream_t st);
+int scan_tmp_ints(int n);
+bool launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_t st);
+void launch_outline_mask(const float2* verts, const int* pindex, int P, const int* edge_poly, int V,
+                         const HybXf& h, float margin, uint32_t* mask, int words, int sms, cudaStream_t st);
+void launch_dilate_mask(const uint32_t* in, uint32_t* out, int resx, int resy, int words, int radius,
+                        int sms, cudaStream_t st);
+
+// point side
+// smem_hist: histogram capacity decision done by the launcher.
+void launch_raster_splat(const PointArgs& pa, const CanvasXf& cx, uint32_t* canvas_c, double* canvas_s,
+                         int sms, cudaStream_t st);
+void launch_raster_label(const PointArgs& pa, const CanvasXf& cx, const uint32_t* label, int sms,
+                         cudaStream_t st);
+void launch_index_points(const PointArgs& pa, const IndexArgs& ia, int sms, cudaStream_t st);
+void launch_hybrid_points(const PointArgs& pa, const IndexArgs& ia, const HybridArgs& ha, int sms,
+                          cudaStream_t st);
+
+}  // namespace rj

@@ -1,0 +1,991 @@
+// rj_runtime.cu -- host runtime behind the C ABI (include/rj.h).
+//
+// It plays the role of the reference's GLHandler + GLFunction layer
+// (RasterJoin/join/GLHandler.cpp, GLFunction.cpp): it owns the device, a
+// stream, the resident point table and polygon set, the derived per-polygon-set
+// structures (grid index, label maps, masks) and plans every query into kernel
+// launches.  Join types dispatch through a table indexed by the reference's
+// FunctionType, like GLHandler::initFunctions (GLHandler.cpp:157-186).
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "rj_device.cuh"
+#include "rj_launch.h"
+
+using namespace rj;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct Column {
+    int attrib = -1;
+    int type = RJ_FLOAT;
+    void* d = nullptr;
+    bool owned = false;
+};
+
+// Derived structures of the current polygon set, rebuilt on demand.
+struct GridCache {
+    bool valid = false;
+    int res = 0;
+    int clamp = 0;
+    float lbx = 0, lby = 0, csx = 0, csy = 0;
+    size_t nentries = 0;
+};
+
+}  // namespace
+
+struct rj_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int sms = 1;
+    int64_t budget = 0;       // bytes, 0 = unlimited
+    size_t used = 0;
+    std::string err;
+
+    // point table (QueryResult columns)
+    uint64_t npts = 0;
+    int loc_attrib = -1;
+    std::vector<Column> cols;
+
+    // polygon set (PolyHandler polys / pindexes / bounds)
+    int P = 0, V = 0;
+    std::vector<float> h_xy;
+    std::vector<int> h_pindex;
+    double bbox[4] = {0, 0, 0, 0};
+    float max_abs_coord = 0.f, max_edge_dx = 0.f, max_edge_dy = 0.f;
+    DevBuf d_verts, d_pindex, d_edge_poly;
+    uint64_t poly_version = 0;
+    int overlap_known = -1;   // -1 unknown, 0 no overlap, 1 overlap
+
+    GridCache grid;
+    std::map<std::string, DevBuf> scratch;
+
+    rj_timings tm{};
+    cudaEvent_t ev[8]{};
+};
+
+namespace {
+
+int fail(rj_ctx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+#define RJ_CUDA(call)                                                                         \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(ctx, RJ_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                        __FILE__, __LINE__);                                                  \
+    } while (0)
+
+int dev_alloc(rj_ctx* ctx, DevBuf& b, size_t bytes) {
+    if (b.p && b.bytes >= bytes) return RJ_OK;
+    if (b.p) {
+        cudaFree(b.p);
+        ctx->used -= b.bytes;
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    if (bytes == 0) bytes = 16;
+    bytes = (bytes + 255) & ~size_t(255);
+    if (ctx->budget > 0 && (int64_t)(ctx->used + bytes) > ctx->budget)
+        return fail(ctx, RJ_E_OOM, "device memory budget exceeded: need %zu more bytes, %zu of %lld in use",
+                    bytes, ctx->used, (long long)ctx->budget);
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        b.p = nullptr;
+        return fail(ctx, RJ_E_OOM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    b.bytes = bytes;
+    ctx->used += bytes;
+    return RJ_OK;
+}
+
+void dev_free(rj_ctx* ctx, DevBuf& b) {
+    if (b.p) {
+        cudaFree(b.p);
+        ctx->used -= b.bytes;
+    }
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+int scratch(rj_ctx* ctx, const char* key, size_t bytes, void** out) {
+    DevBuf& b = ctx->scratch[key];
+    int rc = dev_alloc(ctx, b, bytes);
+    if (rc) return rc;
+    *out = b.p;
+    return RJ_OK;
+}
+
+template <class T>
+int scratch_t(rj_ctx* ctx, const char* key, size_t count, T** out) {
+    void* p = nullptr;
+    int rc = scratch(ctx, key, count * sizeof(T), &p);
+    *out = (T*)p;
+    return rc;
+}
+
+const Column* find_col(const rj_ctx* ctx, int attrib) {
+    for (const Column& c : ctx->cols)
+        if (c.attrib == attrib) return &c;
+    return nullptr;
+}
+
+void free_points(rj_ctx* ctx) {
+    for (Column& c : ctx->cols) {
+        if (c.owned && c.d) cudaFree(c.d);
+    }
+    // owned column sizes are tracked in ctx->used by load_points
+    ctx->cols.clear();
+    ctx->npts = 0;
+    ctx->loc_attrib = -1;
+}
+
+double now_ms() {
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+// ---------------------------------------------------------------------------
+// Raster canvas plan: RasterJoin::updateBuffers (RasterJoin.cpp:51-78) and the
+// per-tile MVP (RasterJoin.cpp:224-231, Utils.h:36-46).
+struct RasterPlan {
+    double cell = 0;
+    int actual_x = 0, actual_y = 0;
+    int splitx = 1, splity = 1;
+    int resx = 1, resy = 1;
+    std::vector<float4> colxf, rowxf;
+};
+
+int plan_raster(rj_ctx* ctx, const rj_query* q, RasterPlan& rp) {
+    double ground = q->ground_resolution > 0 ? q->ground_resolution : 1.0;
+    double cell = q->cell_size > 0 ? q->cell_size : (q->accuracy_m / std::sqrt(2.0)) / ground;
+    if (!(cell > 0) || !std::isfinite(cell)) return fail(ctx, RJ_E_INVALID, "invalid cell size %g", cell);
+    double dx = ctx->bbox[2] - ctx->bbox[0], dy = ctx->bbox[3] - ctx->bbox[1];
+    if (!(dx > 0 && dy > 0)) return fail(ctx, RJ_E_INVALID, "degenerate polygon bounds");
+    double ax = std::ceil(dx / cell), ay = std::ceil(dy / cell);
+    if (ax > 2e6 || ay > 2e6) return fail(ctx, RJ_E_INVALID, "canvas too large: %.0f x %.0f", ax, ay);
+    rp.cell = cell;
+    rp.actual_x = std::max(1, (int)ax);
+    rp.actual_y = std::max(1, (int)ay);
+    int max_res = q->max_fbo_size > 0 ? q->max_fbo_size : RJ_MAX_FBO_SIZE;
+    rp.splitx = (int)std::ceil(double(rp.actual_x) / max_res);
+    rp.splity = (int)std::ceil(double(rp.actual_y) / max_res);
+    rp.resx = (int)std::ceil(double(rp.actual_x) / rp.splitx);
+    rp.resy = (int)std::ceil(double(rp.actual_y) / rp.splity);
+    if ((size_t)rp.splitx * rp.splity > 65536) return fail(ctx, RJ_E_INVALID, "too many canvas tiles");
+    double tdx = dx / rp.splitx, tdy = dy / rp.splity;
+    rp.colxf.resize(rp.splitx);
+    rp.rowxf.resize(rp.splity);
+    for (int c = 0; c < rp.splitx; ++c) {
+        double lb = ctx->bbox[0] + c * tdx, rt = lb + tdx;
+        double origin = (rt + lb) / 2, half = (rt - lb) / 2;
+        float s = (float)(1.0 / half);
+        float t = s * (float)(-origin);
+        rp.colxf[c] = make_float4(s, t, rp.resx * 0.5f, (float)tdx);
+    }
+    for (int r = 0; r < rp.splity; ++r) {
+        double lb = ctx->bbox[1] + r * tdy, rt = lb + tdy;
+        double origin = (rt + lb) / 2, half = (rt - lb) / 2;
+        float s = (float)(1.0 / half);
+        float t = s * (float)(-origin);
+        rp.rowxf[r] = make_float4(s, t, rp.resy * 0.5f, (float)tdy);
+    }
+    return RJ_OK;
+}
+
+// Filter + aggregation (GLFunction::setupPoints GLFunction.cpp:199-344).
+int build_filter(rj_ctx* ctx, const rj_query* q, DevFilter& f, bool force_count) {
+    std::memset(&f, 0, sizeof f);
+    if (q->n_constraints < 0) return fail(ctx, RJ_E_INVALID, "negative constraint count");
+    if (q->n_constraints > RJ_MAX_CONSTRAINTS)
+        return fail(ctx, RJ_E_TOO_MANY_CONSTRAINTS, "%d constraints, at most %d supported", q->n_constraints,
+                    RJ_MAX_CONSTRAINTS);
+    int k = 0;
+    for (int i = 0; i < q->n_constraints; ++i) {
+        const rj_constraint& c = q->constraints[i];
+        const Column* col = find_col(ctx, c.attrib_id);
+        if (!col) return fail(ctx, RJ_E_INVALID, "constraint %d: unknown attribute %d", i, c.attrib_id);
+        if (col->type == RJ_LOCATION)
+            return fail(ctx, RJ_E_UNSUPPORTED, "constraint %d: location attributes cannot be filtered", i);
+        if (c.type < RJ_EQ || c.type > RJ_GTE)
+            return fail(ctx, RJ_E_INVALID, "constraint %d: bad constraint type %d", i, c.type);
+        f.col[k] = (const uint32_t*)col->d;
+        f.op[k] = c.type;
+        f.typ[k] = col->type;
+        f.val[k] = c.val.uval;
+        if (q->flags & RJ_FLAG_COMPAT_FLOAT_EQ) f.compat_mask |= 1u << k;
+        ++k;
+    }
+    if (q->time_attrib >= 0) {
+        const Column* col = find_col(ctx, q->time_attrib);
+        if (!col || col->type == RJ_LOCATION)
+            return fail(ctx, RJ_E_INVALID, "time attribute %d is not a loaded scalar column", q->time_attrib);
+        f.col[k] = (const uint32_t*)col->d; f.op[k] = RJ_GTE; f.typ[k] = col->type; f.val[k] = q->t_start; ++k;
+        f.col[k] = (const uint32_t*)col->d; f.op[k] = RJ_LTE; f.typ[k] = col->type; f.val[k] = q->t_end; ++k;
+    }
+    f.n = k;
+    if (!force_count && q->aggregation != RJ_COUNT) {
+        if (q->aggregation != RJ_AVG && q->aggregation != RJ_SUM)
+            return fail(ctx, RJ_E_INVALID, "bad aggregation %d", q->aggregation);
+        const Column* col = find_col(ctx, q->aggr_attrib);
+        if (!col) return fail(ctx, RJ_E_INVALID, "aggregation attribute %d not loaded", q->aggr_attrib);
+        if (col->type == RJ_LOCATION)
+            return fail(ctx, RJ_E_UNSUPPORTED, "cannot aggregate a location attribute");
+        f.aggr = 1;
+        f.aggr_typ = col->type;
+        f.aggr_col = (const uint32_t*)col->d;
+    }
+    return RJ_OK;
+}
+
+struct Phase {
+    rj_ctx* ctx;
+    bool on;
+    explicit Phase(rj_ctx* c, bool enabled) : ctx(c), on(enabled) {}
+    void mark(int i) {
+        if (on) cudaEventRecord(ctx->ev[i], ctx->stream);
+    }
+    double ms(int a, int b) {
+        if (!on) return 0.0;
+        float v = 0.f;
+        cudaEventElapsedTime(&v, ctx->ev[a], ctx->ev[b]);
+        return v;
+    }
+};
+
+// Window-space vertices of the polygon set for every canvas tile.
+int transform_vertices(rj_ctx* ctx, const std::vector<float4>& colxf, const std::vector<float4>& rowxf,
+                       int2** wv, float2** wf, bool want_float) {
+    const int T = (int)(colxf.size() * rowxf.size());
+    float4 *dcol, *drow;
+    int rc;
+    if ((rc = scratch_t(ctx, "colxf", colxf.size(), &dcol))) return rc;
+    if ((rc = scratch_t(ctx, "rowxf", rowxf.size(), &drow))) return rc;
+    RJ_CUDA(cudaMemcpyAsync(dcol, colxf.data(), colxf.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+    RJ_CUDA(cudaMemcpyAsync(drow, rowxf.data(), rowxf.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+    if ((rc = scratch_t(ctx, "wv", (size_t)T * ctx->V, wv))) return rc;
+    *wf = nullptr;
+    if (want_float && (rc = scratch_t(ctx, "wf", (size_t)T * ctx->V, wf))) return rc;
+    launch_transform_vertices((const float2*)ctx->d_verts.p, ctx->V, dcol, drow, (int)colxf.size(), T, *wv,
+                              want_float ? *wf : nullptr, ctx->sms, ctx->stream);
+    RJ_CUDA(cudaGetLastError());
+    return RJ_OK;
+}
+
+// Grid index (GLFunction::createPolyIndex GLFunction.cpp:65-156).
+int build_grid(rj_ctx* ctx, int res, int clamp, IndexArgs& ia) {
+    if (res <= 0 || res > 8192) return fail(ctx, RJ_E_INVALID, "grid resolution %d out of range", res);
+    GridCache& g = ctx->grid;
+    const double dx = ctx->bbox[2] - ctx->bbox[0], dy = ctx->bbox[3] - ctx->bbox[1];
+    const float lbx = (float)ctx->bbox[0], lby = (float)ctx->bbox[1];
+    const float csx = (float)(dx / res), csy = (float)(dy / res);
+    int *cell_start, *entries;
+    int rc;
+    const size_t ncells = (size_t)res * res;
+    if (!(g.valid && g.res == res && g.clamp == clamp)) {
+        int *cnt, *cursor, *tmp;
+        if ((rc = scratch_t(ctx, "grid_cnt", ncells, &cnt))) return rc;
+        if ((rc = scratch_t(ctx, "grid_start", ncells + 1, &cell_start))) return rc;
+        if ((rc = scratch_t(ctx, "grid_tmp", (size_t)scan_tmp_ints((int)ncells), &tmp))) return rc;
+        RJ_CUDA(cudaMemsetAsync(cnt, 0, ncells * sizeof(int), ctx->stream));
+        GridArgs ga{};
+        ga.verts = (const float2*)ctx->d_verts.p;
+        ga.pindex = (const int*)ctx->d_pindex.p;
+        ga.P = ctx->P;
+        ga.lbx = lbx; ga.lby = lby; ga.csx = csx; ga.csy = csy;
+        ga.res = res;
+        ga.compat_clamp = clamp;
+        ga.cell_count = cnt;
+        launch_grid_count(ga, ctx->sms, ctx->stream);
+        if (!launch_exclusive_scan(cnt, cell_start, (int)ncells, tmp, ctx->stream))
+            return fail(ctx, RJ_E_INVALID, "grid too large to scan");
+        int total = 0;
+        RJ_CUDA(cudaMemcpyAsync(&total, cell_start + ncells, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        if ((rc = scratch_t(ctx, "grid_entries", (size_t)std::max(total, 1), &entries))) return rc;
+        if ((rc = scratch_t(ctx, "grid_cursor", ncells, &cursor))) return rc;
+        RJ_CUDA(cudaMemsetAsync(cursor, 0, ncells * sizeof(int), ctx->stream));
+        ga.cell_start = cell_start;
+        ga.cursor = cursor;
+        ga.entries = entries;
+        launch_grid_fill(ga, ctx->sms, ctx->stream);
+        launch_grid_sort(cell_start, entries, (int)ncells, ctx->sms, ctx->stream);
+        RJ_CUDA(cudaGetLastError());
+        g.valid = true;
+        g.res = res;
+        g.clamp = clamp;
+        g.nentries = (size_t)total;
+    } else {
+        if ((rc = scratch_t(ctx, "grid_start", ncells + 1, &cell_start))) return rc;
+        if ((rc = scratch_t(ctx, "grid_entries", std::max<size_t>(g.nentries, 1), &entries))) return rc;
+    }
+    ia.verts = (const float2*)ctx->d_verts.p;
+    ia.pindex = (const int*)ctx->d_pindex.p;
+    ia.cell_start = cell_start;
+    ia.entries = entries;
+    ia.lbx = lbx; ia.lby = lby; ia.csx = csx; ia.csy = csy;
+    ia.res = res;
+    return RJ_OK;
+}
+
+PointArgs make_point_args(rj_ctx* ctx, const DevFilter& f, unsigned long long* oc, double* os) {
+    PointArgs pa{};
+    const Column* loc = find_col(ctx, ctx->loc_attrib);
+    pa.xy = (const float2*)loc->d;
+    pa.n = ctx->npts;
+    pa.f = f;
+    pa.P = ctx->P;
+    pa.out_count = oc;
+    pa.out_sum = os;
+    return pa;
+}
+
+CanvasXf make_canvas_xf(rj_ctx* ctx, const RasterPlan& rp, const float4* dcol, const float4* drow) {
+    CanvasXf cx{};
+    cx.colxf = dcol;
+    cx.rowxf = drow;
+    cx.splitx = rp.splitx;
+    cx.splity = rp.splity;
+    cx.resx = rp.resx;
+    cx.resy = rp.resy;
+    cx.lbx = (float)ctx->bbox[0];
+    cx.lby = (float)ctx->bbox[1];
+    cx.tdx = rp.colxf[0].w;
+    cx.tdy = rp.rowxf[0].w;
+    cx.col0 = rp.colxf[0];
+    cx.row0 = rp.rowxf[0];
+    return cx;
+}
+
+// ---------------------------------------------------------------------------
+// Join operators.  Each fills out_count / out_sum (and out_bounds) on device.
+struct ExecState {
+    unsigned long long* out_count;
+    double* out_sum;
+    long long* out_bounds;
+    Phase* ph;
+    int passes = 1;
+};
+
+int poly_pass(rj_ctx* ctx, int mode, PolyPassArgs& a) {
+    unsigned int* ctr;
+    int* flag;
+    int rc;
+    if ((rc = scratch_t(ctx, "work_ctr", 1, &ctr))) return rc;
+    if ((rc = scratch_t(ctx, "flag", 1, &flag))) return rc;
+    RJ_CUDA(cudaMemsetAsync(ctr, 0, sizeof(unsigned), ctx->stream));
+    RJ_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream));
+    a.work_ctr = ctr;
+    a.flag = flag;
+    launch_poly_pass(mode, a, ctx->sms, ctx->stream);
+    RJ_CUDA(cudaGetLastError());
+    return RJ_OK;
+}
+
+// Raster join (RasterJoin::performJoin RasterJoin.cpp:196-243) and the
+// error-bounds join (RasterJoinBounds::performJoin RasterJoinBounds.cpp:306-381).
+int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
+    int rc;
+    RasterPlan rp;
+    if ((rc = plan_raster(ctx, q, rp))) return rc;
+    DevFilter f;
+    if ((rc = build_filter(ctx, q, f, bounds))) return rc;   // bounds: count only (RasterJoinBounds.cpp:124)
+    const int T = rp.splitx * rp.splity;
+    const size_t tile_px = (size_t)rp.resx * rp.resy;
+    const size_t npix = tile_px * T;
+
+    es.ph->mark(1);
+    int2* wv;
+    float2* wf;
+    if ((rc = transform_vertices(ctx, rp.colxf, rp.rowxf, &wv, &wf, bounds))) return rc;
+    const float4* dcol = (const float4*)ctx->scratch["colxf"].p;
+    const float4* drow = (const float4*)ctx->scratch["rowxf"].p;
+    CanvasXf cx = make_canvas_xf(ctx, rp, dcol, drow);
+
+    PolyPassArgs a{};
+    a.wv = wv;
+    a.wf = wf;
+    a.pindex = (const int*)ctx->d_pindex.p;
+    a.P = ctx->P;
+    a.V = ctx->V;
+    a.T = T;
+    a.resx = rp.resx;
+    a.resy = rp.resy;
+    a.out_count = es.out_count;
+    a.out_sum = es.out_sum;
+    a.out_bounds = es.out_bounds;
+    a.line_filter = (q->flags & RJ_FLAG_LINE_FILTER) ? 1 : 0;
+
+    bool use_label = !bounds && !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->overlap_known != 1;
+    if (use_label) {
+        uint32_t* label;
+        if ((rc = scratch_t(ctx, "label", npix, &label))) return rc;
+        RJ_CUDA(cudaMemsetAsync(label, 0xFF, npix * sizeof(uint32_t), ctx->stream));
+        a.label = label;
+        if ((rc = poly_pass(ctx, MODE_LABEL, a))) return rc;
+        int flag = 0;
+        RJ_CUDA(cudaMemcpyAsync(&flag, a.flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (flag & 1) {
+            ctx->overlap_known = 1;
+            use_label = false;
+        } else {
+            ctx->overlap_known = 0;
+        }
+        es.ph->mark(2);
+        if (use_label) {
+            PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
+            launch_raster_label(pa, cx, label, ctx->sms, ctx->stream);
+            RJ_CUDA(cudaGetLastError());
+            es.ph->mark(3);
+            es.ph->mark(4);
+            return RJ_OK;
+        }
+    } else {
+        es.ph->mark(2);
+    }
+    // canvas path: point pass (additive splat) then polygon pass
+    uint32_t* canvas_c;
+    double* canvas_s = nullptr;
+    if ((rc = scratch_t(ctx, "canvas_c", npix, &canvas_c))) return rc;
+    RJ_CUDA(cudaMemsetAsync(canvas_c, 0, npix * sizeof(uint32_t), ctx->stream));
+    if (f.aggr) {
+        if ((rc = scratch_t(ctx, "canvas_s", npix, &canvas_s))) return rc;
+        RJ_CUDA(cudaMemsetAsync(canvas_s, 0, npix * sizeof(double), ctx->stream));
+    }
+    PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
+    launch_raster_splat(pa, cx, canvas_c, canvas_s, ctx->sms, ctx->stream);
+    RJ_CUDA(cudaGetLastError());
+    es.ph->mark(3);
+    a.canvas_c = canvas_c;
+    a.canvas_s = canvas_s;
+    a.label = nullptr;
+    if ((rc = poly_pass(ctx, bounds ? MODE_BOUNDS : MODE_REDUCE, a))) return rc;
+    es.ph->mark(4);
+    return RJ_OK;
+}
+
+// Index join (IndexJoin::performJoin IndexJoin.cpp:156-166).
+int exec_index(rj_ctx* ctx, const rj_query* q, ExecState& es) {
+    int rc;
+    DevFilter f;
+    if ((rc = build_filter(ctx, q, f, false))) return rc;
+    es.ph->mark(1);
+    IndexArgs ia{};
+    if ((rc = build_grid(ctx, q->grid_res, (q->flags & RJ_FLAG_COMPAT_INDEX_CLAMP) ? 1 : 0, ia))) return rc;
+    es.ph->mark(2);
+    PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
+    launch_index_points(pa, ia, ctx->sms, ctx->stream);
+    RJ_CUDA(cudaGetLastError());
+    es.ph->mark(3);
+    es.ph->mark(4);
+    return RJ_OK;
+}
+
+// Hybrid join (HybridJoin::performJoin HybridJoin.cpp:339-359).
+int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
+    int rc;
+    DevFilter f;
+    if ((rc = build_filter(ctx, q, f, false))) return rc;
+    es.ph->mark(1);
+    IndexArgs ia{};
+    if ((rc = build_grid(ctx, q->grid_res, 0, ia))) return rc;
+
+    // canvas: getResolution(bbox, 8192) (HybridJoin.cpp:62-66, Utils.h:29-34)
+    const double dx = ctx->bbox[2] - ctx->bbox[0], dy = ctx->bbox[3] - ctx->bbox[1];
+    const int fbo = q->hybrid_canvas > 0 ? q->hybrid_canvas : 8192;
+    const float cellf = (float)std::max(dx / fbo, dy / fbo);
+    const int resx = std::max(1, (int)std::fabs(std::ceil(dx / cellf)));
+    const int resy = std::max(1, (int)std::fabs(std::ceil(dy / cellf)));
+    HybXf h{};
+    {
+        float lbx = (float)ctx->bbox[0], lby = (float)ctx->bbox[1];
+        float rtx = (float)ctx->bbox[2], rty = (float)ctx->bbox[3];
+        volatile float sx = rtx + lbx, sy = rty + lby, qx = rtx - lbx, qy = rty - lby;
+        h.ox = sx / 2.0f;
+        h.oy = sy / 2.0f;
+        h.dx = qx / 2.0f;
+        h.dy = qy / 2.0f;
+        h.resx = resx;
+        h.resy = resy;
+    }
+    // border mask: conservative outline + dilation.  The dilation radius
+    // covers the fp32 error of the crossing test expressed in pixels.
+    const int words = (resx + 31) / 32;
+    uint32_t *mraw, *mask;
+    if ((rc = scratch_t(ctx, "hyb_mraw", (size_t)words * resy, &mraw))) return rc;
+    if ((rc = scratch_t(ctx, "hyb_mask", (size_t)words * resy, &mask))) return rc;
+    RJ_CUDA(cudaMemsetAsync(mraw, 0, (size_t)words * resy * 4, ctx->stream));
+    const double pix_w = std::min(dx / resx, dy / resy);
+    const double err_world = std::ldexp(1.0, -22) * (ctx->max_abs_coord + 6.0 * std::max(ctx->max_edge_dx, ctx->max_edge_dy) + 1.0);
+    const int radius = 1 + (int)std::ceil(err_world / pix_w + 0.1);
+    if (radius > 31) return fail(ctx, RJ_E_UNSUPPORTED, "hybrid canvas too fine for fp32 coordinates (radius %d)", radius);
+    launch_outline_mask((const float2*)ctx->d_verts.p, (const int*)ctx->d_pindex.p, ctx->P,
+                        (const int*)ctx->d_edge_poly.p, ctx->V, h, 0.05f, mraw, words, ctx->sms, ctx->stream);
+    launch_dilate_mask(mraw, mask, resx, resy, words, radius, ctx->sms, ctx->stream);
+    RJ_CUDA(cudaGetLastError());
+
+    // polygon coverage of the hybrid canvas (getMVP(bbox), HybridJoin.cpp:63)
+    std::vector<float4> colxf(1), rowxf(1);
+    {
+        double ox = (ctx->bbox[2] + ctx->bbox[0]) / 2, hx = (ctx->bbox[2] - ctx->bbox[0]) / 2;
+        double oy = (ctx->bbox[3] + ctx->bbox[1]) / 2, hy = (ctx->bbox[3] - ctx->bbox[1]) / 2;
+        float sx = (float)(1.0 / hx), sy = (float)(1.0 / hy);
+        colxf[0] = make_float4(sx, sx * (float)(-ox), resx * 0.5f, (float)dx);
+        rowxf[0] = make_float4(sy, sy * (float)(-oy), resy * 0.5f, (float)dy);
+    }
+    int2* wv;
+    float2* wf;
+    if ((rc = transform_vertices(ctx, colxf, rowxf, &wv, &wf, false))) return rc;
+    PolyPassArgs a{};
+    a.wv = wv;
+    a.pindex = (const int*)ctx->d_pindex.p;
+    a.P = ctx->P;
+    a.V = ctx->V;
+    a.T = 1;
+    a.resx = resx;
+    a.resy = resy;
+    a.out_count = es.out_count;
+    a.out_sum = es.out_sum;
+    const size_t npix = (size_t)resx * resy;
+
+    HybridArgs ha{};
+    ha.h = h;
+    ha.border = mask;
+    ha.words = words;
+    bool use_label = !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->overlap_known != 1;
+    if (use_label) {
+        uint32_t* label;
+        if ((rc = scratch_t(ctx, "hyb_label", npix, &label))) return rc;
+        RJ_CUDA(cudaMemsetAsync(label, 0xFF, npix * sizeof(uint32_t), ctx->stream));
+        a.label = label;
+        if ((rc = poly_pass(ctx, MODE_LABEL, a))) return rc;
+        int flag = 0;
+        RJ_CUDA(cudaMemcpyAsync(&flag, a.flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (flag & 1) {
+            ctx->overlap_known = 1;
+            use_label = false;
+        } else {
+            ctx->overlap_known = 0;
+            ha.label = label;
+        }
+    }
+    es.ph->mark(2);
+    PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
+    if (use_label) {
+        launch_hybrid_points(pa, ia, ha, ctx->sms, ctx->stream);
+        RJ_CUDA(cudaGetLastError());
+        es.ph->mark(3);
+        es.ph->mark(4);
+        return RJ_OK;
+    }
+    uint32_t* canvas_c;
+    double* canvas_s = nullptr;
+    if ((rc = scratch_t(ctx, "hyb_canvas_c", npix, &canvas_c))) return rc;
+    RJ_CUDA(cudaMemsetAsync(canvas_c, 0, npix * sizeof(uint32_t), ctx->stream));
+    if (f.aggr) {
+        if ((rc = scratch_t(ctx, "hyb_canvas_s", npix, &canvas_s))) return rc;
+        RJ_CUDA(cudaMemsetAsync(canvas_s, 0, npix * sizeof(double), ctx->stream));
+    }
+    ha.canvas_c = canvas_c;
+    ha.canvas_s = canvas_s;
+    ha.label = nullptr;
+    launch_hybrid_points(pa, ia, ha, ctx->sms, ctx->stream);
+    RJ_CUDA(cudaGetLastError());
+    es.ph->mark(3);
+    // polygon-inside pass over non-border pixels (polygon-inside.frag:30-57)
+    a.label = nullptr;
+    a.canvas_c = canvas_c;
+    a.canvas_s = canvas_s;
+    a.border = mask;
+    a.border_words = words;
+    if ((rc = poly_pass(ctx, MODE_REDUCE, a))) return rc;
+    es.ph->mark(4);
+    return RJ_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+extern "C" {
+
+int rj_abi_version(void) { return RJ_ABI_VERSION; }
+
+void rj_query_init(rj_query* q) {
+    if (!q) return;
+    std::memset(q, 0, sizeof *q);
+    q->function_type = RJ_RASTER_JOIN;
+    q->aggregation = RJ_COUNT;
+    q->aggr_attrib = -1;
+    q->accuracy_m = 100.0;
+    q->ground_resolution = 1.0;
+    q->grid_res = 256;
+    q->max_fbo_size = RJ_MAX_FBO_SIZE;
+    q->time_attrib = -1;
+    q->hybrid_canvas = 8192;
+}
+
+int rj_create(const rj_config* cfg, rj_ctx** out) {
+    if (!out) return RJ_E_INVALID;
+    *out = nullptr;
+    rj_ctx* ctx = new rj_ctx();
+    int dev = cfg ? cfg->device : 0;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        delete ctx;
+        return RJ_E_CUDA;
+    }
+    if (dev < 0 || dev >= ndev) {
+        delete ctx;
+        return RJ_E_INVALID;
+    }
+    ctx->device = dev;
+    if (cudaSetDevice(dev) != cudaSuccess) {
+        delete ctx;
+        return RJ_E_CUDA;
+    }
+    cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cfg && cfg->gpu_mem_mb > 0) ctx->budget = cfg->gpu_mem_mb * 1024LL * 1024LL;
+    if (cfg && cfg->stream) {
+        ctx->stream = (cudaStream_t)cfg->stream;
+    } else {
+        cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+        ctx->own_stream = true;
+    }
+    for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+    *out = ctx;
+    return RJ_OK;
+}
+
+void rj_destroy(rj_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_points(ctx);
+    dev_free(ctx, ctx->d_verts);
+    dev_free(ctx, ctx->d_pindex);
+    dev_free(ctx, ctx->d_edge_poly);
+    for (auto& kv : ctx->scratch) dev_free(ctx, kv.second);
+    for (auto& ev : ctx->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* rj_last_error(const rj_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int rj_set_stream(rj_ctx* ctx, void* stream) {
+    if (!ctx) return RJ_E_INVALID;
+    cudaSetDevice(ctx->device);
+    if (ctx->own_stream && ctx->stream) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaStreamDestroy(ctx->stream);
+        ctx->own_stream = false;
+    }
+    if (stream) {
+        ctx->stream = (cudaStream_t)stream;
+    } else {
+        cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+        ctx->own_stream = true;
+    }
+    return RJ_OK;
+}
+
+static int load_points_impl(rj_ctx* ctx, const rj_column* cols, int32_t ncols, uint64_t npoints, int32_t loc,
+                            bool device) {
+    if (!ctx) return RJ_E_INVALID;
+    ctx->err.clear();
+    if (!cols || ncols <= 0 || ncols > RJ_MAX_ATTRIBUTES)
+        return fail(ctx, RJ_E_INVALID, "ncols must be 1..%d", RJ_MAX_ATTRIBUTES);
+    int nloc = 0;
+    for (int i = 0; i < ncols; ++i) {
+        if (cols[i].type < RJ_LOCATION || cols[i].type > RJ_FLOAT)
+            return fail(ctx, RJ_E_INVALID, "column %d: bad type %d", i, cols[i].type);
+        if (!cols[i].data && npoints) return fail(ctx, RJ_E_INVALID, "column %d: null data", i);
+        for (int j = 0; j < i; ++j)
+            if (cols[j].attrib_id == cols[i].attrib_id)
+                return fail(ctx, RJ_E_INVALID, "duplicate attribute id %d", cols[i].attrib_id);
+        if (cols[i].attrib_id == loc) {
+            if (cols[i].type != RJ_LOCATION) return fail(ctx, RJ_E_INVALID, "location attribute must have type LOCATION");
+            ++nloc;
+        }
+        if (device && ((uintptr_t)cols[i].data & 15))
+            return fail(ctx, RJ_E_INVALID, "column %d: device pointer not 16-byte aligned", i);
+    }
+    if (nloc != 1) return fail(ctx, RJ_E_INVALID, "location attribute %d not among the columns", loc);
+    cudaSetDevice(ctx->device);
+    // same layout as the resident table: copy into the existing buffers
+    bool same = !device && (int)ctx->cols.size() == ncols && ctx->npts == npoints && ctx->loc_attrib == loc;
+    for (int i = 0; same && i < ncols; ++i)
+        same = ctx->cols[i].owned && ctx->cols[i].attrib == cols[i].attrib_id && ctx->cols[i].type == cols[i].type;
+    if (same) {
+        for (int i = 0; i < ncols; ++i) {
+            const size_t esz = cols[i].type == RJ_LOCATION ? 8 : 4;
+            if (npoints)
+                RJ_CUDA(cudaMemcpyAsync(ctx->cols[i].d, cols[i].data, esz * npoints, cudaMemcpyHostToDevice, ctx->stream));
+        }
+        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        return RJ_OK;
+    }
+    // release the previous table
+    for (Column& c : ctx->cols) {
+        if (c.owned && c.d) {
+            cudaFree(c.d);
+            ctx->used -= (c.type == RJ_LOCATION ? 8 : 4) * ((ctx->npts + 3) & ~3ULL) + 256;
+        }
+    }
+    ctx->cols.clear();
+    ctx->npts = 0;
+    ctx->loc_attrib = -1;
+    for (int i = 0; i < ncols; ++i) {
+        Column c;
+        c.attrib = cols[i].attrib_id;
+        c.type = cols[i].type;
+        const size_t esz = c.type == RJ_LOCATION ? 8 : 4;
+        if (device) {
+            c.d = const_cast<void*>(cols[i].data);
+            c.owned = false;
+        } else {
+            // padded to a multiple of four points so 128-bit loads stay in bounds
+            const size_t bytes = esz * ((npoints + 3) & ~3ULL) + 256;
+            if (ctx->budget > 0 && (int64_t)(ctx->used + bytes) > ctx->budget) {
+                for (Column& o : ctx->cols) if (o.owned) cudaFree(o.d);
+                ctx->cols.clear();
+                return fail(ctx, RJ_E_OOM, "point table exceeds the device memory budget");
+            }
+            cudaError_t e = cudaMalloc(&c.d, bytes);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                for (Column& o : ctx->cols) if (o.owned) cudaFree(o.d);
+                ctx->cols.clear();
+                return fail(ctx, RJ_E_OOM, "cudaMalloc for column %d failed: %s", i, cudaGetErrorString(e));
+            }
+            ctx->used += bytes;
+            c.owned = true;
+            if (npoints) RJ_CUDA(cudaMemcpyAsync(c.d, cols[i].data, esz * npoints, cudaMemcpyHostToDevice, ctx->stream));
+        }
+        ctx->cols.push_back(c);
+    }
+    ctx->npts = npoints;
+    ctx->loc_attrib = loc;
+    RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    return RJ_OK;
+}
+
+int rj_load_points(rj_ctx* ctx, const rj_column* cols, int32_t ncols, uint64_t npoints, int32_t loc_attrib) {
+    return load_points_impl(ctx, cols, ncols, npoints, loc_attrib, false);
+}
+
+int rj_attach_points_device(rj_ctx* ctx, const rj_column* cols, int32_t ncols, uint64_t npoints,
+                            int32_t loc_attrib) {
+    return load_points_impl(ctx, cols, ncols, npoints, loc_attrib, true);
+}
+
+int rj_free_points(rj_ctx* ctx) {
+    if (!ctx) return RJ_E_INVALID;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (Column& c : ctx->cols) {
+        if (c.owned && c.d) {
+            cudaFree(c.d);
+            ctx->used -= (c.type == RJ_LOCATION ? 8 : 4) * ((ctx->npts + 3) & ~3ULL) + 256;
+        }
+    }
+    ctx->cols.clear();
+    ctx->npts = 0;
+    ctx->loc_attrib = -1;
+    return RJ_OK;
+}
+
+int rj_set_polygons(rj_ctx* ctx, const float* xy, const int32_t* pindex, int32_t npolys, const double* bbox) {
+    if (!ctx) return RJ_E_INVALID;
+    ctx->err.clear();
+    if (npolys <= 0 || !pindex || !xy) return fail(ctx, RJ_E_INVALID, "empty polygon set");
+    if (pindex[0] != 0) return fail(ctx, RJ_E_INVALID, "pindex[0] must be 0");
+    for (int i = 0; i < npolys; ++i)
+        if (pindex[i + 1] < pindex[i]) return fail(ctx, RJ_E_INVALID, "pindex not monotone at %d", i);
+    const int V = pindex[npolys];
+    double bb[4] = {INFINITY, INFINITY, -INFINITY, -INFINITY};
+    float maxabs = 0.f, mdx = 0.f, mdy = 0.f;
+    for (int i = 0; i < npolys; ++i) {
+        const int v0 = pindex[i], n = pindex[i + 1] - v0;
+        for (int k = 0; k < n; ++k) {
+            float x = xy[2 * (v0 + k)], y = xy[2 * (v0 + k) + 1];
+            if (!std::isfinite(x) || !std::isfinite(y)) return fail(ctx, RJ_E_INVALID, "non-finite vertex in polygon %d", i);
+            bb[0] = std::min(bb[0], (double)x); bb[1] = std::min(bb[1], (double)y);
+            bb[2] = std::max(bb[2], (double)x); bb[3] = std::max(bb[3], (double)y);
+            maxabs = std::max(maxabs, std::max(std::fabs(x), std::fabs(y)));
+            int kn = (k + 1 == n) ? 0 : k + 1;
+            mdx = std::max(mdx, std::fabs(xy[2 * (v0 + kn)] - x));
+            mdy = std::max(mdy, std::fabs(xy[2 * (v0 + kn) + 1] - y));
+        }
+    }
+    if (bbox) {
+        for (int i = 0; i < 4; ++i) bb[i] = bbox[i];
+        maxabs = std::max(maxabs, (float)std::max(std::max(std::fabs(bb[0]), std::fabs(bb[1])),
+                                                   std::max(std::fabs(bb[2]), std::fabs(bb[3]))));
+    }
+    if (!(bb[2] > bb[0] && bb[3] > bb[1]))
+        return fail(ctx, RJ_E_INVALID, "polygon bounds are empty");   // CPUJoin.cpp:51-54
+    cudaSetDevice(ctx->device);
+    int rc;
+    if ((rc = dev_alloc(ctx, ctx->d_verts, (size_t)V * 8))) return rc;
+    if ((rc = dev_alloc(ctx, ctx->d_pindex, (size_t)(npolys + 1) * 4))) return rc;
+    if ((rc = dev_alloc(ctx, ctx->d_edge_poly, (size_t)V * 4))) return rc;
+    std::vector<int> edge_poly(V);
+    for (int i = 0; i < npolys; ++i)
+        for (int k = pindex[i]; k < pindex[i + 1]; ++k) edge_poly[k] = i;
+    ctx->h_xy.assign(xy, xy + 2 * (size_t)V);
+    ctx->h_pindex.assign(pindex, pindex + npolys + 1);
+    RJ_CUDA(cudaMemcpyAsync(ctx->d_verts.p, xy, (size_t)V * 8, cudaMemcpyHostToDevice, ctx->stream));
+    RJ_CUDA(cudaMemcpyAsync(ctx->d_pindex.p, pindex, (size_t)(npolys + 1) * 4, cudaMemcpyHostToDevice, ctx->stream));
+    RJ_CUDA(cudaMemcpyAsync(ctx->d_edge_poly.p, edge_poly.data(), (size_t)V * 4, cudaMemcpyHostToDevice, ctx->stream));
+    RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->P = npolys;
+    ctx->V = V;
+    for (int i = 0; i < 4; ++i) ctx->bbox[i] = bb[i];
+    ctx->max_abs_coord = maxabs;
+    ctx->max_edge_dx = mdx;
+    ctx->max_edge_dy = mdy;
+    ctx->poly_version++;
+    ctx->overlap_known = -1;
+    ctx->grid.valid = false;
+    return RJ_OK;
+}
+
+int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
+    if (!ctx || !q) return RJ_E_INVALID;
+    ctx->err.clear();
+    const double t0 = now_ms();
+    if (ctx->npts == 0 && ctx->cols.empty()) return fail(ctx, RJ_E_NO_DATA, "point table not loaded");
+    if (ctx->P == 0) return fail(ctx, RJ_E_NO_DATA, "polygons not set");
+    if (res && res->npolys != 0 && res->npolys != ctx->P)
+        return fail(ctx, RJ_E_INVALID, "result sized for %d polygons, polygon set has %d", res->npolys, ctx->P);
+    if (q->function_type < RJ_RASTER_JOIN || q->function_type > RJ_RASTER_JOIN_BOUNDS)
+        return fail(ctx, RJ_E_UNSUPPORTED, "function type %d not supported", q->function_type);   // GLHandler.cpp:201
+    cudaSetDevice(ctx->device);
+    int rc;
+    const int P = ctx->P;
+    if (q->flags & RJ_FLAG_NO_CACHE) {
+        ctx->grid.valid = false;
+        ctx->overlap_known = -1;
+    }
+    g_kernel_launches = 0;
+    unsigned long long* oc;
+    double* os;
+    long long* ob;
+    if ((rc = scratch_t(ctx, "out_count", P, &oc))) return rc;
+    if ((rc = scratch_t(ctx, "out_sum", P, &os))) return rc;
+    if ((rc = scratch_t(ctx, "out_bounds", (size_t)4 * P, &ob))) return rc;
+    Phase ph(ctx, (q->flags & RJ_FLAG_PHASE_TIMING) != 0);
+    ph.mark(0);
+    RJ_CUDA(cudaMemsetAsync(oc, 0, P * sizeof(unsigned long long), ctx->stream));
+    RJ_CUDA(cudaMemsetAsync(os, 0, P * sizeof(double), ctx->stream));
+    RJ_CUDA(cudaMemsetAsync(ob, 0, (size_t)4 * P * sizeof(long long), ctx->stream));
+    ExecState es{oc, os, ob, &ph};
+    const double t_setup = now_ms();
+    switch (q->function_type) {
+        case RJ_RASTER_JOIN: rc = exec_raster(ctx, q, es, false); break;
+        case RJ_INDEX_JOIN: rc = exec_index(ctx, q, es); break;
+        case RJ_HYBRID_JOIN: rc = exec_hybrid(ctx, q, es); break;
+        default: rc = exec_raster(ctx, q, es, true); break;
+    }
+    if (rc) {
+        cudaStreamSynchronize(ctx->stream);
+        return rc;
+    }
+    std::vector<unsigned long long> hc(P);
+    std::vector<double> hs(P);
+    std::vector<long long> hb;
+    RJ_CUDA(cudaMemcpyAsync(hc.data(), oc, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    RJ_CUDA(cudaMemcpyAsync(hs.data(), os, P * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (q->function_type == RJ_RASTER_JOIN_BOUNDS && res && res->bounds) {
+        hb.resize((size_t)4 * P);
+        RJ_CUDA(cudaMemcpyAsync(hb.data(), ob, (size_t)4 * P * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    ph.mark(5);
+    RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    RJ_CUDA(cudaGetLastError());
+    if (res) {
+        if (res->count) for (int i = 0; i < P; ++i) res->count[i] = hc[i];
+        if (res->sum) for (int i = 0; i < P; ++i) res->sum[i] = hs[i];
+        if (res->compat3) {
+            for (int i = 0; i < P; ++i) {
+                // [count | sum/100 | decimal*10], decodable by printResults (main.cpp:206-208)
+                double s = hs[i];
+                double hi = std::trunc(s / 100.0);
+                double lo = std::nearbyint((s - 100.0 * hi) * 10.0);
+                res->compat3[i] = (int32_t)std::min<unsigned long long>(hc[i], 0x7fffffffULL);
+                res->compat3[P + i] = (int32_t)std::max(-2147483647.0, std::min(2147483647.0, hi));
+                res->compat3[2 * P + i] = (int32_t)lo;
+            }
+        }
+        if (res->bounds) {
+            for (size_t i = 0; i < (size_t)4 * P; ++i) res->bounds[i] = hb.empty() ? 0 : (int32_t)std::min<long long>(hb[i], 0x7fffffffLL);
+        }
+    }
+    // timings (GLHandler::printTimeStats fields)
+    rj_timings& t = ctx->tm;
+    std::memset(&t, 0, sizeof t);
+    t.pts_size = ctx->npts;
+    t.poly_size = P;
+    t.function = q->function_type;
+    t.no_pt_passes = 1;
+    t.no_constraints = q->n_constraints;
+    t.setup_ms = t_setup - t0;
+    t.poly_index_ms = (q->function_type == RJ_INDEX_JOIN || q->function_type == RJ_HYBRID_JOIN) ? ph.ms(1, 2) : 0.0;
+    t.poly_render_ms = (q->function_type == RJ_INDEX_JOIN || q->function_type == RJ_HYBRID_JOIN) ? ph.ms(3, 4) : ph.ms(1, 2) + ph.ms(3, 4);
+    t.pt_render_ms = ph.ms(2, 3);
+    t.poly_mem_ms = ph.ms(4, 5);
+    t.execute_ms = now_ms() - t0;
+    t.accuracy = (q->function_type == RJ_RASTER_JOIN) ? (int)q->accuracy_m : 0;
+    t.kernel_launches = g_kernel_launches;
+    return RJ_OK;
+}
+
+int rj_get_timings(const rj_ctx* ctx, rj_timings* out) {
+    if (!ctx || !out) return RJ_E_INVALID;
+    *out = ctx->tm;
+    return RJ_OK;
+}
+
+int rj_format_time_stats(const rj_ctx* ctx, char* buf, size_t buflen) {
+    if (!ctx || !buf || buflen == 0) return RJ_E_INVALID;
+    const rj_timings& t = ctx->tm;
+    const int fn = t.function == RJ_RASTER_JOIN_BOUNDS ? 5 : t.function;   // GLHandler.cpp:228
+    snprintf(buf, buflen, "%llu\t\t%d\t%d\t%d\t%d\t%lld\t%lld\t%lld\t%lld\t%lld\t%lld\t%lld\t%lld\t%lld\t%d",
+             (unsigned long long)t.pts_size, t.poly_size, fn, t.no_pt_passes, t.no_constraints,
+             (long long)std::llround(t.execute_ms), (long long)std::llround(t.pt_mem_ms),
+             (long long)std::llround(t.pt_render_ms), (long long)std::llround(t.poly_mem_ms),
+             (long long)std::llround(t.poly_render_ms), (long long)std::llround(t.setup_ms),
+             (long long)std::llround(t.triangulation_ms), (long long)std::llround(t.poly_index_ms),
+             (long long)std::llround(t.backend_query_ms), t.accuracy);
+    return RJ_OK;
+}
+
+}  // extern "C"

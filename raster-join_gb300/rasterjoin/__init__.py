@@ -1,0 +1,373 @@
+"""Python binding of librj.so (the C ABI in include/rj.h), via ctypes.
+
+The class :class:`GLHandler` mirrors the reference's join dispatcher
+(RasterJoin/join/GLHandler.hpp:20-78) and :class:`DataHandler` its query/data
+holder (RasterJoin/db/DataHandler.hpp:14-41): same method names, same argument
+meaning, results returned as the reference's flat int32 vector
+``[count | sum/100 | decimal*10]`` (GLFunction.cpp:42) plus exact numpy views.
+
+The binding never computes a join itself: when librj.so is missing or no CUDA
+device is present, constructing a handler raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_PKG = os.path.dirname(_HERE)
+LIB_PATH = os.path.join(_PKG, "lib", "librj.so")
+
+# ---- enums (values identical to the reference) ------------------------------
+# GLHandler::FunctionType, GLHandler.hpp:23-29
+RasterJoinFn, IndexJoinFn, HybridJoinFn, RasterJoinBoundFn = 0, 1, 2, 3
+# Aggregation, Common.h:34
+Count, Avg, Sum = 0, 1, 2
+# ConstraintType, Common.h:30
+EQ, LT, LTE, GT, GTE = 0, 1, 2, 3, 4
+# AttributeType, Common.h:28
+Location, Uint, Int, Float = 0, 1, 2, 3
+
+RJ_OK = 0
+STATUS = {0: "RJ_OK", -1: "RJ_E_INVALID", -2: "RJ_E_OOM", -3: "RJ_E_TOO_MANY_CONSTRAINTS",
+          -4: "RJ_E_TIMEOUT", -5: "RJ_E_CUDA", -6: "RJ_E_NO_DATA", -7: "RJ_E_UNSUPPORTED",
+          -8: "RJ_E_BUSY"}
+MAX_CONSTRAINTS = 10
+
+FLAG_COMPAT_INDEX_CLAMP = 0x1
+FLAG_COMPAT_FLOAT_EQ = 0x2
+FLAG_LINE_FILTER = 0x4
+FLAG_FORCE_CANVAS = 0x8
+FLAG_PHASE_TIMING = 0x10
+FLAG_NO_CELL_CLASSIFY = 0x20
+FLAG_NO_CACHE = 0x40
+
+
+class RJError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (STATUS.get(code, "?"), code, msg))
+        self.code = code
+
+
+# ---- C structs ---------------------------------------------------------------
+class Value(C.Union):
+    _fields_ = [("ival", C.c_int32), ("fval", C.c_float), ("uval", C.c_uint32)]
+
+
+class QueryConstraint(C.Structure):
+    """QueryConstraint, Common.h:42-47 (16 bytes)."""
+    _fields_ = [("attribId", C.c_int32), ("type", C.c_int32), ("val", Value), ("dummy", C.c_int32)]
+
+
+class Query(C.Structure):
+    _fields_ = [("function_type", C.c_int32), ("aggregation", C.c_int32), ("aggr_attrib", C.c_int32),
+                ("n_constraints", C.c_int32), ("constraints", QueryConstraint * MAX_CONSTRAINTS),
+                ("accuracy_m", C.c_double), ("cell_size", C.c_double), ("ground_resolution", C.c_double),
+                ("grid_res", C.c_int32), ("max_fbo_size", C.c_int32), ("time_attrib", C.c_int32),
+                ("t_start", C.c_uint32), ("t_end", C.c_uint32), ("hybrid_canvas", C.c_int32),
+                ("flags", C.c_uint32)]
+
+
+class Result(C.Structure):
+    _fields_ = [("npolys", C.c_int32), ("count", C.POINTER(C.c_uint64)), ("sum", C.POINTER(C.c_double)),
+                ("compat3", C.POINTER(C.c_int32)), ("bounds", C.POINTER(C.c_int32))]
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int32), ("gpu_mem_mb", C.c_int64), ("stream", C.c_void_p)]
+
+
+class Column(C.Structure):
+    _fields_ = [("attrib_id", C.c_int32), ("type", C.c_int32), ("data", C.c_void_p)]
+
+
+class Timings(C.Structure):
+    _fields_ = [("pts_size", C.c_uint64), ("poly_size", C.c_int32), ("function", C.c_int32),
+                ("no_pt_passes", C.c_int32), ("no_constraints", C.c_int32), ("execute_ms", C.c_double),
+                ("pt_mem_ms", C.c_double), ("pt_render_ms", C.c_double), ("poly_mem_ms", C.c_double),
+                ("poly_render_ms", C.c_double), ("setup_ms", C.c_double), ("triangulation_ms", C.c_double),
+                ("poly_index_ms", C.c_double), ("backend_query_ms", C.c_double), ("accuracy", C.c_int32),
+                ("kernel_launches", C.c_int32)]
+
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Load librj.so and declare every entry point of include/rj.h."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("librj.so not built (%s); run __graft_entry__.build()" % path)
+    lib = C.CDLL(path)
+    P = C.POINTER
+    sig = {
+        "rj_abi_version": (C.c_int, []),
+        "rj_query_init": (None, [P(Query)]),
+        "rj_create": (C.c_int, [P(Config), P(C.c_void_p)]),
+        "rj_destroy": (None, [C.c_void_p]),
+        "rj_last_error": (C.c_char_p, [C.c_void_p]),
+        "rj_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+        "rj_load_points": (C.c_int, [C.c_void_p, P(Column), C.c_int32, C.c_uint64, C.c_int32]),
+        "rj_attach_points_device": (C.c_int, [C.c_void_p, P(Column), C.c_int32, C.c_uint64, C.c_int32]),
+        "rj_free_points": (C.c_int, [C.c_void_p]),
+        "rj_set_polygons": (C.c_int, [C.c_void_p, P(C.c_float), P(C.c_int32), C.c_int32, P(C.c_double)]),
+        "rj_execute": (C.c_int, [C.c_void_p, P(Query), P(Result)]),
+        "rj_get_timings": (C.c_int, [C.c_void_p, P(Timings)]),
+        "rj_format_time_stats": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def default_query():
+    q = Query()
+    load_library().rj_query_init(C.byref(q))
+    return q
+
+
+def constraint(attrib_id, ctype, value, attr_type):
+    """QueryConstraint with the value stored by the column's type (Value union)."""
+    c = QueryConstraint()
+    c.attribId = attrib_id
+    c.type = ctype
+    if attr_type == Float:
+        c.val.fval = float(value)
+    elif attr_type == Int:
+        c.val.ival = int(value)
+    else:
+        c.val.uval = int(value) & 0xFFFFFFFF
+    c.dummy = 0
+    return c
+
+
+class JoinResult:
+    """Per-polygon results of one execute call."""
+
+    def __init__(self, count, sum_, compat3, bounds):
+        self.count = count
+        self.sum = sum_
+        self.compat3 = compat3
+        self.bounds = bounds
+
+    @property
+    def avg(self):
+        with np.errstate(invalid="ignore", divide="ignore"):
+            return np.where(self.count > 0, self.sum / np.maximum(self.count, 1), 0.0)
+
+
+class DataHandler:
+    """Point columns, polygons, constraints and aggregation of a query
+    (DataHandler.hpp:14-41)."""
+
+    def __init__(self):
+        self.columns = {}          # attrib id -> (type, ndarray)
+        self.location_attribute = None
+        self.polys = None          # (xy float32 [V,2], pindex int32 [P+1])
+        self.bbox = None
+        self.constraints = []
+        self.aggr = Count
+        self.aggr_attrib = -1
+        self.time_range = None     # (attrib, start, end)
+
+    def add_column(self, attrib_id, attr_type, data):
+        if attr_type == Location:
+            data = np.ascontiguousarray(data, dtype=np.float32).reshape(-1, 2)
+            self.location_attribute = attrib_id
+        elif attr_type == Float:
+            data = np.ascontiguousarray(data, dtype=np.float32)
+        elif attr_type == Int:
+            data = np.ascontiguousarray(data, dtype=np.int32)
+        else:
+            data = np.ascontiguousarray(data, dtype=np.uint32)
+        self.columns[attrib_id] = (attr_type, data)
+
+    def setPolygons(self, xy, pindex, bbox=None):
+        self.polys = (np.ascontiguousarray(xy, dtype=np.float32).reshape(-1, 2),
+                      np.ascontiguousarray(pindex, dtype=np.int32))
+        self.bbox = None if bbox is None else np.asarray(bbox, dtype=np.float64)
+
+    def setQueryConstraints(self, constraints):
+        """constraints: list of (attrib_id, ConstraintType, value)."""
+        self.constraints = list(constraints)
+
+    def setAggregation(self, aggr=Count, attrib_id=-1):
+        self.aggr = aggr
+        self.aggr_attrib = attrib_id
+
+    def setTimeRange(self, attrib_id, start, end):
+        self.time_range = None if attrib_id is None else (attrib_id, start, end)
+
+    def attr_type(self, attrib_id):
+        return self.columns[attrib_id][0]
+
+
+class GLHandler:
+    """Join dispatcher over one CUDA device (GLHandler.hpp:20-78).
+
+    getInstance(gpuMemMB) -> handler; setDataHandler; setAccuracyDistance;
+    setPolyIndexResolution; executeFunction(FunctionType) -> int32[3P];
+    getErrorBounds(FunctionType) -> int32[4P]; printTimeStats.
+    """
+
+    def __init__(self, gpu_mem_mb=0, device=0, stream=None):
+        self.lib = load_library()
+        cfg = Config(device, gpu_mem_mb, stream)
+        h = C.c_void_p()
+        rc = self.lib.rj_create(C.byref(cfg), C.byref(h))
+        if rc != RJ_OK:
+            raise RJError(rc, "rj_create failed (no CUDA device?)")
+        self.ctx = h
+        self.dataHandler = None
+        self.accuracy = 100.0
+        self.cell_size = 0.0
+        self.ground_resolution = 1.0
+        self.presx = 256
+        self.max_fbo_size = 8192
+        self.hybrid_canvas = 8192
+        self.flags = 0
+        self._loaded_points = None
+        self._loaded_polys = None
+        self.bounds = None
+        self.last = None
+
+    @classmethod
+    def getInstance(cls, gpuMemMB=2048, inMemory=True):
+        return cls(gpu_mem_mb=gpuMemMB)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.rj_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != RJ_OK:
+            raise RJError(rc, self.lib.rj_last_error(self.ctx).decode())
+
+    # ---- configuration (GLHandler.cpp:250-262) ----
+    def setDataHandler(self, dh):
+        self.dataHandler = dh
+
+    def setAccuracyDistance(self, metres):
+        self.accuracy = float(metres)
+        self.cell_size = 0.0
+
+    def setCellSize(self, cell):
+        self.cell_size = float(cell)
+
+    def setPolyIndexResolution(self, resx, resy=None):
+        self.presx = int(resx)   # only x is used (GLFunction.cpp:76)
+
+    def setStream(self, stream_ptr):
+        self._check(self.lib.rj_set_stream(self.ctx, C.c_void_p(stream_ptr)))
+
+    # ---- data upload ----
+    def upload(self, force=False):
+        dh = self.dataHandler
+        if dh is None:
+            raise RJError(-6, "DataHandler not set")
+        key = tuple((k, id(v[1])) for k, v in sorted(dh.columns.items()))
+        if force or key != self._loaded_points:
+            cols = (Column * len(dh.columns))()
+            n = None
+            for i, (aid, (typ, arr)) in enumerate(sorted(dh.columns.items())):
+                cols[i].attrib_id = aid
+                cols[i].type = typ
+                cols[i].data = arr.ctypes.data
+                m = arr.shape[0]
+                n = m if n is None else n
+                if m != n:
+                    raise RJError(-1, "columns have different lengths")
+            self._check(self.lib.rj_load_points(self.ctx, cols, len(dh.columns), n or 0,
+                                                dh.location_attribute))
+            self._loaded_points = key
+        pkey = (id(dh.polys[0]), id(dh.polys[1]), None if dh.bbox is None else tuple(dh.bbox))
+        if force or pkey != self._loaded_polys:
+            xy, pidx = dh.polys
+            bb = None
+            if dh.bbox is not None:
+                bb = (C.c_double * 4)(*dh.bbox)
+            self._check(self.lib.rj_set_polygons(self.ctx, xy.ctypes.data_as(C.POINTER(C.c_float)),
+                                                 pidx.ctypes.data_as(C.POINTER(C.c_int32)), len(pidx) - 1,
+                                                 bb))
+            self._loaded_polys = pkey
+
+    def make_query(self, fn):
+        dh = self.dataHandler
+        q = default_query()
+        q.function_type = fn
+        q.aggregation = dh.aggr
+        q.aggr_attrib = dh.aggr_attrib
+        if len(dh.constraints) > MAX_CONSTRAINTS:
+            q.n_constraints = len(dh.constraints)
+        else:
+            q.n_constraints = len(dh.constraints)
+            for i, (aid, ct, val) in enumerate(dh.constraints):
+                q.constraints[i] = constraint(aid, ct, val, dh.attr_type(aid) if aid in dh.columns else Uint)
+        q.accuracy_m = self.accuracy
+        q.cell_size = self.cell_size
+        q.ground_resolution = self.ground_resolution
+        q.grid_res = self.presx
+        q.max_fbo_size = self.max_fbo_size
+        q.hybrid_canvas = self.hybrid_canvas
+        if dh.time_range is not None:
+            q.time_attrib, q.t_start, q.t_end = dh.time_range
+        q.flags = self.flags
+        return q
+
+    def execute(self, fn, query=None):
+        """Run one join; returns JoinResult with exact arrays."""
+        self.upload()
+        q = query if query is not None else self.make_query(fn)
+        P = len(self.dataHandler.polys[1]) - 1
+        count = np.zeros(P, np.uint64)
+        sum_ = np.zeros(P, np.float64)
+        compat3 = np.zeros(3 * P, np.int32)
+        bounds = np.zeros(4 * P, np.int32)
+        r = Result(P, count.ctypes.data_as(C.POINTER(C.c_uint64)), sum_.ctypes.data_as(C.POINTER(C.c_double)),
+                   compat3.ctypes.data_as(C.POINTER(C.c_int32)), bounds.ctypes.data_as(C.POINTER(C.c_int32)))
+        self._check(self.lib.rj_execute(self.ctx, C.byref(q), C.byref(r)))
+        self.last = JoinResult(count, sum_, compat3, bounds if fn == RasterJoinBoundFn else None)
+        self.bounds = bounds if fn == RasterJoinBoundFn else None
+        return self.last
+
+    def executeFunction(self, fn):
+        """GLHandler::executeFunction (GLHandler.cpp:188-204): int32[3P]."""
+        return self.execute(fn).compat3
+
+    def getErrorBounds(self, fn):
+        """GLHandler::getErrorBounds (GLHandler.cpp:206-212): int32[4P] or empty."""
+        if fn == RasterJoinBoundFn and self.bounds is not None:
+            return self.bounds
+        return np.zeros(0, np.int32)
+
+    def timings(self):
+        t = Timings()
+        self._check(self.lib.rj_get_timings(self.ctx, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in Timings._fields_}
+
+    def printTimeStats(self, fn=None):
+        buf = C.create_string_buffer(512)
+        self._check(self.lib.rj_format_time_stats(self.ctx, buf, 512))
+        return buf.value.decode()
+
+
+def decode_avg(agg):
+    """printResults avg decode (RasterJoin/main.cpp:206-208) of an int32[3P] vector."""
+    agg = np.asarray(agg, dtype=np.int64)
+    P = len(agg) // 3
+    num = agg[P:2 * P].astype(np.float32) * np.float32(100) + agg[2 * P:].astype(np.float32) / np.float32(10)
+    den = agg[:P].astype(np.float32)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        return np.where(agg[:P] == 0, 0.0, num / np.where(den == 0, 1, den))

@@ -1,0 +1,359 @@
+"""GPU parity: every join type through the C ABI against the CPU oracle.
+
+Counts must be bit-exact; sums (avg) within 1e-6 relative of the oracle's
+double-precision accumulation; error bounds bit-exact.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import rasterjoin as rj
+from rasterjoin import synth
+
+pytestmark = pytest.mark.gpu
+
+SUM_RTOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def c1():
+    """Benchmark configuration 1: 1M points, 260 Voronoi cells, 40 km box."""
+    pts = synth.points(1_000_000, seed=20261203, columns=True)
+    verts, pidx = synth.voronoi_polygons(260, seed=20261203)
+    return pts, verts, pidx
+
+
+@pytest.fixture(scope="module")
+def stars():
+    pts = synth.points(300_001, seed=5, columns=True)
+    verts, pidx = synth.star_polygons(150, seed=5, vmin=8, vmax=300, rmin=300, rmax=4000)
+    return pts, verts, pidx
+
+
+def make_dh(pts, verts, pidx):
+    dh = rj.DataHandler()
+    dh.add_column(1, rj.Location, pts["xy"])
+    if "t" in pts:
+        dh.add_column(2, rj.Uint, pts["t"])
+        dh.add_column(3, rj.Float, pts["a"])
+        dh.add_column(4, rj.Int, pts["f1"])
+        dh.add_column(5, rj.Int, pts["f2"])
+    dh.setPolygons(verts, pidx)
+    return dh
+
+
+def ocols(pts):
+    return oracle.Columns({2: (oracle.Uint, pts["t"]), 3: (oracle.Float, pts["a"]),
+                           4: (oracle.Int, pts["f1"]), 5: (oracle.Int, pts["f2"])})
+
+
+def check_sums(got, want):
+    np.testing.assert_allclose(got, want, rtol=SUM_RTOL, atol=1e-9 * max(1.0, float(np.abs(want).max())))
+
+
+def test_kat_two_squares(handler):
+    """RasterJoin/test/baseline.hpp:139-217: counts 2 and 3 for every join."""
+    xy, (verts, pidx), expect = synth.kat_two_squares()
+    dh = rj.DataHandler()
+    dh.add_column(0, rj.Location, xy)
+    dh.setPolygons(verts, pidx)
+    handler.setDataHandler(dh)
+    handler.setCellSize(0.001)
+    handler.setPolyIndexResolution(256)
+    for fn in (rj.RasterJoinFn, rj.IndexJoinFn, rj.HybridJoinFn, rj.RasterJoinBoundFn):
+        np.testing.assert_array_equal(handler.execute(fn).count, expect)
+    agg = handler.executeFunction(rj.IndexJoinFn)
+    assert list(agg[:2]) == [2, 3]
+
+
+@pytest.mark.parametrize("cell", [10.0, 10.0 / np.sqrt(2.0)])
+def test_c1_raster_count(handler, c1, cell):
+    pts, verts, pidx = c1
+    handler.setDataHandler(make_dh(pts, verts, pidx))
+    handler.setCellSize(cell)
+    got = handler.execute(rj.RasterJoinFn)
+    want, _, _ = oracle.raster_join(pts["xy"], verts, pidx, cell)
+    np.testing.assert_array_equal(got.count, want)
+
+
+def test_c1_raster_epsilon_semantics(handler, c1):
+    """accuracy 10 m -> cell 10/sqrt(2) (GLFunction::setMaxCellSize)."""
+    pts, verts, pidx = c1
+    handler.setDataHandler(make_dh(pts, verts, pidx))
+    handler.setAccuracyDistance(10.0)
+    got = handler.execute(rj.RasterJoinFn)
+    want, _, _ = oracle.raster_join(pts["xy"], verts, pidx, oracle.raster_cell(accuracy_m=10.0))
+    np.testing.assert_array_equal(got.count, want)
+
+
+@pytest.mark.parametrize("res", [256, 1024])
+def test_c1_index_matches_cpujoin(handler, c1, res):
+    pts, verts, pidx = c1
+    handler.setDataHandler(make_dh(pts, verts, pidx))
+    handler.setPolyIndexResolution(res)
+    got = handler.execute(rj.IndexJoinFn)
+    want, _ = oracle.index_join(pts["xy"], verts, pidx, res)
+    np.testing.assert_array_equal(got.count, want)
+    cpu, _, _, _ = oracle.cpujoin(pts["xy"], verts, pidx, 1024)
+    np.testing.assert_array_equal(got.count, cpu)
+
+
+def test_c1_hybrid_exact(handler, c1):
+    pts, verts, pidx = c1
+    handler.setDataHandler(make_dh(pts, verts, pidx))
+    handler.setPolyIndexResolution(256)
+    got = handler.execute(rj.HybridJoinFn)
+    want, _ = oracle.hybrid_join(pts["xy"], verts, pidx, 256)
+    np.testing.assert_array_equal(got.count, want)
+    cpu, _, _, _ = oracle.cpujoin(pts["xy"], verts, pidx, 1024)
+    np.testing.assert_array_equal(got.count, cpu)
+
+
+def test_c1_error_bounds(handler, c1):
+    pts, verts, pidx = c1
+    handler.setDataHandler(make_dh(pts, verts, pidx))
+    handler.setCellSize(10.0)
+    got = handler.execute(rj.RasterJoinBoundFn)
+    c, _, b = oracle.raster_join(pts["xy"], verts, pidx, 10.0, bounds=True)
+    np.testing.assert_array_equal(got.count, c)
+    np.testing.assert_array_equal(got.bounds.astype(np.int64), b)
+    # every exact count lies inside its hard range [agg - fp1, agg + fn1]
+    exact, _ = oracle.index_join(pts["xy"], verts, pidx, 256)
+    P = len(pidx) - 1
+    agg = got.count.astype(np.int64)
+    lo, hi = agg - b[3 * P:], agg + b[2 * P:3 * P]
+    assert np.all((exact.astype(np.int64) >= lo) & (exact.astype(np.int64) <= hi))
+
+
+def c2_query(dh):
+    dh.setQueryConstraints([(4, rj.GT, 2), (5, rj.LT, 8), (3, rj.LT, 50.0)])
+    dh.setTimeRange(2, synth.T0, synth.T0 + synth.YEAR // 2)
+    dh.setAggregation(rj.Avg, 3)
+
+
+def c2_filter(pts):
+    return ocols(pts).filt([(4, oracle.GT, 2), (5, oracle.LT, 8), (3, oracle.LT, 50.0)], aggr_attrib=3,
+                           time_range=(2, synth.T0, synth.T0 + synth.YEAR // 2))
+
+
+@pytest.mark.parametrize("fn", [rj.IndexJoinFn, rj.HybridJoinFn, rj.RasterJoinFn])
+def test_c2_filters_avg(handler, c1, fn):
+    pts, verts, pidx = c1
+    dh = make_dh(pts, verts, pidx)
+    c2_query(dh)
+    handler.setDataHandler(dh)
+    handler.setAccuracyDistance(100.0)
+    handler.setPolyIndexResolution(256)
+    got = handler.execute(fn)
+    f = c2_filter(pts)
+    if fn == rj.IndexJoinFn:
+        want = oracle.index_join(pts["xy"], verts, pidx, 256, f=f)
+    elif fn == rj.HybridJoinFn:
+        want = oracle.hybrid_join(pts["xy"], verts, pidx, 256, f=f)
+    else:
+        want = oracle.raster_join(pts["xy"], verts, pidx, oracle.raster_cell(accuracy_m=100.0), f=f)[:2]
+    np.testing.assert_array_equal(got.count, want[0])
+    check_sums(got.sum, want[1])
+    if fn != rj.RasterJoinFn:
+        # avg against the FP64 oracle (double-precision point-in-polygon)
+        c64, s64 = oracle.bruteforce_f64(pts["xy"], verts, pidx, f=f)
+        agree = got.count == c64
+        assert agree.mean() > 0.99
+        ok = agree & (c64 > 0)
+        np.testing.assert_allclose(got.avg[ok], (s64 / np.maximum(c64, 1))[ok], rtol=SUM_RTOL)
+
+
+def test_compat3_decodes_to_avg(handler, c1):
+    pts, verts, pidx = c1
+    dh = make_dh(pts, verts, pidx)
+    dh.setAggregation(rj.Avg, 3)
+    handler.setDataHandler(dh)
+    r = handler.execute(rj.IndexJoinFn)
+    dec = rj.decode_avg(r.compat3)
+    np.testing.assert_allclose(dec, r.avg, rtol=1e-3)
+
+
+def test_multi_tile_canvas(handler, c1):
+    """Canvas larger than the tile size splits into tiles (RasterJoin.cpp:59-63)."""
+    pts, verts, pidx = c1
+    dh = make_dh(pts, verts, pidx)
+    dh.setAggregation(rj.Sum, 3)
+    handler.setDataHandler(dh)
+    handler.setCellSize(10.0)
+    handler.max_fbo_size = 1500
+    try:
+        for fn in (rj.RasterJoinFn, rj.RasterJoinBoundFn):
+            got = handler.execute(fn)
+            f = ocols(pts).filt([], aggr_attrib=None if fn == rj.RasterJoinBoundFn else 3)
+            c, s, b = oracle.raster_join(pts["xy"], verts, pidx, 10.0, f=f, max_res=1500,
+                                         bounds=fn == rj.RasterJoinBoundFn)
+            np.testing.assert_array_equal(got.count, c)
+            if fn == rj.RasterJoinBoundFn:
+                np.testing.assert_array_equal(got.bounds.astype(np.int64), b)
+            else:
+                check_sums(got.sum, s)
+    finally:
+        handler.max_fbo_size = 8192
+
+
+def test_force_canvas_equals_label(handler, c1):
+    pts, verts, pidx = c1
+    dh = make_dh(pts, verts, pidx)
+    dh.setAggregation(rj.Avg, 3)
+    handler.setDataHandler(dh)
+    handler.setCellSize(10.0)
+    handler.setPolyIndexResolution(256)
+    for fn in (rj.RasterJoinFn, rj.HybridJoinFn):
+        handler.flags = 0
+        a = handler.execute(fn)
+        handler.flags = rj.FLAG_FORCE_CANVAS
+        b = handler.execute(fn)
+        handler.flags = 0
+        np.testing.assert_array_equal(a.count, b.count)
+        check_sums(a.sum, b.sum)
+
+
+def test_overlapping_stars(handler, stars):
+    """Overlapping polygons: every covering polygon counts (canvas path)."""
+    pts, verts, pidx = stars
+    dh = make_dh(pts, verts, pidx)
+    dh.setAggregation(rj.Avg, 3)
+    handler.setDataHandler(dh)
+    handler.setCellSize(25.0)
+    handler.setPolyIndexResolution(128)
+    f = ocols(pts).filt([], aggr_attrib=3)
+    want = oracle.index_join(pts["xy"], verts, pidx, 128, f=f)
+    for fn in (rj.IndexJoinFn, rj.HybridJoinFn):
+        got = handler.execute(fn)
+        np.testing.assert_array_equal(got.count, want[0])
+        check_sums(got.sum, want[1])
+    got = handler.execute(rj.RasterJoinFn)
+    c, s, _ = oracle.raster_join(pts["xy"], verts, pidx, 25.0, f=f)
+    np.testing.assert_array_equal(got.count, c)
+    check_sums(got.sum, s)
+    dh.setAggregation(rj.Count, -1)
+    got = handler.execute(rj.RasterJoinBoundFn)
+    c, _, b = oracle.raster_join(pts["xy"], verts, pidx, 25.0, bounds=True)
+    np.testing.assert_array_equal(got.count, c)
+    np.testing.assert_array_equal(got.bounds.astype(np.int64), b)
+
+
+def test_compat_index_clamp(handler, c1):
+    pts, verts, pidx = c1
+    handler.setDataHandler(make_dh(pts, verts, pidx))
+    handler.setPolyIndexResolution(64)
+    handler.flags = rj.FLAG_COMPAT_INDEX_CLAMP
+    try:
+        got = handler.execute(rj.IndexJoinFn)
+    finally:
+        handler.flags = 0
+    want, _ = oracle.index_join(pts["xy"], verts, pidx, 64, compat_clamp=True)
+    np.testing.assert_array_equal(got.count, want)
+    exact, _ = oracle.index_join(pts["xy"], verts, pidx, 64)
+    assert want.sum() < exact.sum()   # the clamp drops the last grid row/column
+
+
+@pytest.mark.parametrize("compat", [False, True])
+def test_lte_gte_equality(handler, c1, compat):
+    pts, verts, pidx = c1
+    dh = make_dh(pts, verts, pidx)
+    cons = [(4, rj.LTE, 5), (5, rj.GTE, 3), (3, rj.GTE, 12.5)]
+    dh.setQueryConstraints(cons)
+    handler.setDataHandler(dh)
+    handler.flags = rj.FLAG_COMPAT_FLOAT_EQ if compat else 0
+    try:
+        got = handler.execute(rj.IndexJoinFn)
+    finally:
+        handler.flags = 0
+    f = ocols(pts).filt([(4, oracle.LTE, 5), (5, oracle.GTE, 3), (3, oracle.GTE, 12.5)], compat_float_eq=compat)
+    want, _ = oracle.index_join(pts["xy"], verts, pidx, handler.presx, f=f)
+    np.testing.assert_array_equal(got.count, want)
+
+
+@pytest.mark.parametrize("n", [0, 1, 3, 5, 4099])
+def test_small_and_ragged_tables(handler, c1, n):
+    pts, verts, pidx = c1
+    sub = {k: v[:n] for k, v in pts.items()}
+    dh = make_dh(sub, verts, pidx)
+    dh.setAggregation(rj.Avg, 3)
+    handler.setDataHandler(dh)
+    handler.setCellSize(10.0)
+    f = ocols(sub).filt([], aggr_attrib=3)
+    for fn in (rj.RasterJoinFn, rj.IndexJoinFn, rj.HybridJoinFn):
+        got = handler.execute(fn)
+        if fn == rj.RasterJoinFn:
+            want = oracle.raster_join(sub["xy"], verts, pidx, 10.0, f=f)[:2]
+        else:
+            want = oracle.index_join(sub["xy"], verts, pidx, handler.presx, f=f)
+        np.testing.assert_array_equal(got.count, want[0])
+        check_sums(got.sum, want[1])
+
+
+def test_points_outside_bounds(handler):
+    rng = np.random.default_rng(3)
+    xy = rng.uniform(-20000, 60000, size=(100_000, 2)).astype(np.float32)
+    verts, pidx = synth.voronoi_polygons(40, seed=3)
+    pts = {"xy": xy}
+    handler.setDataHandler(make_dh(pts, verts, pidx))
+    handler.setCellSize(20.0)
+    handler.setPolyIndexResolution(128)
+    got = handler.execute(rj.IndexJoinFn)
+    np.testing.assert_array_equal(got.count, oracle.index_join(xy, verts, pidx, 128)[0])
+    got = handler.execute(rj.HybridJoinFn)
+    np.testing.assert_array_equal(got.count, oracle.hybrid_join(xy, verts, pidx, 128)[0])
+    got = handler.execute(rj.RasterJoinFn)
+    np.testing.assert_array_equal(got.count, oracle.raster_join(xy, verts, pidx, 20.0)[0])
+
+
+def test_hybrid_canvas_size_invariance(handler, c1):
+    """The hybrid join is exact whatever canvas it uses (ε is ignored)."""
+    pts, verts, pidx = c1
+    handler.setDataHandler(make_dh(pts, verts, pidx))
+    handler.setPolyIndexResolution(256)
+    ref = None
+    try:
+        for canvas in (1024, 4096, 8192):
+            handler.hybrid_canvas = canvas
+            got = handler.execute(rj.HybridJoinFn).count
+            if ref is None:
+                ref = got
+            np.testing.assert_array_equal(got, ref)
+    finally:
+        handler.hybrid_canvas = 8192
+
+
+def test_errors_are_status_codes(handler, c1):
+    pts, verts, pidx = c1
+    dh = make_dh(pts, verts, pidx)
+    dh.setQueryConstraints([(4, rj.GT, 0)] * 11)
+    handler.setDataHandler(dh)
+    with pytest.raises(rj.RJError) as e:
+        handler.execute(rj.IndexJoinFn)
+    assert e.value.code == -3
+    dh.setQueryConstraints([(99, rj.GT, 0)])
+    with pytest.raises(rj.RJError) as e:
+        handler.execute(rj.IndexJoinFn)
+    assert e.value.code == -1
+    dh.setQueryConstraints([])
+    q = handler.make_query(7)
+    with pytest.raises(rj.RJError) as e:
+        handler.execute(7, query=q)
+    assert e.value.code == -7
+    # the context stays usable after errors
+    got = handler.execute(rj.IndexJoinFn)
+    assert got.count.sum() > 0
+
+
+def test_timing_line(handler, c1):
+    pts, verts, pidx = c1
+    handler.setDataHandler(make_dh(pts, verts, pidx))
+    handler.flags = rj.FLAG_PHASE_TIMING
+    try:
+        handler.execute(rj.RasterJoinFn)
+    finally:
+        handler.flags = 0
+    line = handler.printTimeStats()
+    fields = line.split()
+    assert len(fields) == 15 and int(fields[0]) == len(pts["xy"]) and int(fields[2]) == 0
+    t = handler.timings()
+    assert t["pt_render_ms"] > 0
