@@ -184,7 +184,7 @@ RJ_API int rj_create(const rj_config *cfg, rj_ctx **out);
 /* replaces GLHandler::~GLHandler (GLHandler.cpp:56-62) */
 RJ_API void rj_destroy(rj_ctx *ctx);
 /* human-readable text of the last failing call on this context */
-const char *rj_last_error(const rj_ctx *ctx);
+RJ_API const char *rj_last_error(const rj_ctx *ctx);
 /* run subsequent work on a caller stream (cudaStream_t) */
 RJ_API int rj_set_stream(rj_ctx *ctx, void *stream);
 RJ_API int rj_abi_version(void);
