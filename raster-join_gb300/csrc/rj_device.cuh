@@ -14,7 +14,11 @@
 namespace rj {
 
 constexpr int kMaxFilters = RJ_MAX_CONSTRAINTS + 2;   // + time range (2 predicates)
-constexpr uint32_t kEmptyLabel = 0xFFFFFFFFu;
+constexpr uint16_t kEmptyLabel = 0xFFFFu;     // pixel covered by no polygon
+constexpr uint16_t kBorderLabel = 0xFFFEu;    // hybrid: pixel near an outline
+constexpr int kMaxLabelPolys = 0xFFFD;        // polygon ids that fit a 16-bit label
+constexpr uint32_t kCodeEmpty = 0xFFFFFFFFu;  // classified cell without polygons
+constexpr uint32_t kCodeList = 0x80000000u;   // classified cell: consult the entry list
 constexpr int kSubpixelBits = 8;                      // GL_SUBPIXEL_BITS on NVIDIA
 constexpr int kSub = 1 << kSubpixelBits;              // 256 fixed-point units per pixel
 constexpr float kWinClamp = 1048576.0f;               // |window coord| clamp (2^20 px)

@@ -22,15 +22,20 @@ struct PolyPassArgs {
     int resx, resy;
     const uint32_t* canvas_c;    // [T][resy][resx] point counts
     const double* canvas_s;      // [T][resy][resx] sums or null
-    uint32_t* label;             // [T][resy][resx] polygon label (MODE_LABEL)
+    uint16_t* label;             // [T][resy][resx] polygon label (MODE_LABEL)
+    unsigned long long* covered; // MODE_LABEL: pixels covered, summed over polygons
     const uint32_t* border;      // dilated hybrid border mask (skip) or null
     int border_words;
     unsigned long long* out_count;
     double* out_sum;
     long long* out_bounds;       // [4P]
     unsigned int* work_ctr;
-    int* flag;                   // bit0: label conflict (overlapping polygons)
     int line_filter;
+    // per (tile, polygon) work description (k_poly_info)
+    int4* info_a;                // i_lo, i_hi, r_lo, r_hi
+    int2* info_b;                // j_lo, j_hi (rows whose centre can be crossed)
+    int* nbands;                 // bands of kBand rows
+    const int* band_start;       // exclusive scan of nbands, [T*P + 1]
 };
 
 struct GridArgs {
@@ -44,6 +49,40 @@ struct GridArgs {
     const int* cell_start;
     int* cursor;
     int* entries;
+    int* pair_cell;              // optional: cell of every entry
+};
+
+// Classified grid: every (cell, candidate polygon) pair is FULL (every point
+// of the cell is inside), OUT (none is; dropped) or EDGE (points need the
+// crossing test, against the few edges that can change its outcome).
+struct ClsArgs {
+    const float2* verts;
+    const int* pindex;
+    int P;
+    const int* pair_off;         // [P+1] first candidate pair of each polygon (polygon-major)
+    const int4* prange;          // [P] candidate cells [stx, enx) x [sty, eny)
+    int npairs;
+    float lbx, lby, csx, csy;    // classified grid lower-left / cell size (fp32, as the points use)
+    int res;
+    float margin;                // world units: fp32 error of the test + cell assignment
+    int4* info;                  // per pair: poly, nr (-1 full, -2 out), nf, cell
+    int* ecount;                 // per pair: edges kept
+    const int* eoff;             // per pair: first edge (exclusive scan of ecount)
+    float4* edges;
+    int* cell_kept;              // per cell: kept pairs
+    const int* cell_start;       // per cell: exclusive scan of cell_kept
+    int* cursor;
+    int4* entries;               // cell-major kept pairs: poly, nr, nf, edge offset
+};
+
+struct ExactIndex {
+    const uint32_t* code;        // [res*res] polygon id of a cell inside exactly one polygon,
+                                 // kCodeEmpty, or kCodeList (consult the entries)
+    const int* cell_start;       // [res*res + 1] classified CSR
+    const int4* entries;         // poly, nr (-1: full cell), nf, edge offset
+    const float4* edges;         // (vi.x, vi.y, vj.x, vj.y): nr straddle-only edges, then nf full
+    float lbx, lby, csx, csy;    // resolution = query grid resolution * 2^k
+    int res;
 };
 
 // Per-axis tile transforms of a raster canvas.
@@ -79,16 +118,17 @@ struct IndexArgs {
 
 struct HybridArgs {
     HybXf h;
-    const uint32_t* border;      // dilated border mask [resy][words]
+    const uint32_t* border;      // dilated border mask [resy][words] (canvas mode)
     int words;
     uint32_t* canvas_c;          // canvas mode: [resy][resx]
     double* canvas_s;
-    const uint32_t* label;       // label mode: [resy][resx]
+    const uint16_t* label;       // label mode: [resy][resx], kBorderLabel on border pixels
 };
 
 // polygon side
 void launch_transform_vertices(const float2* verts, int V, const float4* colxf, const float4* rowxf,
                                int splitx, int T, int2* wv, float2* wf, int sms, cudaStream_t st);
+void launch_poly_info(int mode, const PolyPassArgs& a, int sms, cudaStream_t st);
 void launch_poly_pass(int mode, const PolyPassArgs& a, int sms, cudaStream_t st);
 void launch_grid_count(const GridArgs& g, int sms, cudaStream_t st);
 void launch_grid_fill(const GridArgs& g, int sms, cudaStream_t st);
@@ -104,10 +144,21 @@ void launch_dilate_mask(const uint32_t* in, uint32_t* out, int resx, int resy, i
 // smem_hist: histogram capacity decision done by the launcher.
 void launch_raster_splat(const PointArgs& pa, const CanvasXf& cx, uint32_t* canvas_c, double* canvas_s,
                          int sms, cudaStream_t st);
-void launch_raster_label(const PointArgs& pa, const CanvasXf& cx, const uint32_t* label, int sms,
+void launch_raster_label(const PointArgs& pa, const CanvasXf& cx, const uint16_t* label, int sms,
                          cudaStream_t st);
 void launch_index_points(const PointArgs& pa, const IndexArgs& ia, int sms, cudaStream_t st);
-void launch_hybrid_points(const PointArgs& pa, const IndexArgs& ia, const HybridArgs& ha, int sms,
+void launch_exact_points(const PointArgs& pa, const ExactIndex& ix, int sms, cudaStream_t st);
+void launch_hybrid_points(const PointArgs& pa, const ExactIndex& ix, const HybridArgs& ha, int sms,
                           cudaStream_t st);
+
+// classified grid build
+void launch_cls_classify(const ClsArgs& c, int sms, cudaStream_t st);
+void launch_cls_emit(const ClsArgs& c, int sms, cudaStream_t st);
+void launch_cls_fill_edges(const ClsArgs& c, int sms, cudaStream_t st);
+// count labelled pixels (before border marking) and mark border pixels
+void launch_label_finish(uint16_t* label, const uint32_t* mask, int resx, int resy, int ntiles, int words,
+                         unsigned long long* nonempty, int sms, cudaStream_t st);
+void launch_cls_codes(const int* cell_start, const int4* entries, uint32_t* code, int ncells, int sms,
+                      cudaStream_t st);
 
 }  // namespace rj

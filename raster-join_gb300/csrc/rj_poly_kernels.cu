@@ -128,36 +128,23 @@ __device__ bool compute_fraction(float x0, float y0, float x1, float y1,
 
 // ---------------------------------------------------------------------------
 constexpr int kPolyWarps = 8;
-constexpr int kBand = 16;          // pixel rows per band
+constexpr int kBand = 16;          // pixel rows per work item
 constexpr int kBandCap = 256;      // staged edges per warp
 constexpr int kCrossCap = 64;      // crossings per row per warp
 
+// Per (tile, polygon): pixel column range that can be covered, rows to visit
+// and rows whose centre line the polygon can cross; number of row bands.
 template <int MODE>
-__global__ void __launch_bounds__(kPolyWarps * 32)
-k_poly_pass(PolyPassArgs a) {
-    __shared__ int4 s_edge[kPolyWarps][kBandCap];
-    __shared__ int s_eidx[kPolyWarps][kBandCap];
-    __shared__ int s_cross[kPolyWarps][kCrossCap];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const unsigned FULL = 0xffffffffu;
-    const int total = a.T * a.P;
-    int4* my_edge = s_edge[warp];
-    int* my_eidx = s_eidx[warp];
-    int* my_cross = s_cross[warp];
-
-    for (;;) {
-        int item = 0;
-        if (lane == 0) item = (int)atomicAdd(a.work_ctr, 1u);
-        item = __shfl_sync(FULL, item, 0);
-        if (item >= total) break;
+__global__ void k_poly_info(PolyPassArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int TP = a.T * a.P;
+    for (int item = wid; item < TP; item += nw) {
         const int t = item / a.P, p = item - t * a.P;
         const int v0 = __ldg(a.pindex + p);
         const int n = __ldg(a.pindex + p + 1) - v0;
-        if (n < 2) continue;
         const int2* pv = a.wv + (size_t)t * a.V + v0;
-        const float2* pf = a.wf ? a.wf + (size_t)t * a.V + v0 : nullptr;
-        const size_t tile_off = (size_t)t * a.resx * a.resy;
-
         int xmin = INT_MAX, xmax = INT_MIN, ymin = INT_MAX, ymax = INT_MIN;
         for (int k = lane; k < n; k += 32) {
             int2 q = pv[k];
@@ -166,177 +153,235 @@ k_poly_pass(PolyPassArgs a) {
         }
         xmin = warp_min(xmin); xmax = warp_max(xmax);
         ymin = warp_min(ymin); ymax = warp_max(ymax);
-
-        // rows whose centre can be crossed: ymin < Cy <= ymax
-        int j_lo = (int)floordiv64((int64_t)ymin - kSub / 2, kSub) + 1;
-        int j_hi = (int)floordiv64((int64_t)ymax - kSub / 2, kSub);
-        // pixels that can be inside: ceil((xmin-128)/256) .. ceil((xmax-128)/256)-1
-        int i_lo = (int)floordiv64((int64_t)xmin - kSub / 2 + kSub - 1, kSub);
-        int i_hi = (int)floordiv64((int64_t)xmax - kSub / 2 + kSub - 1, kSub) - 1;
-        int r_lo = j_lo, r_hi = j_hi;
-        if (MODE == MODE_BOUNDS) {
-            // rows whose pixel rectangle an edge may touch
-            r_lo = min(r_lo, (int)floordiv64((int64_t)ymin, kSub) - 1);
-            r_hi = max(r_hi, (int)floordiv64((int64_t)ymax, kSub) + 1);
+        if (lane != 0) continue;
+        int nbands = 0;
+        int4 ia = make_int4(0, -1, 0, -1);
+        int2 ib = make_int2(0, -1);
+        if (n >= 2) {
+            // rows whose centre can be crossed: ymin < Cy <= ymax
+            int j_lo = (int)floordiv64((int64_t)ymin - kSub / 2, kSub) + 1;
+            int j_hi = (int)floordiv64((int64_t)ymax - kSub / 2, kSub);
+            // pixels that can be inside: ceil((xmin-128)/256) .. ceil((xmax-128)/256)-1
+            int i_lo = (int)floordiv64((int64_t)xmin - kSub / 2 + kSub - 1, kSub);
+            int i_hi = (int)floordiv64((int64_t)xmax - kSub / 2 + kSub - 1, kSub) - 1;
+            int r_lo = j_lo, r_hi = j_hi;
+            if (MODE == MODE_BOUNDS) {
+                // rows whose pixel rectangle an edge may touch
+                r_lo = min(r_lo, (int)floordiv64((int64_t)ymin, kSub) - 1);
+                r_hi = max(r_hi, (int)floordiv64((int64_t)ymax, kSub) + 1);
+            }
+            r_lo = max(r_lo, 0);
+            r_hi = min(r_hi, a.resy - 1);
+            i_lo = max(i_lo, 0);
+            i_hi = min(i_hi, a.resx - 1);
+            if (r_lo <= r_hi && (MODE == MODE_BOUNDS || i_lo <= i_hi)) {
+                nbands = (r_hi - r_lo + kBand) / kBand;
+                ia = make_int4(i_lo, i_hi, r_lo, r_hi);
+                ib = make_int2(j_lo, j_hi);
+            }
         }
-        r_lo = max(r_lo, 0);
-        r_hi = min(r_hi, a.resy - 1);
-        i_lo = max(i_lo, 0);
-        i_hi = min(i_hi, a.resx - 1);
-        if (r_lo > r_hi) continue;
-        if (MODE != MODE_BOUNDS && i_lo > i_hi) continue;
+        a.info_a[item] = ia;
+        a.info_b[item] = ib;
+        a.nbands[item] = nbands;
+    }
+}
+
+// One warp per (tile, polygon, band of kBand rows): the band's edges are
+// staged in shared memory, each row's centre-line crossings are computed
+// exactly, and every pixel of the row is inside iff an odd number of
+// crossings lies to its right.
+template <int MODE>
+__global__ void __launch_bounds__(kPolyWarps * 32)
+k_poly_pass(PolyPassArgs a) {
+    __shared__ int4 s_edge[kPolyWarps][kBandCap];
+    __shared__ int s_eidx[kPolyWarps][kBandCap];
+    __shared__ int s_cross[kPolyWarps][kCrossCap];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned FULL = 0xffffffffu;
+    const int TP = a.T * a.P;
+    const int total = a.band_start[TP];
+    int4* my_edge = s_edge[warp];
+    int* my_eidx = s_eidx[warp];
+    int* my_cross = s_cross[warp];
+
+    for (;;) {
+        int item = 0, tp = 0;
+        if (lane == 0) {
+            item = (int)atomicAdd(a.work_ctr, 1u);
+            if (item < total) {
+                // last tp with band_start[tp] <= item
+                int lo = 0, hi = TP - 1;
+                while (lo < hi) {
+                    int mid = (lo + hi + 1) >> 1;
+                    if (a.band_start[mid] <= item) lo = mid; else hi = mid - 1;
+                }
+                tp = lo;
+            }
+        }
+        item = __shfl_sync(FULL, item, 0);
+        tp = __shfl_sync(FULL, tp, 0);
+        if (item >= total) break;
+        const int t = tp / a.P, p = tp - t * a.P;
+        const int band = item - a.band_start[tp];
+        const int4 ia = a.info_a[tp];
+        const int2 ib = a.info_b[tp];
+        const int i_lo = ia.x, i_hi = ia.y, j_lo = ib.x, j_hi = ib.y;
+        const int jb = ia.z + band * kBand;
+        const int je = min(jb + kBand - 1, ia.w);
+        const int v0 = __ldg(a.pindex + p);
+        const int n = __ldg(a.pindex + p + 1) - v0;
+        const int2* pv = a.wv + (size_t)t * a.V + v0;
+        const float2* pf = a.wf ? a.wf + (size_t)t * a.V + v0 : nullptr;
+        const size_t tile_off = (size_t)t * a.resx * a.resy;
 
         unsigned long long acc_c = 0;
         double acc_s = 0.0;
         long long b_fn = 0, b_fp = 0, b_fn1 = 0, b_fp1 = 0;
 
-        for (int jb = r_lo; jb <= r_hi; jb += kBand) {
-            const int je = min(jb + kBand - 1, r_hi);
-            // fixed-point y window of the band (one pixel of margin each side)
-            const int64_t band_lo = (int64_t)jb * kSub - kSub;
-            const int64_t band_hi = (int64_t)(je + 1) * kSub + kSub;
-            int nb = 0;
-            bool overflow = false;
-            for (int k0 = 0; k0 < n; k0 += 32) {
-                int k = k0 + lane;
-                bool take = false;
-                int4 e = make_int4(0, 0, 0, 0);
-                if (k < n) {
-                    int2 A = pv[k];
-                    int2 B = pv[(k + 1 == n) ? 0 : k + 1];
-                    int lo = min(A.y, B.y), hi = max(A.y, B.y);
-                    take = (hi >= band_lo) && (lo <= band_hi);
-                    e = make_int4(A.x, A.y, B.x, B.y);
-                }
-                unsigned m = __ballot_sync(FULL, take);
-                int pos = nb + __popc(m & ((1u << lane) - 1u));
-                if (take && pos < kBandCap) { my_edge[pos] = e; my_eidx[pos] = k; }
-                nb += __popc(m);
+        // fixed-point y window of the band (one pixel of margin each side)
+        const int64_t band_lo = (int64_t)jb * kSub - kSub;
+        const int64_t band_hi = (int64_t)(je + 1) * kSub + kSub;
+        int nb = 0;
+        for (int k0 = 0; k0 < n; k0 += 32) {
+            int k = k0 + lane;
+            bool take = false;
+            int4 e = make_int4(0, 0, 0, 0);
+            if (k < n) {
+                int2 A = pv[k];
+                int2 B = pv[(k + 1 == n) ? 0 : k + 1];
+                int lo = min(A.y, B.y), hi = max(A.y, B.y);
+                take = (hi >= band_lo) && (lo <= band_hi);
+                e = make_int4(A.x, A.y, B.x, B.y);
             }
-            if (nb > kBandCap) overflow = true;
-            __syncwarp();
+            unsigned m = __ballot_sync(FULL, take);
+            int pos = nb + __popc(m & ((1u << lane) - 1u));
+            if (take && pos < kBandCap) { my_edge[pos] = e; my_eidx[pos] = k; }
+            nb += __popc(m);
+        }
+        const bool overflow = nb > kBandCap;
+        __syncwarp();
 
-            for (int j = jb; j <= je; ++j) {
-                const int32_t cy = j * kSub + kSub / 2;
-                // crossings of this row's centre line
-                int m = 0;
-                bool cover_slow = overflow;
-                if (!overflow) {
-                    for (int e0 = 0; e0 < nb; e0 += 32) {
-                        int e = e0 + lane;
-                        bool c = false;
-                        int L = 0;
-                        if (e < nb) {
-                            int4 q = my_edge[e];
-                            if (cross_row(q.y, q.w, cy)) { c = true; L = cross_L(q.x, q.y, q.z, q.w, cy); }
-                        }
-                        unsigned bm = __ballot_sync(FULL, c);
-                        int pos = m + __popc(bm & ((1u << lane) - 1u));
-                        if (c && pos < kCrossCap) my_cross[pos] = L;
-                        m += __popc(bm);
+        for (int j = jb; j <= je; ++j) {
+            const int32_t cy = j * kSub + kSub / 2;
+            // crossings of this row's centre line
+            int m = 0;
+            bool cover_slow = overflow;
+            if (!overflow) {
+                for (int e0 = 0; e0 < nb; e0 += 32) {
+                    int e = e0 + lane;
+                    bool c = false;
+                    int L = 0;
+                    if (e < nb) {
+                        int4 q = my_edge[e];
+                        if (cross_row(q.y, q.w, cy)) { c = true; L = cross_L(q.x, q.y, q.z, q.w, cy); }
                     }
-                    if (m > kCrossCap) cover_slow = true;
+                    unsigned bm = __ballot_sync(FULL, c);
+                    int pos = m + __popc(bm & ((1u << lane) - 1u));
+                    if (c && pos < kCrossCap) my_cross[pos] = L;
+                    m += __popc(bm);
                 }
-                __syncwarp();
-                const bool centre_row = (j >= j_lo && j <= j_hi);
-                if (centre_row && (m > 0 || cover_slow)) {
-                    for (int i = i_lo + lane; i <= i_hi; i += 32) {
+                if (m > kCrossCap) cover_slow = true;
+            }
+            __syncwarp();
+            const bool centre_row = (j >= j_lo && j <= j_hi);
+            if (centre_row && (m > 0 || cover_slow)) {
+                for (int i = i_lo + lane; i <= i_hi; i += 32) {
+                    bool inside = false;
+                    if (!cover_slow) {
+                        for (int k = 0; k < m; ++k) inside ^= (i < my_cross[k]);
+                    } else {
+                        for (int k = 0; k < n; ++k) {
+                            int2 A = pv[k];
+                            int2 B = pv[(k + 1 == n) ? 0 : k + 1];
+                            if (cross_row(A.y, B.y, cy)) inside ^= (i < cross_L(A.x, A.y, B.x, B.y, cy));
+                        }
+                    }
+                    if (!inside) continue;
+                    const size_t pix = tile_off + (size_t)j * a.resx + i;
+                    if (a.border) {
+                        uint32_t w = __ldg(a.border + ((size_t)j * a.border_words + (i >> 5)));
+                        if ((w >> (i & 31)) & 1u) continue;
+                    }
+                    if (MODE == MODE_LABEL) {
+                        a.label[pix] = (uint16_t)p;   // overlaps detected by counting, see k_label_finish
+                        ++acc_c;
+                    } else {
+                        acc_c += __ldg(a.canvas_c + pix);
+                        if (a.canvas_s) acc_s += __ldg(a.canvas_s + pix);
+                    }
+                }
+            }
+            if (MODE == MODE_BOUNDS) {
+                // Outline pass: every edge of the polygon touching this pixel
+                // row, every pixel of the row the edge clips.
+                const float ylo = (float)j, yhi = (float)(j + 1);
+                const int ne = overflow ? n : nb;
+                for (int e0 = 0; e0 < ne; e0 += 32) {
+                    int e = e0 + lane;
+                    if (e >= ne) continue;
+                    int k = overflow ? e : my_eidx[e];
+                    float2 P0 = pf[k];
+                    float2 P1 = pf[(k + 1 == n) ? 0 : k + 1];
+                    float eylo = fminf(P0.y, P1.y), eyhi = fmaxf(P0.y, P1.y);
+                    if (eyhi < ylo - 0.01f || eylo > yhi + 0.01f) continue;
+                    // x range of the edge inside the slab (conservative, +-1 px)
+                    float xa, xb;
+                    if (P0.y == P1.y) {
+                        xa = fminf(P0.x, P1.x); xb = fmaxf(P0.x, P1.x);
+                    } else {
+                        float ta = (ylo - P0.y) / (P1.y - P0.y);
+                        float tb = (yhi - P0.y) / (P1.y - P0.y);
+                        ta = fminf(fmaxf(ta, 0.0f), 1.0f);
+                        tb = fminf(fmaxf(tb, 0.0f), 1.0f);
+                        float x_a = P0.x + (P1.x - P0.x) * ta;
+                        float x_b = P0.x + (P1.x - P0.x) * tb;
+                        xa = fminf(x_a, x_b); xb = fmaxf(x_a, x_b);
+                    }
+                    int ia0 = max((int)floorf(xa) - 1, 0);
+                    int ib0 = min((int)floorf(xb) + 1, a.resx - 1);
+                    for (int i = ia0; i <= ib0; ++i) {
+                        const size_t pix = tile_off + (size_t)j * a.resx + i;
+                        uint32_t val = __ldg(a.canvas_c + pix);
+                        if (val == 0) continue;
+                        if (a.line_filter) {
+                            // varying interpolation along the line (projection of
+                            // the pixel centre), kept within 0.5 px: line-bound.frag:245
+                            float cxp = (float)i + 0.5f, cyp = (float)j + 0.5f;
+                            float dx = __fsub_rn(P1.x, P0.x), dy = __fsub_rn(P1.y, P0.y);
+                            float l2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+                            if (!(l2 > 0.0f)) continue;
+                            float tt = __fdiv_rn(__fadd_rn(__fmul_rn(__fsub_rn(cxp, P0.x), dx),
+                                                          __fmul_rn(__fsub_rn(cyp, P0.y), dy)), l2);
+                            float qx = __fadd_rn(P0.x, __fmul_rn(tt, dx));
+                            float qy = __fadd_rn(P0.y, __fmul_rn(tt, dy));
+                            if (fabsf(__fsub_rn(qx, cxp)) >= 0.5f || fabsf(__fsub_rn(qy, cyp)) >= 0.5f) continue;
+                        }
+                        float frac;
+                        if (!compute_fraction(P0.x, P0.y, P1.x, P1.y, (float)i, ylo, (float)(i + 1), yhi, frac)) continue;
+                        // inside test of the pixel centre: the same coverage rule
                         bool inside = false;
-                        if (!cover_slow) {
-                            for (int k = 0; k < m; ++k) inside ^= (i < my_cross[k]);
-                        } else {
-                            const int32_t cx = i * kSub + kSub / 2;
-                            for (int k = 0; k < n; ++k) {
-                                int2 A = pv[k];
-                                int2 B = pv[(k + 1 == n) ? 0 : k + 1];
+                        if (!cover_slow && centre_row) {
+                            for (int kk = 0; kk < m; ++kk) inside ^= (i < my_cross[kk]);
+                        } else if (centre_row) {
+                            for (int kk = 0; kk < n; ++kk) {
+                                int2 A = pv[kk];
+                                int2 B = pv[(kk + 1 == n) ? 0 : kk + 1];
                                 if (cross_row(A.y, B.y, cy)) inside ^= (i < cross_L(A.x, A.y, B.x, B.y, cy));
                             }
-                            (void)cx;
                         }
-                        if (!inside) continue;
-                        const size_t pix = tile_off + (size_t)j * a.resx + i;
-                        if (a.border) {
-                            uint32_t w = __ldg(a.border + ((size_t)j * a.border_words + (i >> 5)));
-                            if ((w >> (i & 31)) & 1u) continue;
-                        }
-                        if (MODE == MODE_LABEL) {
-                            uint32_t old = atomicExch(a.label + pix, (uint32_t)p);
-                            if (old != kEmptyLabel && old != (uint32_t)p) atomicOr(a.flag, 1);
-                        } else {
-                            acc_c += __ldg(a.canvas_c + pix);
-                            if (a.canvas_s) acc_s += __ldg(a.canvas_s + pix);
-                        }
+                        if (frac > 0.5f) frac = __fsub_rn(1.0f, frac);
+                        int toAdd = (int)ceilf(__fmul_rn(frac, (float)val));
+                        if (inside) { b_fp += toAdd; b_fp1 += val; }
+                        else        { b_fn += toAdd; b_fn1 += val; }
                     }
                 }
-                if (MODE == MODE_BOUNDS) {
-                    // Outline pass: every edge of the polygon touching this
-                    // pixel row, every pixel of the row the edge clips.
-                    const float ylo = (float)j, yhi = (float)(j + 1);
-                    for (int e0 = 0; e0 < (overflow ? n : nb); e0 += 32) {
-                        int e = e0 + lane;
-                        if (e >= (overflow ? n : nb)) continue;
-                        int k = overflow ? e : my_eidx[e];
-                        float2 P0 = pf[k];
-                        float2 P1 = pf[(k + 1 == n) ? 0 : k + 1];
-                        float eylo = fminf(P0.y, P1.y), eyhi = fmaxf(P0.y, P1.y);
-                        if (eyhi < ylo - 0.01f || eylo > yhi + 0.01f) continue;
-                        // x range of the edge inside the slab (conservative, +-1 px)
-                        float xa, xb;
-                        if (P0.y == P1.y) {
-                            xa = fminf(P0.x, P1.x); xb = fmaxf(P0.x, P1.x);
-                        } else {
-                            float ta = (ylo - P0.y) / (P1.y - P0.y);
-                            float tb = (yhi - P0.y) / (P1.y - P0.y);
-                            ta = fminf(fmaxf(ta, 0.0f), 1.0f);
-                            tb = fminf(fmaxf(tb, 0.0f), 1.0f);
-                            float x_a = P0.x + (P1.x - P0.x) * ta;
-                            float x_b = P0.x + (P1.x - P0.x) * tb;
-                            xa = fminf(x_a, x_b); xb = fmaxf(x_a, x_b);
-                        }
-                        int ia = max((int)floorf(xa) - 1, 0);
-                        int ib = min((int)floorf(xb) + 1, a.resx - 1);
-                        for (int i = ia; i <= ib; ++i) {
-                            const size_t pix = tile_off + (size_t)j * a.resx + i;
-                            uint32_t val = __ldg(a.canvas_c + pix);
-                            if (val == 0) continue;
-                            if (a.line_filter) {
-                                // varying interpolation along the line (projection of
-                                // the pixel centre), kept within 0.5 px: line-bound.frag:245
-                                float cxp = (float)i + 0.5f, cyp = (float)j + 0.5f;
-                                float dx = __fsub_rn(P1.x, P0.x), dy = __fsub_rn(P1.y, P0.y);
-                                float l2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-                                if (!(l2 > 0.0f)) continue;
-                                float tt = __fdiv_rn(__fadd_rn(__fmul_rn(__fsub_rn(cxp, P0.x), dx),
-                                                              __fmul_rn(__fsub_rn(cyp, P0.y), dy)), l2);
-                                float qx = __fadd_rn(P0.x, __fmul_rn(tt, dx));
-                                float qy = __fadd_rn(P0.y, __fmul_rn(tt, dy));
-                                if (fabsf(__fsub_rn(qx, cxp)) >= 0.5f || fabsf(__fsub_rn(qy, cyp)) >= 0.5f) continue;
-                            }
-                            float frac;
-                            if (!compute_fraction(P0.x, P0.y, P1.x, P1.y, (float)i, ylo, (float)(i + 1), yhi, frac)) continue;
-                            // inside test of the pixel centre: the same coverage rule
-                            bool inside = false;
-                            if (!overflow && !cover_slow && centre_row) {
-                                for (int kk = 0; kk < m; ++kk) inside ^= (i < my_cross[kk]);
-                            } else if (centre_row) {
-                                for (int kk = 0; kk < n; ++kk) {
-                                    int2 A = pv[kk];
-                                    int2 B = pv[(kk + 1 == n) ? 0 : kk + 1];
-                                    if (cross_row(A.y, B.y, cy)) inside ^= (i < cross_L(A.x, A.y, B.x, B.y, cy));
-                                }
-                            }
-                            if (frac > 0.5f) frac = __fsub_rn(1.0f, frac);
-                            int toAdd = (int)ceilf(__fmul_rn(frac, (float)val));
-                            if (inside) { b_fp += toAdd; b_fp1 += val; }
-                            else        { b_fn += toAdd; b_fn1 += val; }
-                        }
-                    }
-                }
-                __syncwarp();
             }
             __syncwarp();
         }
-        if (MODE != MODE_LABEL) {
+        if (MODE == MODE_LABEL) {
+            acc_c = warp_sum_u64(acc_c);
+            if (lane == 0 && acc_c) atomicAdd(a.covered, acc_c);
+        } else {
             acc_c = warp_sum_u64(acc_c);
             if (a.canvas_s) acc_s = warp_sum_f64(acc_s);
             if (lane == 0 && acc_c) atomicAdd(a.out_count + p, acc_c);
@@ -415,6 +460,7 @@ __global__ void k_grid_fill(GridArgs g) {
             size_t cell = (size_t)y * g.res + x;
             int pos = g.cell_start[cell] + atomicAdd(g.cursor + cell, 1);
             g.entries[pos] = p;
+            if (g.pair_cell) g.pair_cell[pos] = (int)cell;
         }
     }
 }
@@ -428,6 +474,204 @@ __global__ void k_grid_sort(const int* __restrict__ cell_start, int* __restrict_
             while (j >= s && entries[j] > v) { entries[j + 1] = entries[j]; --j; }
             entries[j + 1] = v;
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Classified grid.  For the pair (cell c, polygon p) let R be the cell grown
+// by `margin` (>= the fp32 error of the crossing test, of the point-to-cell
+// assignment and of the relative coordinates used here).  If no edge of p
+// meets R, every point assigned to c has the same crossing-number result as
+// the cell centre: the pair is FULL or OUT.  Otherwise only edges whose
+// y-extent meets R's rows can toggle a point of c; of those, edges entirely
+// left of R never toggle and edges entirely right of R toggle exactly when
+// they straddle the point's y.  Candidate pairs are polygon-major: polygon
+// p owns pairs [pair_off[p], pair_off[p+1]) over its candidate cell range.
+struct CellRect {
+    float cx, cy;      // centre
+    float hw, hh;      // half extents grown by the margin
+};
+
+__device__ __forceinline__ int pair_poly(const ClsArgs& a, int k) {
+    int lo = 0, hi = a.P - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(a.pair_off + mid) <= k) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int pair_cell(const ClsArgs& a, int k, int p) {
+    const int4 r = __ldg(a.prange + p);
+    const int w = r.y - r.x;
+    const int l = k - __ldg(a.pair_off + p);
+    return (r.z + l / w) * a.res + (r.x + l % w);
+}
+
+__device__ __forceinline__ CellRect cell_rect(const ClsArgs& a, int cell) {
+    const int gx = cell % a.res, gy = cell / a.res;
+    float x0 = a.lbx + (float)gx * a.csx, x1 = a.lbx + (float)(gx + 1) * a.csx;
+    float y0 = a.lby + (float)gy * a.csy, y1 = a.lby + (float)(gy + 1) * a.csy;
+    // cell 0 also receives points with (p - lb)/cs in (-1, 0): int() truncates
+    if (gx == 0) x0 = a.lbx - a.csx;
+    if (gy == 0) y0 = a.lby - a.csy;
+    CellRect r;
+    r.cx = 0.5f * (x0 + x1);
+    r.cy = 0.5f * (y0 + y1);
+    r.hw = 0.5f * (x1 - x0) + a.margin;
+    r.hh = 0.5f * (y1 - y0) + a.margin;
+    return r;
+}
+
+// Does the segment a-b meet the box [-hw,hw] x [-hh,hh]?  (Liang-Barsky)
+__device__ __forceinline__ bool seg_meets_box(float ax, float ay, float bx, float by, float hw, float hh) {
+    if (fmaxf(ax, bx) < -hw || fminf(ax, bx) > hw || fmaxf(ay, by) < -hh || fminf(ay, by) > hh) return false;
+    float t0 = 0.0f, t1 = 1.0f;
+    const float dx = bx - ax, dy = by - ay;
+    const float p[4] = {-dx, dx, -dy, dy};
+    const float q[4] = {ax + hw, hw - ax, ay + hh, hh - ay};
+    #pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (p[i] == 0.0f) {
+            if (q[i] < 0.0f) return false;
+        } else {
+            float r = q[i] / p[i];
+            if (p[i] < 0.0f) t0 = fmaxf(t0, r);
+            else t1 = fminf(t1, r);
+            if (t0 > t1) return false;
+        }
+    }
+    return true;
+}
+
+// per edge of the pair: bit0 meets R, bit1 kept (may toggle), bit2 straddle-only
+__device__ __forceinline__ int edge_class(const CellRect& r, float2 vi, float2 vj) {
+    const float ax = vi.x - r.cx, ay = vi.y - r.cy;
+    const float bx = vj.x - r.cx, by = vj.y - r.cy;
+    int c = seg_meets_box(ax, ay, bx, by, r.hw, r.hh) ? 1 : 0;
+    const bool band = !(fmaxf(ay, by) < -r.hh || fminf(ay, by) > r.hh) && !(fmaxf(ax, bx) < -r.hw);
+    if (band) {
+        c |= 2;
+        if (fminf(ax, bx) > r.hw) c |= 4;
+    }
+    return c;
+}
+
+__global__ void k_cls_classify(ClsArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const unsigned FULL = 0xffffffffu;
+    for (int k = wid; k < a.npairs; k += nw) {
+        const int p = pair_poly(a, k);
+        const int cell = pair_cell(a, k, p);
+        const int v0 = __ldg(a.pindex + p), n = __ldg(a.pindex + p + 1) - v0;
+        const CellRect r = cell_rect(a, cell);
+        int meets = 0, nr = 0, nf = 0;
+        bool inside = false;
+        for (int e0 = 0; e0 < n; e0 += 32) {
+            int e = e0 + lane;
+            int c = 0;
+            bool tog = false;
+            if (e < n) {
+                float2 vi = __ldg(a.verts + v0 + e);
+                float2 vj = __ldg(a.verts + v0 + (e == 0 ? n - 1 : e - 1));
+                c = edge_class(r, vi, vj);
+                tog = edge_toggles(vi.x, vi.y, vj.x, vj.y, r.cx, r.cy);
+            }
+            meets += __popc(__ballot_sync(FULL, c & 1));
+            nr += __popc(__ballot_sync(FULL, (c & 6) == 6));
+            nf += __popc(__ballot_sync(FULL, (c & 6) == 2));
+            inside ^= (__popc(__ballot_sync(FULL, tog)) & 1) != 0;
+        }
+        if (lane == 0) {
+            int4 info;
+            if (meets == 0) info = make_int4(p, inside ? -1 : -2, 0, cell);
+            else info = make_int4(p, nr, nf, cell);
+            a.info[k] = info;
+            a.ecount[k] = (meets == 0) ? 0 : nr + nf;
+            if (info.y != -2) atomicAdd(a.cell_kept + cell, 1);
+        }
+    }
+}
+
+// Kept pairs into the cell-major list (order inside a cell is immaterial).
+__global__ void k_cls_emit(ClsArgs a) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.npairs; k += gridDim.x * blockDim.x) {
+        int4 in = a.info[k];
+        if (in.y == -2) continue;
+        const int cell = in.w;
+        const int pos = a.cell_start[cell] + atomicAdd(a.cursor + cell, 1);
+        in.w = a.eoff[k];
+        a.entries[pos] = in;
+    }
+}
+
+__global__ void k_cls_fill_edges(ClsArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const unsigned FULL = 0xffffffffu;
+    for (int k = wid; k < a.npairs; k += nw) {
+        if (a.ecount[k] == 0) continue;
+        const int4 in = a.info[k];
+        const int p = in.x, cell = in.w, nr = in.y;
+        const int v0 = __ldg(a.pindex + p), n = __ldg(a.pindex + p + 1) - v0;
+        const CellRect r = cell_rect(a, cell);
+        float4* out = a.edges + a.eoff[k];
+        int wr = 0, wf = nr;
+        for (int e0 = 0; e0 < n; e0 += 32) {
+            int e = e0 + lane;
+            int c = 0;
+            float2 vi = make_float2(0.f, 0.f), vj = vi;
+            if (e < n) {
+                vi = __ldg(a.verts + v0 + e);
+                vj = __ldg(a.verts + v0 + (e == 0 ? n - 1 : e - 1));
+                c = edge_class(r, vi, vj);
+            }
+            const bool is_r = (c & 6) == 6, is_f = (c & 6) == 2;
+            const unsigned mr = __ballot_sync(FULL, is_r), mf = __ballot_sync(FULL, is_f);
+            const unsigned below = (1u << lane) - 1u;
+            if (is_r) out[wr + __popc(mr & below)] = make_float4(vi.x, vi.y, vj.x, vj.y);
+            if (is_f) out[wf + __popc(mf & below)] = make_float4(vi.x, vi.y, vj.x, vj.y);
+            wr += __popc(mr);
+            wf += __popc(mf);
+        }
+    }
+}
+
+// Count labelled pixels (a polygon set overlaps iff fewer pixels carry a
+// label than polygon coverages were written) and fuse the dilated border mask
+// of the hybrid canvas into the label map.
+__global__ void k_label_finish(uint16_t* __restrict__ label, const uint32_t* __restrict__ mask, int resx, int resy,
+                               int ntiles, int words, unsigned long long* __restrict__ nonempty) {
+    const size_t tile_px = (size_t)resx * resy;
+    const size_t total = tile_px * ntiles;
+    unsigned long long cnt = 0;
+    for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < total; g += (size_t)gridDim.x * blockDim.x) {
+        uint16_t l = label[g];
+        cnt += (l != kEmptyLabel);
+        if (mask) {
+            size_t r = g % tile_px;
+            int j = (int)(r / resx), i = (int)(r % resx);
+            if ((__ldg(mask + (size_t)j * words + (i >> 5)) >> (i & 31)) & 1u) label[g] = kBorderLabel;
+        }
+    }
+    cnt = warp_sum_u64(cnt);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(nonempty, cnt);
+}
+
+// Per classified cell: the polygon id when the cell lies inside exactly one
+// polygon and needs no test, else kCodeEmpty / kCodeList.
+__global__ void k_cls_codes(const int* __restrict__ cell_start, const int4* __restrict__ entries,
+                            uint32_t* __restrict__ code, int ncells) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += gridDim.x * blockDim.x) {
+        const int s = cell_start[c], e = cell_start[c + 1];
+        uint32_t v;
+        if (e == s) v = kCodeEmpty;
+        else if (e == s + 1 && entries[s].y == -1) v = (uint32_t)entries[s].x;
+        else v = kCodeList;
+        code[c] = v;
     }
 }
 
@@ -463,7 +707,7 @@ __device__ int block_exclusive_scan(int v, int* s_warp) {
     return r;
 }
 
-__global__ void k_scan_tiles(const int* __restrict__ in, int* __restrict__ out, int n, int* __restrict__ tile_sums) {
+__global__ void k_scan_tiles(const int* in, int* out, int n, int* __restrict__ tile_sums) {
     __shared__ int s_warp[32];
     const size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
     int v[kScanItems];
@@ -589,12 +833,17 @@ void launch_transform_vertices(const float2* verts, int V, const float4* colxf, 
     ++g_kernel_launches;
 }
 
+void launch_poly_info(int mode, const PolyPassArgs& a, int sms, cudaStream_t st) {
+    int items = a.T * a.P;
+    int blocks = std::min((items * 32 + 255) / 256, sms * 8);
+    if (blocks < 1) blocks = 1;
+    ++g_kernel_launches;
+    if (mode == MODE_BOUNDS) k_poly_info<MODE_BOUNDS><<<blocks, 256, 0, st>>>(a);
+    else k_poly_info<MODE_REDUCE><<<blocks, 256, 0, st>>>(a);
+}
+
 void launch_poly_pass(int mode, const PolyPassArgs& a, int sms, cudaStream_t st) {
     int blocks = sms * 4;
-    int items = a.T * a.P;
-    int need = (items + kPolyWarps - 1) / kPolyWarps;
-    if (blocks > need) blocks = need;
-    if (blocks < 1) blocks = 1;
     ++g_kernel_launches;
     switch (mode) {
         case MODE_REDUCE: k_poly_pass<MODE_REDUCE><<<blocks, kPolyWarps * 32, 0, st>>>(a); break;
@@ -622,17 +871,72 @@ void launch_grid_sort(const int* cell_start, int* entries, int ncells, int sms, 
     ++g_kernel_launches;
 }
 
-int scan_tmp_ints(int n) { return (n + kScanTile - 1) / kScanTile + 1; }
+// Scratch ints for launch_exclusive_scan: one level of tile sums per 4096x.
+int scan_tmp_ints(int n) {
+    int total = 0;
+    int m = n;
+    do {
+        int ntiles = (m + kScanTile - 1) / kScanTile;
+        if (ntiles < 1) ntiles = 1;
+        total += ntiles + 1;
+        m = ntiles;
+    } while (m > kScanTile);
+    return total + 1;
+}
 
 bool launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_t st) {
     int ntiles = (n + kScanTile - 1) / kScanTile;
     if (ntiles < 1) ntiles = 1;
-    if (ntiles > kScanTile) return false;
     k_scan_tiles<<<ntiles, kScanThreads, 0, st>>>(in, out, n, tmp);
-    k_scan_sums<<<1, kScanThreads, 0, st>>>(tmp, ntiles, out + n);
+    if (ntiles <= kScanTile) {
+        k_scan_sums<<<1, kScanThreads, 0, st>>>(tmp, ntiles, out + n);
+        g_kernel_launches += 2;
+    } else {
+        // scan the tile sums recursively (in place through a second buffer level)
+        int* sums = tmp;
+        int* next = tmp + ntiles + 1;
+        if (!launch_exclusive_scan(sums, sums, ntiles, next, st)) return false;
+        // out[n] = total of all tiles = scanned sums[ntiles]
+        cudaMemcpyAsync(out + n, sums + ntiles, sizeof(int), cudaMemcpyDeviceToDevice, st);
+        g_kernel_launches += 1;
+    }
     k_scan_add<<<(n + 255) / 256, 256, 0, st>>>(out, n, tmp);
-    g_kernel_launches += 3;
+    g_kernel_launches += 1;
     return true;
+}
+
+void launch_cls_classify(const ClsArgs& c, int sms, cudaStream_t st) {
+    int blocks = (int)std::min<long long>(((long long)c.npairs * 32 + 255) / 256, (long long)sms * 32);
+    if (blocks < 1) blocks = 1;
+    ++g_kernel_launches;
+    k_cls_classify<<<blocks, 256, 0, st>>>(c);
+}
+void launch_cls_emit(const ClsArgs& c, int sms, cudaStream_t st) {
+    int blocks = std::min((c.npairs + 255) / 256, sms * 16);
+    if (blocks < 1) blocks = 1;
+    ++g_kernel_launches;
+    k_cls_emit<<<blocks, 256, 0, st>>>(c);
+}
+void launch_cls_fill_edges(const ClsArgs& c, int sms, cudaStream_t st) {
+    int blocks = (int)std::min<long long>(((long long)c.npairs * 32 + 255) / 256, (long long)sms * 32);
+    if (blocks < 1) blocks = 1;
+    ++g_kernel_launches;
+    k_cls_fill_edges<<<blocks, 256, 0, st>>>(c);
+}
+void launch_label_finish(uint16_t* label, const uint32_t* mask, int resx, int resy, int ntiles, int words,
+                         unsigned long long* nonempty, int sms, cudaStream_t st) {
+    size_t total = (size_t)resx * resy * ntiles;
+    int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)sms * 16);
+    if (blocks < 1) blocks = 1;
+    ++g_kernel_launches;
+    k_label_finish<<<blocks, 256, 0, st>>>(label, mask, resx, resy, ntiles, words, nonempty);
+}
+void launch_cls_codes(const int* cell_start, const int4* entries, uint32_t* code, int ncells, int sms,
+                      cudaStream_t st) {
+    int blocks = std::min((ncells + 255) / 256, sms * 16);
+    if (blocks < 1) blocks = 1;
+    ++g_kernel_launches;
+    k_cls_codes<<<blocks, 256, 0, st>>>(cell_start, entries, code, ncells);
 }
 
 void launch_outline_mask(const float2* verts, const int* pindex, int P, const int* edge_poly, int V,

@@ -39,8 +39,15 @@ struct GridCache {
     bool valid = false;
     int res = 0;
     int clamp = 0;
-    float lbx = 0, lby = 0, csx = 0, csy = 0;
+    bool pair_cell = false;
     size_t nentries = 0;
+};
+
+struct ExactCache {
+    bool valid = false;
+    int res = 0;
+    int user_res = 0;
+    size_t nentries = 0, nedges = 0;
 };
 
 }  // namespace
@@ -63,6 +70,7 @@ struct rj_ctx {
     int P = 0, V = 0;
     std::vector<float> h_xy;
     std::vector<int> h_pindex;
+    std::vector<float4> h_mbr;      // per polygon (minx, miny, maxx, maxy)
     double bbox[4] = {0, 0, 0, 0};
     float max_abs_coord = 0.f, max_edge_dx = 0.f, max_edge_dy = 0.f;
     DevBuf d_verts, d_pindex, d_edge_poly;
@@ -70,6 +78,7 @@ struct rj_ctx {
     int overlap_known = -1;   // -1 unknown, 0 no overlap, 1 overlap
 
     GridCache grid;
+    ExactCache exact;
     std::map<std::string, DevBuf> scratch;
 
     rj_timings tm{};
@@ -294,7 +303,7 @@ int transform_vertices(rj_ctx* ctx, const std::vector<float4>& colxf, const std:
 }
 
 // Grid index (GLFunction::createPolyIndex GLFunction.cpp:65-156).
-int build_grid(rj_ctx* ctx, int res, int clamp, IndexArgs& ia) {
+int build_grid(rj_ctx* ctx, int res, int clamp, IndexArgs& ia, bool with_pair_cell = false) {
     if (res <= 0 || res > 8192) return fail(ctx, RJ_E_INVALID, "grid resolution %d out of range", res);
     GridCache& g = ctx->grid;
     const double dx = ctx->bbox[2] - ctx->bbox[0], dy = ctx->bbox[3] - ctx->bbox[1];
@@ -303,7 +312,7 @@ int build_grid(rj_ctx* ctx, int res, int clamp, IndexArgs& ia) {
     int *cell_start, *entries;
     int rc;
     const size_t ncells = (size_t)res * res;
-    if (!(g.valid && g.res == res && g.clamp == clamp)) {
+    if (!(g.valid && g.res == res && g.clamp == clamp && (g.pair_cell || !with_pair_cell))) {
         int *cnt, *cursor, *tmp;
         if ((rc = scratch_t(ctx, "grid_cnt", ncells, &cnt))) return rc;
         if ((rc = scratch_t(ctx, "grid_start", ncells + 1, &cell_start))) return rc;
@@ -329,6 +338,8 @@ int build_grid(rj_ctx* ctx, int res, int clamp, IndexArgs& ia) {
         ga.cell_start = cell_start;
         ga.cursor = cursor;
         ga.entries = entries;
+        ga.pair_cell = nullptr;
+        if (with_pair_cell && (rc = scratch_t(ctx, "grid_pair_cell", (size_t)std::max(total, 1), &ga.pair_cell))) return rc;
         launch_grid_fill(ga, ctx->sms, ctx->stream);
         launch_grid_sort(cell_start, entries, (int)ncells, ctx->sms, ctx->stream);
         RJ_CUDA(cudaGetLastError());
@@ -336,6 +347,7 @@ int build_grid(rj_ctx* ctx, int res, int clamp, IndexArgs& ia) {
         g.res = res;
         g.clamp = clamp;
         g.nentries = (size_t)total;
+        g.pair_cell = with_pair_cell;
     } else {
         if ((rc = scratch_t(ctx, "grid_start", ncells + 1, &cell_start))) return rc;
         if ((rc = scratch_t(ctx, "grid_entries", std::max<size_t>(g.nentries, 1), &entries))) return rc;
@@ -346,6 +358,144 @@ int build_grid(rj_ctx* ctx, int res, int clamp, IndexArgs& ia) {
     ia.entries = entries;
     ia.lbx = lbx; ia.lby = lby; ia.csx = csx; ia.csy = csy;
     ia.res = res;
+    return RJ_OK;
+}
+
+// Resolution of the classified grid: the query grid times 2^k, about 1024
+// cells across, with cells much larger than the fp32 error of the test.
+int exact_res(const rj_ctx* ctx, int res) {
+    const double ext = std::max(ctx->bbox[2] - ctx->bbox[0], ctx->bbox[3] - ctx->bbox[1]);
+    const double err = std::ldexp(1.0, -21) * (ctx->max_abs_coord + 6.0 * std::max(ctx->max_edge_dx, ctx->max_edge_dy) + 1.0);
+    int g = res;
+    while (g * 2 <= 1024 && ext / (g * 2) > 64.0 * err) g *= 2;
+    return g;
+}
+
+// Classified grid (FULL / OUT / EDGE per cell and candidate polygon).  The
+// candidates of a cell are exactly the reference's: polygons whose MBR cell
+// range on the query grid (index-size.glsl:50-68, upper bound clamped to the
+// grid) contains the query-grid cell holding it; every query-grid cell is a
+// block of 2^k x 2^k classified cells.
+int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix) {
+    int rc;
+    const int G = exact_res(ctx, user_res);
+    const int scale = G / user_res;
+    ExactCache& xc = ctx->exact;
+    const size_t ncells = (size_t)G * G;
+    const double dx = ctx->bbox[2] - ctx->bbox[0], dy = ctx->bbox[3] - ctx->bbox[1];
+    const float lbx = (float)ctx->bbox[0], lby = (float)ctx->bbox[1];
+    const float csx = (float)(dx / G), csy = (float)(dy / G);
+    int* start2;
+    int4* entries2;
+    float4* edges;
+    if (!(xc.valid && xc.res == G && xc.user_res == user_res)) {
+        // candidate ranges on the query grid, in fp32 as the reference computes them
+        const float rcsx = (float)(dx / user_res), rcsy = (float)(dy / user_res);
+        const int P = ctx->P;
+        std::vector<int> off(P + 1);
+        std::vector<int4> rng(P);
+        long long total = 0;
+        for (int p = 0; p < P; ++p) {
+            off[p] = (int)total;
+            const float4 m = ctx->h_mbr[p];
+            int stx = 0, sty = 0, enx = 0, eny = 0;
+            if (ctx->h_pindex[p + 1] > ctx->h_pindex[p]) {
+                volatile float ax = m.x - lbx, ay = m.y - lby, bx = m.z - lbx, by = m.w - lby;
+                volatile float qx0 = ax / rcsx, qy0 = ay / rcsy, qx1 = bx / rcsx, qy1 = by / rcsy;
+                stx = (int)qx0; sty = (int)qy0;
+                enx = (int)qx1 + 1; eny = (int)qy1 + 1;
+                if (enx >= user_res) enx = user_res;
+                if (eny >= user_res) eny = user_res;
+                if (stx < 0) stx = 0;
+                if (sty < 0) sty = 0;
+                if (enx < stx) enx = stx;
+                if (eny < sty) eny = sty;
+            }
+            rng[p] = make_int4(stx * scale, enx * scale, sty * scale, eny * scale);
+            total += (long long)(enx - stx) * (eny - sty) * scale * scale;
+        }
+        off[P] = (int)total;
+        if (total > (1LL << 30)) return fail(ctx, RJ_E_UNSUPPORTED, "too many cell/polygon candidate pairs (%lld)", total);
+        const int npairs = (int)total;
+        int *doff, *ecount, *eoff, *cell_kept, *cursor, *tmp;
+        int4 *drng, *info;
+        if ((rc = scratch_t(ctx, "cls_off", (size_t)P + 1, &doff))) return rc;
+        if ((rc = scratch_t(ctx, "cls_rng", (size_t)P, &drng))) return rc;
+        if ((rc = scratch_t(ctx, "cls_info", (size_t)std::max(npairs, 1), &info))) return rc;
+        if ((rc = scratch_t(ctx, "cls_ecount", (size_t)std::max(npairs, 1), &ecount))) return rc;
+        if ((rc = scratch_t(ctx, "cls_eoff", (size_t)npairs + 1, &eoff))) return rc;
+        if ((rc = scratch_t(ctx, "cls_kept", ncells, &cell_kept))) return rc;
+        if ((rc = scratch_t(ctx, "cls_cursor", ncells, &cursor))) return rc;
+        if ((rc = scratch_t(ctx, "cls_start", ncells + 1, &start2))) return rc;
+        const int ntmp = std::max(scan_tmp_ints((int)ncells), scan_tmp_ints(std::max(npairs, 1)));
+        if ((rc = scratch_t(ctx, "cls_tmp", (size_t)ntmp, &tmp))) return rc;
+        RJ_CUDA(cudaMemcpyAsync(doff, off.data(), sizeof(int) * (P + 1), cudaMemcpyHostToDevice, ctx->stream));
+        RJ_CUDA(cudaMemcpyAsync(drng, rng.data(), sizeof(int4) * P, cudaMemcpyHostToDevice, ctx->stream));
+        RJ_CUDA(cudaMemsetAsync(cell_kept, 0, ncells * sizeof(int), ctx->stream));
+        RJ_CUDA(cudaMemsetAsync(cursor, 0, ncells * sizeof(int), ctx->stream));
+        ClsArgs c{};
+        c.verts = (const float2*)ctx->d_verts.p;
+        c.pindex = (const int*)ctx->d_pindex.p;
+        c.P = P;
+        c.pair_off = doff;
+        c.prange = drng;
+        c.npairs = npairs;
+        c.lbx = lbx; c.lby = lby; c.csx = csx; c.csy = csy;
+        c.res = G;
+        const double U = std::ldexp(1.0, -24);
+        const double Mc = std::max<double>(ctx->max_abs_coord, std::max(std::fabs(ctx->bbox[0]), std::fabs(ctx->bbox[2])));
+        const double E = 8.0 * U * (Mc + 6.0 * std::max(ctx->max_edge_dx, ctx->max_edge_dy));
+        const double delta = 8.0 * U * (2.0 * Mc + G * std::max((double)csx, (double)csy));
+        const double rel = 8.0 * U * (Mc + G * std::max((double)csx, (double)csy));
+        c.margin = (float)(2.0 * (E + delta + rel) + 1e-7 * std::max(dx, dy));
+        c.info = info;
+        c.ecount = ecount;
+        c.eoff = eoff;
+        c.cell_kept = cell_kept;
+        c.cell_start = start2;
+        c.cursor = cursor;
+        if (npairs > 0) launch_cls_classify(c, ctx->sms, ctx->stream);
+        if (!launch_exclusive_scan(cell_kept, start2, (int)ncells, tmp, ctx->stream))
+            return fail(ctx, RJ_E_INVALID, "classified grid too large");
+        int totals[2] = {0, 0};
+        if (npairs > 0) {
+            if (!launch_exclusive_scan(ecount, eoff, npairs, tmp, ctx->stream))
+                return fail(ctx, RJ_E_UNSUPPORTED, "too many cell/polygon pairs to scan (%d)", npairs);
+            RJ_CUDA(cudaMemcpyAsync(&totals[1], eoff + npairs, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        RJ_CUDA(cudaMemcpyAsync(&totals[0], start2 + ncells, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        if ((rc = scratch_t(ctx, "cls_entries", (size_t)std::max(totals[0], 1), &entries2))) return rc;
+        if ((rc = scratch_t(ctx, "cls_edges", (size_t)std::max(totals[1], 1), &edges))) return rc;
+        c.entries = entries2;
+        c.edges = edges;
+        uint32_t* code;
+        if ((rc = scratch_t(ctx, "cls_code", ncells, &code))) return rc;
+        if (npairs > 0) {
+            launch_cls_emit(c, ctx->sms, ctx->stream);
+            launch_cls_fill_edges(c, ctx->sms, ctx->stream);
+        }
+        launch_cls_codes(start2, entries2, code, (int)ncells, ctx->sms, ctx->stream);
+        RJ_CUDA(cudaGetLastError());
+        xc.valid = true;
+        xc.res = G;
+        xc.user_res = user_res;
+        xc.nentries = (size_t)totals[0];
+        xc.nedges = (size_t)totals[1];
+    } else {
+        if ((rc = scratch_t(ctx, "cls_start", ncells + 1, &start2))) return rc;
+        if ((rc = scratch_t(ctx, "cls_entries", std::max<size_t>(xc.nentries, 1), &entries2))) return rc;
+        if ((rc = scratch_t(ctx, "cls_edges", std::max<size_t>(xc.nedges, 1), &edges))) return rc;
+    }
+    ix.code = (const uint32_t*)ctx->scratch["cls_code"].p;
+    ix.cell_start = start2;
+    ix.entries = entries2;
+    ix.edges = edges;
+    ix.lbx = lbx;
+    ix.lby = lby;
+    ix.csx = csx;
+    ix.csy = csy;
+    ix.res = G;
     return RJ_OK;
 }
 
@@ -390,16 +540,58 @@ struct ExecState {
 
 int poly_pass(rj_ctx* ctx, int mode, PolyPassArgs& a) {
     unsigned int* ctr;
-    int* flag;
     int rc;
+    const int TP = a.T * a.P;
+    int4* info_a;
+    int2* info_b;
+    int *nbands, *band_start, *tmp;
     if ((rc = scratch_t(ctx, "work_ctr", 1, &ctr))) return rc;
-    if ((rc = scratch_t(ctx, "flag", 1, &flag))) return rc;
+    if ((rc = scratch_t(ctx, "pp_info_a", TP, &info_a))) return rc;
+    if ((rc = scratch_t(ctx, "pp_info_b", TP, &info_b))) return rc;
+    if ((rc = scratch_t(ctx, "pp_nbands", TP, &nbands))) return rc;
+    if ((rc = scratch_t(ctx, "pp_band_start", (size_t)TP + 1, &band_start))) return rc;
+    if ((rc = scratch_t(ctx, "pp_tmp", (size_t)scan_tmp_ints(TP), &tmp))) return rc;
     RJ_CUDA(cudaMemsetAsync(ctr, 0, sizeof(unsigned), ctx->stream));
-    RJ_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream));
     a.work_ctr = ctr;
-    a.flag = flag;
+    a.info_a = info_a;
+    a.info_b = info_b;
+    a.nbands = nbands;
+    a.band_start = band_start;
+    launch_poly_info(mode, a, ctx->sms, ctx->stream);
+    if (!launch_exclusive_scan(nbands, band_start, TP, tmp, ctx->stream))
+        return fail(ctx, RJ_E_INVALID, "too many (tile, polygon) items");
     launch_poly_pass(mode, a, ctx->sms, ctx->stream);
     RJ_CUDA(cudaGetLastError());
+    return RJ_OK;
+}
+
+// Polygon label map of a canvas (MODE_LABEL).  Returns 1 in *overlap when
+// some pixel centre lies in two polygons (the label map cannot represent the
+// set; the canvas path is used instead).
+int label_map(rj_ctx* ctx, PolyPassArgs& a, const char* key, size_t npix, const uint32_t* mask, int words,
+              uint16_t** out, int* overlap) {
+    int rc;
+    uint16_t* label;
+    unsigned long long* cnt;
+    if ((rc = scratch_t(ctx, key, npix, &label))) return rc;
+    if ((rc = scratch_t(ctx, "label_counts", 2, &cnt))) return rc;
+    RJ_CUDA(cudaMemsetAsync(label, 0xFF, npix * sizeof(uint16_t), ctx->stream));
+    RJ_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    a.label = label;
+    a.covered = cnt;
+    if ((rc = poly_pass(ctx, MODE_LABEL, a))) return rc;
+    launch_label_finish(label, mask, a.resx, a.resy, a.T, words, cnt + 1, ctx->sms, ctx->stream);
+    RJ_CUDA(cudaGetLastError());
+    *overlap = 0;
+    if (ctx->overlap_known != 0) {
+        unsigned long long h[2] = {0, 0};
+        RJ_CUDA(cudaMemcpyAsync(h, cnt, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        *overlap = h[0] != h[1];
+        ctx->overlap_known = *overlap;
+    }
+    *out = label;
+    a.label = nullptr;
     return RJ_OK;
 }
 
@@ -437,24 +629,14 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
     a.out_bounds = es.out_bounds;
     a.line_filter = (q->flags & RJ_FLAG_LINE_FILTER) ? 1 : 0;
 
-    bool use_label = !bounds && !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->overlap_known != 1;
+    bool use_label = !bounds && !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->overlap_known != 1 &&
+                     ctx->P <= kMaxLabelPolys;
     if (use_label) {
-        uint32_t* label;
-        if ((rc = scratch_t(ctx, "label", npix, &label))) return rc;
-        RJ_CUDA(cudaMemsetAsync(label, 0xFF, npix * sizeof(uint32_t), ctx->stream));
-        a.label = label;
-        if ((rc = poly_pass(ctx, MODE_LABEL, a))) return rc;
-        int flag = 0;
-        RJ_CUDA(cudaMemcpyAsync(&flag, a.flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
-        if (flag & 1) {
-            ctx->overlap_known = 1;
-            use_label = false;
-        } else {
-            ctx->overlap_known = 0;
-        }
+        uint16_t* label;
+        int overlap = 0;
+        if ((rc = label_map(ctx, a, "label", npix, nullptr, 0, &label, &overlap))) return rc;
         es.ph->mark(2);
-        if (use_label) {
+        if (!overlap) {
             PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
             launch_raster_label(pa, cx, label, ctx->sms, ctx->stream);
             RJ_CUDA(cudaGetLastError());
@@ -486,35 +668,50 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
     return RJ_OK;
 }
 
-// Index join (IndexJoin::performJoin IndexJoin.cpp:156-166).
+// Index join (IndexJoin::performJoin IndexJoin.cpp:156-166).  Default: the
+// classified grid; RJ_FLAG_NO_CELL_CLASSIFY / RJ_FLAG_COMPAT_INDEX_CLAMP: the
+// plain candidate lists with the full crossing test per candidate.
 int exec_index(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     int rc;
     DevFilter f;
     if ((rc = build_filter(ctx, q, f, false))) return rc;
+    if (q->grid_res <= 0 || q->grid_res > 8192) return fail(ctx, RJ_E_INVALID, "grid resolution %d out of range", q->grid_res);
     es.ph->mark(1);
-    IndexArgs ia{};
-    if ((rc = build_grid(ctx, q->grid_res, (q->flags & RJ_FLAG_COMPAT_INDEX_CLAMP) ? 1 : 0, ia))) return rc;
-    es.ph->mark(2);
+    const bool plain = (q->flags & (RJ_FLAG_NO_CELL_CLASSIFY | RJ_FLAG_COMPAT_INDEX_CLAMP)) != 0;
     PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
-    launch_index_points(pa, ia, ctx->sms, ctx->stream);
+    if (plain) {
+        IndexArgs ia{};
+        if ((rc = build_grid(ctx, q->grid_res, (q->flags & RJ_FLAG_COMPAT_INDEX_CLAMP) ? 1 : 0, ia))) return rc;
+        es.ph->mark(2);
+        launch_index_points(pa, ia, ctx->sms, ctx->stream);
+    } else {
+        ExactIndex ix{};
+        if ((rc = build_exact(ctx, q->grid_res, ix))) return rc;
+        es.ph->mark(2);
+        launch_exact_points(pa, ix, ctx->sms, ctx->stream);
+    }
     RJ_CUDA(cudaGetLastError());
     es.ph->mark(3);
     es.ph->mark(4);
     return RJ_OK;
 }
 
-// Hybrid join (HybridJoin::performJoin HybridJoin.cpp:339-359).
+// Hybrid join (HybridJoin::performJoin HybridJoin.cpp:339-359): points on
+// non-border pixels take the pixel's polygon (label map, or canvas + polygon
+// pass for overlapping polygon sets); points near an outline take the exact
+// test through the grid.
 int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     int rc;
     DevFilter f;
     if ((rc = build_filter(ctx, q, f, false))) return rc;
+    if (q->grid_res <= 0 || q->grid_res > 8192) return fail(ctx, RJ_E_INVALID, "grid resolution %d out of range", q->grid_res);
     es.ph->mark(1);
-    IndexArgs ia{};
-    if ((rc = build_grid(ctx, q->grid_res, 0, ia))) return rc;
+    ExactIndex ix{};
+    if ((rc = build_exact(ctx, q->grid_res, ix))) return rc;
 
-    // canvas: getResolution(bbox, 8192) (HybridJoin.cpp:62-66, Utils.h:29-34)
+    // canvas: getResolution(bbox, fboSize) (HybridJoin.cpp:62-66, Utils.h:29-34)
     const double dx = ctx->bbox[2] - ctx->bbox[0], dy = ctx->bbox[3] - ctx->bbox[1];
-    const int fbo = q->hybrid_canvas > 0 ? q->hybrid_canvas : 8192;
+    const int fbo = q->hybrid_canvas > 0 ? q->hybrid_canvas : 4096;
     const float cellf = (float)std::max(dx / fbo, dy / fbo);
     const int resx = std::max(1, (int)std::fabs(std::ceil(dx / cellf)));
     const int resy = std::max(1, (int)std::fabs(std::ceil(dy / cellf)));
@@ -530,16 +727,17 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
         h.resx = resx;
         h.resy = resy;
     }
-    // border mask: conservative outline + dilation.  The dilation radius
-    // covers the fp32 error of the crossing test expressed in pixels.
+    // Border mask: conservative outline + dilation.  A pixel is safe when no
+    // edge comes within `radius` pixels; the radius covers the fp32 error of
+    // the crossing test expressed in pixels (isBorder's 3x3 for radius 1).
     const int words = (resx + 31) / 32;
     uint32_t *mraw, *mask;
     if ((rc = scratch_t(ctx, "hyb_mraw", (size_t)words * resy, &mraw))) return rc;
     if ((rc = scratch_t(ctx, "hyb_mask", (size_t)words * resy, &mask))) return rc;
     RJ_CUDA(cudaMemsetAsync(mraw, 0, (size_t)words * resy * 4, ctx->stream));
     const double pix_w = std::min(dx / resx, dy / resy);
-    const double err_world = std::ldexp(1.0, -22) * (ctx->max_abs_coord + 6.0 * std::max(ctx->max_edge_dx, ctx->max_edge_dy) + 1.0);
-    const int radius = 1 + (int)std::ceil(err_world / pix_w + 0.1);
+    const double err_world = std::ldexp(1.0, -21) * (ctx->max_abs_coord + 6.0 * std::max(ctx->max_edge_dx, ctx->max_edge_dy) + 1.0);
+    const int radius = std::max(1, (int)std::ceil(err_world / pix_w + 0.05));
     if (radius > 31) return fail(ctx, RJ_E_UNSUPPORTED, "hybrid canvas too fine for fp32 coordinates (radius %d)", radius);
     launch_outline_mask((const float2*)ctx->d_verts.p, (const int*)ctx->d_pindex.p, ctx->P,
                         (const int*)ctx->d_edge_poly.p, ctx->V, h, 0.05f, mraw, words, ctx->sms, ctx->stream);
@@ -574,28 +772,18 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     ha.h = h;
     ha.border = mask;
     ha.words = words;
-    bool use_label = !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->overlap_known != 1;
+    bool use_label = !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->overlap_known != 1 && ctx->P <= kMaxLabelPolys;
     if (use_label) {
-        uint32_t* label;
-        if ((rc = scratch_t(ctx, "hyb_label", npix, &label))) return rc;
-        RJ_CUDA(cudaMemsetAsync(label, 0xFF, npix * sizeof(uint32_t), ctx->stream));
-        a.label = label;
-        if ((rc = poly_pass(ctx, MODE_LABEL, a))) return rc;
-        int flag = 0;
-        RJ_CUDA(cudaMemcpyAsync(&flag, a.flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
-        if (flag & 1) {
-            ctx->overlap_known = 1;
-            use_label = false;
-        } else {
-            ctx->overlap_known = 0;
-            ha.label = label;
-        }
+        uint16_t* label;
+        int overlap = 0;
+        if ((rc = label_map(ctx, a, "hyb_label", npix, mask, words, &label, &overlap))) return rc;
+        if (overlap) use_label = false;
+        else ha.label = label;
     }
     es.ph->mark(2);
     PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
     if (use_label) {
-        launch_hybrid_points(pa, ia, ha, ctx->sms, ctx->stream);
+        launch_hybrid_points(pa, ix, ha, ctx->sms, ctx->stream);
         RJ_CUDA(cudaGetLastError());
         es.ph->mark(3);
         es.ph->mark(4);
@@ -612,7 +800,7 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     ha.canvas_c = canvas_c;
     ha.canvas_s = canvas_s;
     ha.label = nullptr;
-    launch_hybrid_points(pa, ia, ha, ctx->sms, ctx->stream);
+    launch_hybrid_points(pa, ix, ha, ctx->sms, ctx->stream);
     RJ_CUDA(cudaGetLastError());
     es.ph->mark(3);
     // polygon-inside pass over non-border pixels (polygon-inside.frag:30-57)
@@ -645,7 +833,7 @@ void rj_query_init(rj_query* q) {
     q->grid_res = 256;
     q->max_fbo_size = RJ_MAX_FBO_SIZE;
     q->time_attrib = -1;
-    q->hybrid_canvas = 8192;
+    q->hybrid_canvas = 4096;
 }
 
 int rj_create(const rj_config* cfg, rj_ctx** out) {
@@ -862,6 +1050,15 @@ int rj_set_polygons(rj_ctx* ctx, const float* xy, const int32_t* pindex, int32_t
         for (int k = pindex[i]; k < pindex[i + 1]; ++k) edge_poly[k] = i;
     ctx->h_xy.assign(xy, xy + 2 * (size_t)V);
     ctx->h_pindex.assign(pindex, pindex + npolys + 1);
+    ctx->h_mbr.assign(npolys, make_float4(0.f, 0.f, 0.f, 0.f));
+    for (int i = 0; i < npolys; ++i) {
+        float a = INFINITY, b = INFINITY, c = -INFINITY, d = -INFINITY;
+        for (int k = pindex[i]; k < pindex[i + 1]; ++k) {
+            a = std::min(a, xy[2 * k]); c = std::max(c, xy[2 * k]);
+            b = std::min(b, xy[2 * k + 1]); d = std::max(d, xy[2 * k + 1]);
+        }
+        ctx->h_mbr[i] = make_float4(a, b, c, d);
+    }
     RJ_CUDA(cudaMemcpyAsync(ctx->d_verts.p, xy, (size_t)V * 8, cudaMemcpyHostToDevice, ctx->stream));
     RJ_CUDA(cudaMemcpyAsync(ctx->d_pindex.p, pindex, (size_t)(npolys + 1) * 4, cudaMemcpyHostToDevice, ctx->stream));
     RJ_CUDA(cudaMemcpyAsync(ctx->d_edge_poly.p, edge_poly.data(), (size_t)V * 4, cudaMemcpyHostToDevice, ctx->stream));
@@ -875,6 +1072,7 @@ int rj_set_polygons(rj_ctx* ctx, const float* xy, const int32_t* pindex, int32_t
     ctx->poly_version++;
     ctx->overlap_known = -1;
     ctx->grid.valid = false;
+    ctx->exact.valid = false;
     return RJ_OK;
 }
 
@@ -893,6 +1091,7 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
     const int P = ctx->P;
     if (q->flags & RJ_FLAG_NO_CACHE) {
         ctx->grid.valid = false;
+        ctx->exact.valid = false;
         ctx->overlap_known = -1;
     }
     g_kernel_launches = 0;

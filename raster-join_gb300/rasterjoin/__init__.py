@@ -229,7 +229,7 @@ class GLHandler:
         self.ground_resolution = 1.0
         self.presx = 256
         self.max_fbo_size = 8192
-        self.hybrid_canvas = 8192
+        self.hybrid_canvas = 0          # 0: library default
         self.flags = 0
         self._loaded_points = None
         self._loaded_polys = None

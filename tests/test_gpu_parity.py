@@ -319,7 +319,46 @@ def test_hybrid_canvas_size_invariance(handler, c1):
                 ref = got
             np.testing.assert_array_equal(got, ref)
     finally:
-        handler.hybrid_canvas = 8192
+        handler.hybrid_canvas = 0
+
+
+def near_edge_points(verts, pidx, seed=1):
+    """Points on vertices, on edges and within 1e-4..1 m of them."""
+    rng = np.random.default_rng(seed)
+    out = [verts.astype(np.float32)]
+    for p in range(len(pidx) - 1):
+        v = verts[pidx[p]:pidx[p + 1]].astype(np.float64)
+        w = np.roll(v, -1, axis=0)
+        t = rng.random((len(v), 3))
+        for k in range(3):
+            q = v + (w - v) * t[:, k:k + 1]
+            d = w - v
+            nrm = np.c_[-d[:, 1], d[:, 0]] / np.maximum(np.hypot(d[:, 0], d[:, 1]), 1e-9)[:, None]
+            for off in (0.0, 1e-4, -1e-4, 1e-2, -1e-2, 0.5, -0.5):
+                out.append((q + off * nrm).astype(np.float32))
+    xy = np.concatenate(out)
+    return xy[(xy[:, 0] >= 0) & (xy[:, 1] >= 0)]
+
+
+@pytest.mark.parametrize("polys", ["voronoi", "stars"])
+def test_points_on_and_near_edges(handler, polys):
+    if polys == "voronoi":
+        verts, pidx = synth.voronoi_polygons(80, seed=21)
+    else:
+        verts, pidx = synth.star_polygons(60, seed=21, vmin=5, vmax=200, rmin=300, rmax=5000)
+    xy = near_edge_points(verts, pidx)
+    handler.setDataHandler(make_dh({"xy": xy}, verts, pidx))
+    for res in (64, 256):
+        handler.setPolyIndexResolution(res)
+        want, _ = oracle.index_join(xy, verts, pidx, res)
+        np.testing.assert_array_equal(handler.execute(rj.IndexJoinFn).count, want)
+        np.testing.assert_array_equal(handler.execute(rj.HybridJoinFn).count,
+                                      oracle.hybrid_join(xy, verts, pidx, res)[0])
+        handler.flags = rj.FLAG_NO_CELL_CLASSIFY
+        try:
+            np.testing.assert_array_equal(handler.execute(rj.IndexJoinFn).count, want)
+        finally:
+            handler.flags = 0
 
 
 def test_errors_are_status_codes(handler, c1):
