@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--points", type=int, default=100_000_000)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--count-only", action="store_true", help="count instead of avg(a) (diagnostic)")
     return ap.parse_args()
 
 
@@ -229,7 +230,7 @@ def run_gb300(args):
     cons, trange = query_constraints()
     dh.setQueryConstraints(cons)
     dh.setTimeRange(*trange)
-    dh.setAggregation(rj.Avg, 3)
+    dh.setAggregation(rj.Count if args.count_only else rj.Avg, -1 if args.count_only else 3)
     h.setDataHandler(dh)
     h.setAccuracyDistance(10.0 if args.join == "raster" else 100.0)
     h.setPolyIndexResolution(256)

@@ -27,16 +27,38 @@ constexpr float kWinClamp = 1048576.0f;               // |window coord| clamp (2
 // Filter + aggregate description (GLFunction::setupPoints GLFunction.cpp:199-344
 // gathers constraint columns; points.vert:138-159 evaluates them).
 struct DevFilter {
+    int ncol;                                // distinct columns the predicates read
+    const uint32_t* col[kMaxFilters];
+    // Interval form (general == 0): the predicates of column c hold exactly
+    // when order_key(ctyp[c], value) - lo[c] <= span[c] (unsigned).
+    int general;
+    int ctyp[kMaxFilters];
+    uint32_t lo[kMaxFilters], span[kMaxFilters];
+    // General form: predicates of column c: [pstart[c], pstart[c+1])
+    int pstart[kMaxFilters + 1];
     int n;                                   // predicates (constraints + time range)
-    const uint32_t* col[kMaxFilters];        // column of each predicate
     int op[kMaxFilters];                     // rj_constraint_type
     int typ[kMaxFilters];                    // rj_attribute_type of the column
     uint32_t val[kMaxFilters];               // comparison value (bit pattern)
     uint32_t compat_mask;                    // bit k: predicate k uses RJ_FLAG_COMPAT_FLOAT_EQ
     int aggr;                                // 0: count only, else sum of aggr_col
     int aggr_typ;
+    int aggr_ci;                             // index of aggr_col in col[], or -1
     const uint32_t* aggr_col;
+    float sum_scale;                         // 2^(s-32): values are summed as int64 round(v * 2^s)
 };
+
+// Fixed-point value of an aggregate: round(v * 2^s) as int64, from only
+// 32-bit conversions (t = v * 2^(s-32) = hi + r with hi = floor(t), r in
+// [0,1); r * 2^32 needs rounding only when |t| < 1).  |v| * 2^s < 2^63 by the
+// choice of s; non-finite values are summed separately in fp64.
+__device__ __forceinline__ long long fixed_value(float v, float scale) {
+    const float t = __fmul_rn(v, scale);
+    const float hi = floorf(t);
+    const float r = __fsub_rn(t, hi);
+    const unsigned lo = __float2uint_rn(__fmul_rn(r, 4294967296.0f));
+    return (long long)(((unsigned long long)(long long)(int)hi << 32) + (unsigned long long)lo);
+}
 
 // aLessThan / aGreaterThan / aEqual, points.vert:24-85: Uint and Int compare
 // the reinterpreted bits, Float compares as fp32; Location (or anything else)
@@ -112,11 +134,25 @@ __host__ __device__ __forceinline__ float agg_value(int typ, uint32_t a) {
     }
 }
 
+// Order-preserving map of a 4-byte value to uint32: unsigned compare of the
+// keys equals the typed compare of the values (floats: -NaN < -inf < ... <
+// -0 < +0 < ... < +inf < +NaN; the intervals exclude the NaNs).
+__host__ __device__ __forceinline__ uint32_t order_key(int typ, uint32_t a) {
+    if (typ == RJ_INT) return a ^ 0x80000000u;
+    if (typ == RJ_FLOAT) return (a & 0x80000000u) ? ~a : (a | 0x80000000u);
+    return a;
+}
+
 __device__ __forceinline__ bool filter_point(const DevFilter& f, uint64_t i) {
     #pragma unroll 1
-    for (int k = 0; k < f.n; ++k) {
-        uint32_t a = __ldg(f.col[k] + i);
-        if (!pred_eval(f.op[k], f.typ[k], a, f.val[k], (int)((f.compat_mask >> k) & 1u))) return false;
+    for (int c = 0; c < f.ncol; ++c) {
+        const uint32_t a = __ldg(f.col[c] + i);
+        if (!f.general) {
+            if (order_key(f.ctyp[c], a) - f.lo[c] > f.span[c]) return false;
+            continue;
+        }
+        for (int k = f.pstart[c]; k < f.pstart[c + 1]; ++k)
+            if (!pred_eval(f.op[k], f.typ[k], a, f.val[k], (int)((f.compat_mask >> k) & 1u))) return false;
     }
     return true;
 }
@@ -267,6 +303,64 @@ __device__ __forceinline__ double warp_sum_f64(double v) {
     #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
+}
+
+}  // namespace rj
+
+// ---------------------------------------------------------------------------
+// Bulk-copy pipeline primitives (mbarrier + cp.async.bulk, sm_90+ PTX).
+namespace rj {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Wait for the phase of the given parity to complete; false after the
+// iteration limit (the caller records an error and stops).
+constexpr uint32_t kWaitLimit = 1u << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (uint32_t i = 0; i < kWaitLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+// global -> shared bulk copy completing on an mbarrier (16-byte aligned, size % 16 == 0)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar, uint64_t pol) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
+        : "memory");
+}
+__device__ __forceinline__ void named_sync(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
 }  // namespace rj

@@ -21,13 +21,13 @@ struct PolyPassArgs {
     int P, V, T;
     int resx, resy;
     const uint32_t* canvas_c;    // [T][resy][resx] point counts
-    const double* canvas_s;      // [T][resy][resx] sums or null
+    const long long* canvas_s;   // [T][resy][resx] fixed-point sums or null
     uint16_t* label;             // [T][resy][resx] polygon label (MODE_LABEL)
     unsigned long long* covered; // MODE_LABEL: pixels covered, summed over polygons
     const uint32_t* border;      // dilated hybrid border mask (skip) or null
     int border_words;
     unsigned long long* out_count;
-    double* out_sum;
+    unsigned long long* out_sum; // fixed-point sums (int64 two's complement)
     long long* out_bounds;       // [4P]
     unsigned int* work_ctr;
     int line_filter;
@@ -59,20 +59,27 @@ struct ClsArgs {
     const float2* verts;
     const int* pindex;
     int P;
-    const int* pair_off;         // [P+1] first candidate pair of each polygon (polygon-major)
-    const int4* prange;          // [P] candidate cells [stx, enx) x [sty, eny)
-    int npairs;
-    float lbx, lby, csx, csy;    // classified grid lower-left / cell size (fp32, as the points use)
-    int res;
+    // level 1: candidate pairs over coarse cells (the query grid), polygon-major
+    const int* pair_off;         // [P+1] first coarse pair of each polygon
+    const int4* prange;          // [P] coarse candidate cells [stx, enx) x [sty, eny)
+    int npairs;                  // pairs of the level being classified
+    // level 2: explicit (polygon, fine cell) pairs refined from EDGE coarse pairs
+    int2* plist;
+    int* plist_n;
+    int level;                   // 1 or 2
+    int scale;                   // fine cells per coarse cell along an axis
+    float lbx, lby, csx, csy;    // fine grid lower-left / cell size (fp32, as the points use)
+    int res;                     // fine grid resolution
     float margin;                // world units: fp32 error of the test + cell assignment
-    int4* info;                  // per pair: poly, nr (-1 full, -2 out), nf, cell
-    int* ecount;                 // per pair: edges kept
-    const int* eoff;             // per pair: first edge (exclusive scan of ecount)
+    int4* info;                  // level 1: poly, kind (-1 full, -2 out, 0 edge), -, coarse cell
+                                 // level 2: poly, nr (-1 full, -2 out), nf, fine cell
+    int* ecount;                 // level 2: edges kept per pair
+    const int* eoff;             // level 2: first edge (exclusive scan of ecount)
     float4* edges;
-    int* cell_kept;              // per cell: kept pairs
-    const int* cell_start;       // per cell: exclusive scan of cell_kept
+    int* cell_kept;              // per fine cell: kept entries
+    const int* cell_start;       // per fine cell: exclusive scan of cell_kept
     int* cursor;
-    int4* entries;               // cell-major kept pairs: poly, nr, nf, edge offset
+    int4* entries;               // cell-major: poly, nr, nf, edge offset
 };
 
 struct ExactIndex {
@@ -103,7 +110,9 @@ struct PointArgs {
     DevFilter f;
     int P;
     unsigned long long* out_count;
-    double* out_sum;
+    unsigned long long* out_sum; // fixed-point sums (int64 two's complement)
+    double* out_nonfinite;       // fp64 sums of the non-finite aggregate values
+    int* err;                    // bit0: a bounded pipeline wait ran out
 };
 
 // Exact point-in-polygon index (CSR over a uniform grid).
@@ -121,9 +130,13 @@ struct HybridArgs {
     const uint32_t* border;      // dilated border mask [resy][words] (canvas mode)
     int words;
     uint32_t* canvas_c;          // canvas mode: [resy][resx]
-    double* canvas_s;
+    long long* canvas_s;         // fixed-point sums
+    float scale;                 // fixed-point scale 2^(s-32)
     const uint16_t* label;       // label mode: [resy][resx], kBorderLabel on border pixels
 };
+
+// column statistics: largest finite |aggregate value| as float bits (atomicMax)
+void launch_col_absmax(const uint32_t* col, int typ, uint64_t n, unsigned* out_bits, int sms, cudaStream_t st);
 
 // polygon side
 void launch_transform_vertices(const float2* verts, int V, const float4* colxf, const float4* rowxf,
@@ -142,7 +155,7 @@ void launch_dilate_mask(const uint32_t* in, uint32_t* out, int resx, int resy, i
 
 // point side
 // smem_hist: histogram capacity decision done by the launcher.
-void launch_raster_splat(const PointArgs& pa, const CanvasXf& cx, uint32_t* canvas_c, double* canvas_s,
+void launch_raster_splat(const PointArgs& pa, const CanvasXf& cx, uint32_t* canvas_c, long long* canvas_s,
                          int sms, cudaStream_t st);
 void launch_raster_label(const PointArgs& pa, const CanvasXf& cx, const uint16_t* label, int sms,
                          cudaStream_t st);
@@ -153,7 +166,7 @@ void launch_hybrid_points(const PointArgs& pa, const ExactIndex& ix, const Hybri
 
 // classified grid build
 void launch_cls_classify(const ClsArgs& c, int sms, cudaStream_t st);
-void launch_cls_emit(const ClsArgs& c, int sms, cudaStream_t st);
+void launch_cls_emit(const ClsArgs& c, int sms, cudaStream_t st);   // level-1 FULL and level-2 kept pairs
 void launch_cls_fill_edges(const ClsArgs& c, int sms, cudaStream_t st);
 // count labelled pixels (before border marking) and mark border pixels
 void launch_label_finish(uint16_t* label, const uint32_t* mask, int resx, int resy, int ntiles, int words,

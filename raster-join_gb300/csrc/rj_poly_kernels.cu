@@ -235,7 +235,7 @@ k_poly_pass(PolyPassArgs a) {
         const size_t tile_off = (size_t)t * a.resx * a.resy;
 
         unsigned long long acc_c = 0;
-        double acc_s = 0.0;
+        long long acc_s = 0;
         long long b_fn = 0, b_fp = 0, b_fn1 = 0, b_fp1 = 0;
 
         // fixed-point y window of the band (one pixel of margin each side)
@@ -383,9 +383,9 @@ k_poly_pass(PolyPassArgs a) {
             if (lane == 0 && acc_c) atomicAdd(a.covered, acc_c);
         } else {
             acc_c = warp_sum_u64(acc_c);
-            if (a.canvas_s) acc_s = warp_sum_f64(acc_s);
+            if (a.canvas_s) acc_s = (long long)warp_sum_u64((unsigned long long)acc_s);
             if (lane == 0 && acc_c) atomicAdd(a.out_count + p, acc_c);
-            if (lane == 0 && a.canvas_s && acc_s != 0.0) atomicAdd(a.out_sum + p, acc_s);
+            if (lane == 0 && a.canvas_s && acc_s != 0) atomicAdd(a.out_sum + p, (unsigned long long)acc_s);
         }
         if (MODE == MODE_BOUNDS) {
             b_fn = (long long)warp_sum_u64((unsigned long long)b_fn);
@@ -485,8 +485,11 @@ __global__ void k_grid_sort(const int* __restrict__ cell_start, int* __restrict_
 // the cell centre: the pair is FULL or OUT.  Otherwise only edges whose
 // y-extent meets R's rows can toggle a point of c; of those, edges entirely
 // left of R never toggle and edges entirely right of R toggle exactly when
-// they straddle the point's y.  Candidate pairs are polygon-major: polygon
-// p owns pairs [pair_off[p], pair_off[p+1]) over its candidate cell range.
+// they straddle the point's y.
+// Level 1 classifies the candidate pairs on the coarse (query) grid; FULL and
+// OUT results hold for every fine cell inside, EDGE pairs are refined into
+// their scale x scale fine cells and classified again (level 2), keeping the
+// edge lists of the fine EDGE pairs.
 struct CellRect {
     float cx, cy;      // centre
     float hw, hh;      // half extents grown by the margin
@@ -501,17 +504,10 @@ __device__ __forceinline__ int pair_poly(const ClsArgs& a, int k) {
     return lo;
 }
 
-__device__ __forceinline__ int pair_cell(const ClsArgs& a, int k, int p) {
-    const int4 r = __ldg(a.prange + p);
-    const int w = r.y - r.x;
-    const int l = k - __ldg(a.pair_off + p);
-    return (r.z + l / w) * a.res + (r.x + l % w);
-}
-
-__device__ __forceinline__ CellRect cell_rect(const ClsArgs& a, int cell) {
-    const int gx = cell % a.res, gy = cell / a.res;
-    float x0 = a.lbx + (float)gx * a.csx, x1 = a.lbx + (float)(gx + 1) * a.csx;
-    float y0 = a.lby + (float)gy * a.csy, y1 = a.lby + (float)(gy + 1) * a.csy;
+// rectangle of fine cells [gx, gx+n) x [gy, gy+n) of the fine grid
+__device__ __forceinline__ CellRect cells_rect(const ClsArgs& a, int gx, int gy, int n) {
+    float x0 = a.lbx + (float)gx * a.csx, x1 = a.lbx + (float)(gx + n) * a.csx;
+    float y0 = a.lby + (float)gy * a.csy, y1 = a.lby + (float)(gy + n) * a.csy;
     // cell 0 also receives points with (p - lb)/cs in (-1, 0): int() truncates
     if (gx == 0) x0 = a.lbx - a.csx;
     if (gy == 0) y0 = a.lby - a.csy;
@@ -562,20 +558,34 @@ __global__ void k_cls_classify(ClsArgs a) {
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const unsigned FULL = 0xffffffffu;
-    for (int k = wid; k < a.npairs; k += nw) {
-        const int p = pair_poly(a, k);
-        const int cell = pair_cell(a, k, p);
-        const int v0 = __ldg(a.pindex + p), n = __ldg(a.pindex + p + 1) - v0;
-        const CellRect r = cell_rect(a, cell);
+    const int npairs = a.level == 1 ? a.npairs : *a.plist_n;
+    for (int k = wid; k < npairs; k += nw) {
+        int p, gx, gy, n;
+        if (a.level == 1) {
+            p = pair_poly(a, k);
+            const int4 r = __ldg(a.prange + p);
+            const int w = r.y - r.x, l = k - __ldg(a.pair_off + p);
+            gx = (r.x + l % w) * a.scale;
+            gy = (r.z + l / w) * a.scale;
+            n = a.scale;
+        } else {
+            const int2 q = a.plist[k];
+            p = q.x;
+            gx = q.y % a.res;
+            gy = q.y / a.res;
+            n = 1;
+        }
+        const int v0 = __ldg(a.pindex + p), nv = __ldg(a.pindex + p + 1) - v0;
+        const CellRect r = cells_rect(a, gx, gy, n);
         int meets = 0, nr = 0, nf = 0;
         bool inside = false;
-        for (int e0 = 0; e0 < n; e0 += 32) {
+        for (int e0 = 0; e0 < nv; e0 += 32) {
             int e = e0 + lane;
             int c = 0;
             bool tog = false;
-            if (e < n) {
+            if (e < nv) {
                 float2 vi = __ldg(a.verts + v0 + e);
-                float2 vj = __ldg(a.verts + v0 + (e == 0 ? n - 1 : e - 1));
+                float2 vj = __ldg(a.verts + v0 + (e == 0 ? nv - 1 : e - 1));
                 c = edge_class(r, vi, vj);
                 tog = edge_toggles(vi.x, vi.y, vj.x, vj.y, r.cx, r.cy);
             }
@@ -584,49 +594,76 @@ __global__ void k_cls_classify(ClsArgs a) {
             nf += __popc(__ballot_sync(FULL, (c & 6) == 2));
             inside ^= (__popc(__ballot_sync(FULL, tog)) & 1) != 0;
         }
-        if (lane == 0) {
-            int4 info;
-            if (meets == 0) info = make_int4(p, inside ? -1 : -2, 0, cell);
-            else info = make_int4(p, nr, nf, cell);
-            a.info[k] = info;
-            a.ecount[k] = (meets == 0) ? 0 : nr + nf;
-            if (info.y != -2) atomicAdd(a.cell_kept + cell, 1);
+        const int kind = meets ? 0 : (inside ? -1 : -2);
+        if (a.level == 1) {
+            if (lane == 0) a.info[k] = make_int4(p, kind, 0, gy * a.res + gx);
+            if (kind == -1) {
+                for (int s = lane; s < n * n; s += 32)
+                    atomicAdd(a.cell_kept + (gy + s / n) * a.res + gx + s % n, 1);
+            } else if (kind == 0) {
+                int base = 0;
+                if (lane == 0) base = atomicAdd(a.plist_n, n * n);
+                base = __shfl_sync(FULL, base, 0);
+                for (int s = lane; s < n * n; s += 32)
+                    a.plist[base + s] = make_int2(p, (gy + s / n) * a.res + gx + s % n);
+            }
+        } else if (lane == 0) {
+            const int cell = gy * a.res + gx;
+            a.info[k] = (kind == 0) ? make_int4(p, nr, nf, cell) : make_int4(p, kind, 0, cell);
+            a.ecount[k] = (kind == 0) ? nr + nf : 0;
+            if (kind != -2) atomicAdd(a.cell_kept + cell, 1);
         }
     }
 }
 
 // Kept pairs into the cell-major list (order inside a cell is immaterial).
+// Level 1: FULL coarse pairs expand to their fine cells.  Level 2: kept pairs.
 __global__ void k_cls_emit(ClsArgs a) {
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.npairs; k += gridDim.x * blockDim.x) {
+    const int npairs = a.level == 1 ? a.npairs : *a.plist_n;
+    const int nn = a.scale * a.scale;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < npairs; k += gridDim.x * blockDim.x) {
         int4 in = a.info[k];
-        if (in.y == -2) continue;
-        const int cell = in.w;
-        const int pos = a.cell_start[cell] + atomicAdd(a.cursor + cell, 1);
-        in.w = a.eoff[k];
-        a.entries[pos] = in;
+        if (a.level == 1) {
+            if (in.y != -1) continue;
+            const int gx = in.w % a.res, gy = in.w / a.res;
+            for (int s = 0; s < nn; ++s) {
+                const int cell = (gy + s / a.scale) * a.res + gx + s % a.scale;
+                const int pos = a.cell_start[cell] + atomicAdd(a.cursor + cell, 1);
+                a.entries[pos] = make_int4(in.x, -1, 0, 0);
+            }
+        } else {
+            if (in.y == -2) continue;
+            const int cell = in.w;
+            const int pos = a.cell_start[cell] + atomicAdd(a.cursor + cell, 1);
+            in.w = (in.y >= 0) ? a.eoff[k] : 0;
+            if (in.y < 0) in.z = 0;
+            a.entries[pos] = in;
+        }
     }
 }
 
+// Level 2: edge lists of fine EDGE pairs (straddle-only edges first).
 __global__ void k_cls_fill_edges(ClsArgs a) {
     const int lane = threadIdx.x & 31;
     const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const unsigned FULL = 0xffffffffu;
-    for (int k = wid; k < a.npairs; k += nw) {
+    const int npairs = *a.plist_n;
+    for (int k = wid; k < npairs; k += nw) {
         if (a.ecount[k] == 0) continue;
         const int4 in = a.info[k];
         const int p = in.x, cell = in.w, nr = in.y;
-        const int v0 = __ldg(a.pindex + p), n = __ldg(a.pindex + p + 1) - v0;
-        const CellRect r = cell_rect(a, cell);
+        const int v0 = __ldg(a.pindex + p), nv = __ldg(a.pindex + p + 1) - v0;
+        const CellRect r = cells_rect(a, cell % a.res, cell / a.res, 1);
         float4* out = a.edges + a.eoff[k];
         int wr = 0, wf = nr;
-        for (int e0 = 0; e0 < n; e0 += 32) {
+        for (int e0 = 0; e0 < nv; e0 += 32) {
             int e = e0 + lane;
             int c = 0;
             float2 vi = make_float2(0.f, 0.f), vj = vi;
-            if (e < n) {
+            if (e < nv) {
                 vi = __ldg(a.verts + v0 + e);
-                vj = __ldg(a.verts + v0 + (e == 0 ? n - 1 : e - 1));
+                vj = __ldg(a.verts + v0 + (e == 0 ? nv - 1 : e - 1));
                 c = edge_class(r, vi, vj);
             }
             const bool is_r = (c & 6) == 6, is_f = (c & 6) == 2;
@@ -906,6 +943,7 @@ bool launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_
 }
 
 void launch_cls_classify(const ClsArgs& c, int sms, cudaStream_t st) {
+    // level 2 reads its pair count on the device; c.npairs is then an upper bound
     int blocks = (int)std::min<long long>(((long long)c.npairs * 32 + 255) / 256, (long long)sms * 32);
     if (blocks < 1) blocks = 1;
     ++g_kernel_launches;

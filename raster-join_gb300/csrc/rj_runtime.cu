@@ -32,6 +32,7 @@ struct Column {
     int type = RJ_FLOAT;
     void* d = nullptr;
     bool owned = false;
+    float absmax = 0.f;     // largest finite |aggregate value| (sizes the fixed-point sums)
 };
 
 // Derived structures of the current polygon set, rebuilt on demand.
@@ -83,6 +84,8 @@ struct rj_ctx {
 
     rj_timings tm{};
     cudaEvent_t ev[8]{};
+    int* d_err = nullptr;     // device status word of bounded waits
+    int sum_shift = 0;        // fixed-point scale 2^s of the current query's sums
 };
 
 namespace {
@@ -224,13 +227,16 @@ int plan_raster(rj_ctx* ctx, const rj_query* q, RasterPlan& rp) {
 }
 
 // Filter + aggregation (GLFunction::setupPoints GLFunction.cpp:199-344).
-int build_filter(rj_ctx* ctx, const rj_query* q, DevFilter& f, bool force_count) {
+int build_filter(rj_ctx* ctx, const rj_query* q, DevFilter& f, bool force_count, bool* empty = nullptr) {
+    if (empty) *empty = false;
     std::memset(&f, 0, sizeof f);
     if (q->n_constraints < 0) return fail(ctx, RJ_E_INVALID, "negative constraint count");
     if (q->n_constraints > RJ_MAX_CONSTRAINTS)
         return fail(ctx, RJ_E_TOO_MANY_CONSTRAINTS, "%d constraints, at most %d supported", q->n_constraints,
                     RJ_MAX_CONSTRAINTS);
-    int k = 0;
+    // predicates, then grouped by the column they read (each column is loaded once)
+    struct Pred { const uint32_t* col; int op, typ; uint32_t val; bool compat; };
+    std::vector<Pred> preds;
     for (int i = 0; i < q->n_constraints; ++i) {
         const rj_constraint& c = q->constraints[i];
         const Column* col = find_col(ctx, c.attrib_id);
@@ -239,21 +245,87 @@ int build_filter(rj_ctx* ctx, const rj_query* q, DevFilter& f, bool force_count)
             return fail(ctx, RJ_E_UNSUPPORTED, "constraint %d: location attributes cannot be filtered", i);
         if (c.type < RJ_EQ || c.type > RJ_GTE)
             return fail(ctx, RJ_E_INVALID, "constraint %d: bad constraint type %d", i, c.type);
-        f.col[k] = (const uint32_t*)col->d;
-        f.op[k] = c.type;
-        f.typ[k] = col->type;
-        f.val[k] = c.val.uval;
-        if (q->flags & RJ_FLAG_COMPAT_FLOAT_EQ) f.compat_mask |= 1u << k;
-        ++k;
+        preds.push_back({(const uint32_t*)col->d, c.type, col->type, c.val.uval, (q->flags & RJ_FLAG_COMPAT_FLOAT_EQ) != 0});
     }
     if (q->time_attrib >= 0) {
         const Column* col = find_col(ctx, q->time_attrib);
         if (!col || col->type == RJ_LOCATION)
             return fail(ctx, RJ_E_INVALID, "time attribute %d is not a loaded scalar column", q->time_attrib);
-        f.col[k] = (const uint32_t*)col->d; f.op[k] = RJ_GTE; f.typ[k] = col->type; f.val[k] = q->t_start; ++k;
-        f.col[k] = (const uint32_t*)col->d; f.op[k] = RJ_LTE; f.typ[k] = col->type; f.val[k] = q->t_end; ++k;
+        preds.push_back({(const uint32_t*)col->d, RJ_GTE, col->type, q->t_start, false});
+        preds.push_back({(const uint32_t*)col->d, RJ_LTE, col->type, q->t_end, false});
+    }
+    int k = 0;
+    f.ncol = 0;
+    std::vector<bool> used(preds.size(), false);
+    for (size_t i = 0; i < preds.size(); ++i) {
+        if (used[i]) continue;
+        const int c = f.ncol++;
+        f.col[c] = preds[i].col;
+        f.pstart[c] = k;
+        for (size_t j = i; j < preds.size(); ++j) {
+            if (used[j] || preds[j].col != preds[i].col) continue;
+            used[j] = true;
+            f.op[k] = preds[j].op;
+            f.typ[k] = preds[j].typ;
+            f.val[k] = preds[j].val;
+            if (preds[j].compat) f.compat_mask |= 1u << k;
+            ++k;
+        }
+    }
+    f.pstart[f.ncol] = k;
+    // interval form of every column's predicates (unsatisfiable -> *empty)
+    f.general = 0;
+    for (int c = 0; c < f.ncol; ++c) {
+        uint32_t lo = 0u, hi = 0xFFFFFFFFu;
+        const int t = f.typ[f.pstart[c]];
+        f.ctyp[c] = t;
+        if (t == RJ_FLOAT) {
+            lo = order_key(RJ_FLOAT, 0xFF800000u);   // -inf
+            hi = order_key(RJ_FLOAT, 0x7F800000u);   // +inf
+        }
+        for (int j = f.pstart[c]; j < f.pstart[c + 1]; ++j) {
+            if (f.compat_mask & (1u << j)) f.general = 1;
+            const uint32_t v = f.val[j];
+            uint32_t elo, ehi;   // keys of the values equal to v
+            if (t == RJ_FLOAT) {
+                float fv;
+                std::memcpy(&fv, &v, 4);
+                if (std::isnan(fv)) { lo = 1; hi = 0; continue; }   // every comparison with NaN fails
+                if (fv == 0.0f) { elo = order_key(RJ_FLOAT, 0x80000000u); ehi = order_key(RJ_FLOAT, 0u); }
+                else elo = ehi = order_key(RJ_FLOAT, v);
+            } else {
+                elo = ehi = order_key(t, v);
+            }
+            uint64_t plo = lo, phi = hi;
+            const uint64_t kmin = (t == RJ_FLOAT) ? order_key(RJ_FLOAT, 0xFF800000u) : 0u;
+            const uint64_t kmax = (t == RJ_FLOAT) ? order_key(RJ_FLOAT, 0x7F800000u) : 0xFFFFFFFFu;
+            int64_t a = (int64_t)kmin, b = (int64_t)kmax;
+            switch (f.op[j]) {
+                case RJ_EQ: a = elo; b = ehi; break;
+                case RJ_LT: b = (int64_t)elo - 1; break;
+                case RJ_LTE: b = ehi; break;
+                case RJ_GT: a = (int64_t)ehi + 1; break;
+                case RJ_GTE: a = elo; break;
+            }
+            plo = std::max<int64_t>((int64_t)plo, a);
+            phi = std::min<int64_t>((int64_t)phi, b);
+            if ((int64_t)phi < (int64_t)plo || b < a) { lo = 1; hi = 0; continue; }
+            lo = (uint32_t)plo;
+            hi = (uint32_t)phi;
+        }
+        if (hi < lo) {
+            // unsatisfiable: evaluate the predicates one by one (they reject every point)
+            f.general = 1;
+            f.lo[c] = 0;
+            f.span[c] = 0;
+            if (empty) *empty = true;
+        } else {
+            f.lo[c] = lo;
+            f.span[c] = hi - lo;
+        }
     }
     f.n = k;
+    f.aggr_ci = -1;
     if (!force_count && q->aggregation != RJ_COUNT) {
         if (q->aggregation != RJ_AVG && q->aggregation != RJ_SUM)
             return fail(ctx, RJ_E_INVALID, "bad aggregation %d", q->aggregation);
@@ -264,6 +336,15 @@ int build_filter(rj_ctx* ctx, const rj_query* q, DevFilter& f, bool force_count)
         f.aggr = 1;
         f.aggr_typ = col->type;
         f.aggr_col = (const uint32_t*)col->d;
+        f.aggr_ci = -1;
+        for (int c = 0; c < f.ncol; ++c)
+            if (f.col[c] == f.aggr_col) f.aggr_ci = c;
+        // fixed-point sums: |v| * 2^s * n < 2^62 for every value and any subset
+        const double amax = std::max((double)col->absmax, 1e-30);
+        int shift = (int)std::floor(62.0 - std::log2(amax) - std::log2((double)ctx->npts + 1.0));
+        shift = std::max(-90, std::min(150, shift));
+        ctx->sum_shift = shift;
+        f.sum_scale = std::ldexp(1.0f, shift - 32);
     }
     return RJ_OK;
 }
@@ -411,35 +492,38 @@ int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix) {
                 if (enx < stx) enx = stx;
                 if (eny < sty) eny = sty;
             }
-            rng[p] = make_int4(stx * scale, enx * scale, sty * scale, eny * scale);
-            total += (long long)(enx - stx) * (eny - sty) * scale * scale;
+            rng[p] = make_int4(stx, enx, sty, eny);
+            total += (long long)(enx - stx) * (eny - sty);
         }
         off[P] = (int)total;
-        if (total > (1LL << 30)) return fail(ctx, RJ_E_UNSUPPORTED, "too many cell/polygon candidate pairs (%lld)", total);
-        const int npairs = (int)total;
-        int *doff, *ecount, *eoff, *cell_kept, *cursor, *tmp;
-        int4 *drng, *info;
+        const long long max_fine = total * scale * scale;
+        if (max_fine > (1LL << 30)) return fail(ctx, RJ_E_UNSUPPORTED, "too many cell/polygon candidate pairs (%lld)", max_fine);
+        const int npairs1 = (int)total;
+        int *doff, *cell_kept, *cursor, *tmp, *plist_n;
+        int4 *drng, *info1;
+        int2* plist;
         if ((rc = scratch_t(ctx, "cls_off", (size_t)P + 1, &doff))) return rc;
         if ((rc = scratch_t(ctx, "cls_rng", (size_t)P, &drng))) return rc;
-        if ((rc = scratch_t(ctx, "cls_info", (size_t)std::max(npairs, 1), &info))) return rc;
-        if ((rc = scratch_t(ctx, "cls_ecount", (size_t)std::max(npairs, 1), &ecount))) return rc;
-        if ((rc = scratch_t(ctx, "cls_eoff", (size_t)npairs + 1, &eoff))) return rc;
+        if ((rc = scratch_t(ctx, "cls_info1", (size_t)std::max(npairs1, 1), &info1))) return rc;
+        if ((rc = scratch_t(ctx, "cls_plist", (size_t)std::max<long long>(max_fine, 1), &plist))) return rc;
+        if ((rc = scratch_t(ctx, "cls_plist_n", 1, &plist_n))) return rc;
         if ((rc = scratch_t(ctx, "cls_kept", ncells, &cell_kept))) return rc;
         if ((rc = scratch_t(ctx, "cls_cursor", ncells, &cursor))) return rc;
         if ((rc = scratch_t(ctx, "cls_start", ncells + 1, &start2))) return rc;
-        const int ntmp = std::max(scan_tmp_ints((int)ncells), scan_tmp_ints(std::max(npairs, 1)));
-        if ((rc = scratch_t(ctx, "cls_tmp", (size_t)ntmp, &tmp))) return rc;
         RJ_CUDA(cudaMemcpyAsync(doff, off.data(), sizeof(int) * (P + 1), cudaMemcpyHostToDevice, ctx->stream));
         RJ_CUDA(cudaMemcpyAsync(drng, rng.data(), sizeof(int4) * P, cudaMemcpyHostToDevice, ctx->stream));
         RJ_CUDA(cudaMemsetAsync(cell_kept, 0, ncells * sizeof(int), ctx->stream));
         RJ_CUDA(cudaMemsetAsync(cursor, 0, ncells * sizeof(int), ctx->stream));
+        RJ_CUDA(cudaMemsetAsync(plist_n, 0, sizeof(int), ctx->stream));
         ClsArgs c{};
         c.verts = (const float2*)ctx->d_verts.p;
         c.pindex = (const int*)ctx->d_pindex.p;
         c.P = P;
         c.pair_off = doff;
         c.prange = drng;
-        c.npairs = npairs;
+        c.plist = plist;
+        c.plist_n = plist_n;
+        c.scale = scale;
         c.lbx = lbx; c.lby = lby; c.csx = csx; c.csy = csy;
         c.res = G;
         const double U = std::ldexp(1.0, -24);
@@ -448,32 +532,53 @@ int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix) {
         const double delta = 8.0 * U * (2.0 * Mc + G * std::max((double)csx, (double)csy));
         const double rel = 8.0 * U * (Mc + G * std::max((double)csx, (double)csy));
         c.margin = (float)(2.0 * (E + delta + rel) + 1e-7 * std::max(dx, dy));
-        c.info = info;
-        c.ecount = ecount;
-        c.eoff = eoff;
         c.cell_kept = cell_kept;
         c.cell_start = start2;
         c.cursor = cursor;
-        if (npairs > 0) launch_cls_classify(c, ctx->sms, ctx->stream);
+        // level 1: coarse pairs
+        ClsArgs c1 = c;
+        c1.level = 1;
+        c1.npairs = npairs1;
+        c1.info = info1;
+        if (npairs1 > 0) launch_cls_classify(c1, ctx->sms, ctx->stream);
+        int npairs2 = 0;
+        RJ_CUDA(cudaMemcpyAsync(&npairs2, plist_n, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        // level 2: fine cells of the coarse EDGE pairs
+        int4* info2;
+        int *ecount, *eoff;
+        if ((rc = scratch_t(ctx, "cls_info2", (size_t)std::max(npairs2, 1), &info2))) return rc;
+        if ((rc = scratch_t(ctx, "cls_ecount", (size_t)std::max(npairs2, 1), &ecount))) return rc;
+        if ((rc = scratch_t(ctx, "cls_eoff", (size_t)npairs2 + 1, &eoff))) return rc;
+        const int ntmp = std::max(scan_tmp_ints((int)ncells), scan_tmp_ints(std::max(npairs2, 1)));
+        if ((rc = scratch_t(ctx, "cls_tmp", (size_t)ntmp, &tmp))) return rc;
+        ClsArgs c2 = c;
+        c2.level = 2;
+        c2.npairs = npairs2;
+        c2.info = info2;
+        c2.ecount = ecount;
+        c2.eoff = eoff;
+        if (npairs2 > 0) launch_cls_classify(c2, ctx->sms, ctx->stream);
         if (!launch_exclusive_scan(cell_kept, start2, (int)ncells, tmp, ctx->stream))
             return fail(ctx, RJ_E_INVALID, "classified grid too large");
         int totals[2] = {0, 0};
-        if (npairs > 0) {
-            if (!launch_exclusive_scan(ecount, eoff, npairs, tmp, ctx->stream))
-                return fail(ctx, RJ_E_UNSUPPORTED, "too many cell/polygon pairs to scan (%d)", npairs);
-            RJ_CUDA(cudaMemcpyAsync(&totals[1], eoff + npairs, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        if (npairs2 > 0) {
+            if (!launch_exclusive_scan(ecount, eoff, npairs2, tmp, ctx->stream))
+                return fail(ctx, RJ_E_UNSUPPORTED, "too many cell/polygon pairs to scan (%d)", npairs2);
+            RJ_CUDA(cudaMemcpyAsync(&totals[1], eoff + npairs2, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         }
         RJ_CUDA(cudaMemcpyAsync(&totals[0], start2 + ncells, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         RJ_CUDA(cudaStreamSynchronize(ctx->stream));
         if ((rc = scratch_t(ctx, "cls_entries", (size_t)std::max(totals[0], 1), &entries2))) return rc;
         if ((rc = scratch_t(ctx, "cls_edges", (size_t)std::max(totals[1], 1), &edges))) return rc;
-        c.entries = entries2;
-        c.edges = edges;
+        c1.entries = c2.entries = entries2;
+        c2.edges = edges;
         uint32_t* code;
         if ((rc = scratch_t(ctx, "cls_code", ncells, &code))) return rc;
-        if (npairs > 0) {
-            launch_cls_emit(c, ctx->sms, ctx->stream);
-            launch_cls_fill_edges(c, ctx->sms, ctx->stream);
+        if (npairs1 > 0) launch_cls_emit(c1, ctx->sms, ctx->stream);
+        if (npairs2 > 0) {
+            launch_cls_emit(c2, ctx->sms, ctx->stream);
+            launch_cls_fill_edges(c2, ctx->sms, ctx->stream);
         }
         launch_cls_codes(start2, entries2, code, (int)ncells, ctx->sms, ctx->stream);
         RJ_CUDA(cudaGetLastError());
@@ -499,7 +604,7 @@ int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix) {
     return RJ_OK;
 }
 
-PointArgs make_point_args(rj_ctx* ctx, const DevFilter& f, unsigned long long* oc, double* os) {
+PointArgs make_point_args(rj_ctx* ctx, const DevFilter& f, unsigned long long* oc, unsigned long long* os) {
     PointArgs pa{};
     const Column* loc = find_col(ctx, ctx->loc_attrib);
     pa.xy = (const float2*)loc->d;
@@ -508,6 +613,8 @@ PointArgs make_point_args(rj_ctx* ctx, const DevFilter& f, unsigned long long* o
     pa.P = ctx->P;
     pa.out_count = oc;
     pa.out_sum = os;
+    pa.out_nonfinite = (double*)ctx->scratch["out_nonfinite"].p;
+    pa.err = ctx->d_err;
     return pa;
 }
 
@@ -532,7 +639,7 @@ CanvasXf make_canvas_xf(rj_ctx* ctx, const RasterPlan& rp, const float4* dcol, c
 // Join operators.  Each fills out_count / out_sum (and out_bounds) on device.
 struct ExecState {
     unsigned long long* out_count;
-    double* out_sum;
+    unsigned long long* out_sum;
     long long* out_bounds;
     Phase* ph;
     int passes = 1;
@@ -649,12 +756,12 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
     }
     // canvas path: point pass (additive splat) then polygon pass
     uint32_t* canvas_c;
-    double* canvas_s = nullptr;
+    long long* canvas_s = nullptr;
     if ((rc = scratch_t(ctx, "canvas_c", npix, &canvas_c))) return rc;
     RJ_CUDA(cudaMemsetAsync(canvas_c, 0, npix * sizeof(uint32_t), ctx->stream));
     if (f.aggr) {
         if ((rc = scratch_t(ctx, "canvas_s", npix, &canvas_s))) return rc;
-        RJ_CUDA(cudaMemsetAsync(canvas_s, 0, npix * sizeof(double), ctx->stream));
+        RJ_CUDA(cudaMemsetAsync(canvas_s, 0, npix * sizeof(long long), ctx->stream));
     }
     PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
     launch_raster_splat(pa, cx, canvas_c, canvas_s, ctx->sms, ctx->stream);
@@ -790,15 +897,16 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
         return RJ_OK;
     }
     uint32_t* canvas_c;
-    double* canvas_s = nullptr;
+    long long* canvas_s = nullptr;
     if ((rc = scratch_t(ctx, "hyb_canvas_c", npix, &canvas_c))) return rc;
     RJ_CUDA(cudaMemsetAsync(canvas_c, 0, npix * sizeof(uint32_t), ctx->stream));
     if (f.aggr) {
         if ((rc = scratch_t(ctx, "hyb_canvas_s", npix, &canvas_s))) return rc;
-        RJ_CUDA(cudaMemsetAsync(canvas_s, 0, npix * sizeof(double), ctx->stream));
+        RJ_CUDA(cudaMemsetAsync(canvas_s, 0, npix * sizeof(long long), ctx->stream));
     }
     ha.canvas_c = canvas_c;
     ha.canvas_s = canvas_s;
+    ha.scale = f.sum_scale;
     ha.label = nullptr;
     launch_hybrid_points(pa, ix, ha, ctx->sms, ctx->stream);
     RJ_CUDA(cudaGetLastError());
@@ -866,6 +974,11 @@ int rj_create(const rj_config* cfg, rj_ctx** out) {
         ctx->own_stream = true;
     }
     for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+    if (cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        rj_destroy(ctx);
+        return RJ_E_OOM;
+    }
     *out = ctx;
     return RJ_OK;
 }
@@ -881,6 +994,7 @@ void rj_destroy(rj_ctx* ctx) {
     for (auto& kv : ctx->scratch) dev_free(ctx, kv.second);
     for (auto& ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
+    if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -901,6 +1015,24 @@ int rj_set_stream(rj_ctx* ctx, void* stream) {
         cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
         ctx->own_stream = true;
     }
+    return RJ_OK;
+}
+
+// Largest finite |aggregate value| of every scalar column.
+static int column_stats(rj_ctx* ctx) {
+    unsigned* bits;
+    int rc;
+    const int nc = (int)ctx->cols.size();
+    if ((rc = scratch_t(ctx, "col_absmax", (size_t)std::max(nc, 1), &bits))) return rc;
+    RJ_CUDA(cudaMemsetAsync(bits, 0, sizeof(unsigned) * std::max(nc, 1), ctx->stream));
+    for (int i = 0; i < nc; ++i)
+        if (ctx->cols[i].type != RJ_LOCATION && ctx->npts)
+            launch_col_absmax((const uint32_t*)ctx->cols[i].d, ctx->cols[i].type, ctx->npts, bits + i, ctx->sms, ctx->stream);
+    std::vector<unsigned> h(std::max(nc, 1));
+    RJ_CUDA(cudaMemcpyAsync(h.data(), bits, sizeof(unsigned) * std::max(nc, 1), cudaMemcpyDeviceToHost, ctx->stream));
+    RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    RJ_CUDA(cudaGetLastError());
+    for (int i = 0; i < nc; ++i) std::memcpy(&ctx->cols[i].absmax, &h[i], 4);
     return RJ_OK;
 }
 
@@ -937,8 +1069,7 @@ static int load_points_impl(rj_ctx* ctx, const rj_column* cols, int32_t ncols, u
             if (npoints)
                 RJ_CUDA(cudaMemcpyAsync(ctx->cols[i].d, cols[i].data, esz * npoints, cudaMemcpyHostToDevice, ctx->stream));
         }
-        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
-        return RJ_OK;
+        return column_stats(ctx);
     }
     // release the previous table
     for (Column& c : ctx->cols) {
@@ -982,7 +1113,7 @@ static int load_points_impl(rj_ctx* ctx, const rj_column* cols, int32_t ncols, u
     ctx->npts = npoints;
     ctx->loc_attrib = loc;
     RJ_CUDA(cudaStreamSynchronize(ctx->stream));
-    return RJ_OK;
+    return column_stats(ctx);
 }
 
 int rj_load_points(rj_ctx* ctx, const rj_column* cols, int32_t ncols, uint64_t npoints, int32_t loc_attrib) {
@@ -1096,16 +1227,21 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
     }
     g_kernel_launches = 0;
     unsigned long long* oc;
-    double* os;
+    unsigned long long* os;
+    double* onf;
     long long* ob;
     if ((rc = scratch_t(ctx, "out_count", P, &oc))) return rc;
     if ((rc = scratch_t(ctx, "out_sum", P, &os))) return rc;
+    if ((rc = scratch_t(ctx, "out_nonfinite", P, &onf))) return rc;
     if ((rc = scratch_t(ctx, "out_bounds", (size_t)4 * P, &ob))) return rc;
     Phase ph(ctx, (q->flags & RJ_FLAG_PHASE_TIMING) != 0);
     ph.mark(0);
     RJ_CUDA(cudaMemsetAsync(oc, 0, P * sizeof(unsigned long long), ctx->stream));
-    RJ_CUDA(cudaMemsetAsync(os, 0, P * sizeof(double), ctx->stream));
+    RJ_CUDA(cudaMemsetAsync(os, 0, P * sizeof(unsigned long long), ctx->stream));
+    RJ_CUDA(cudaMemsetAsync(onf, 0, P * sizeof(double), ctx->stream));
+    ctx->sum_shift = 0;
     RJ_CUDA(cudaMemsetAsync(ob, 0, (size_t)4 * P * sizeof(long long), ctx->stream));
+    RJ_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
     ExecState es{oc, os, ob, &ph};
     const double t_setup = now_ms();
     switch (q->function_type) {
@@ -1118,18 +1254,23 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
         cudaStreamSynchronize(ctx->stream);
         return rc;
     }
-    std::vector<unsigned long long> hc(P);
-    std::vector<double> hs(P);
+    std::vector<unsigned long long> hc(P), hq(P);
+    std::vector<double> hs(P), hnf(P);
     std::vector<long long> hb;
     RJ_CUDA(cudaMemcpyAsync(hc.data(), oc, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
-    RJ_CUDA(cudaMemcpyAsync(hs.data(), os, P * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    RJ_CUDA(cudaMemcpyAsync(hq.data(), os, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    RJ_CUDA(cudaMemcpyAsync(hnf.data(), onf, P * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     if (q->function_type == RJ_RASTER_JOIN_BOUNDS && res && res->bounds) {
         hb.resize((size_t)4 * P);
         RJ_CUDA(cudaMemcpyAsync(hb.data(), ob, (size_t)4 * P * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
     }
+    int derr = 0;
+    RJ_CUDA(cudaMemcpyAsync(&derr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     ph.mark(5);
     RJ_CUDA(cudaStreamSynchronize(ctx->stream));
     RJ_CUDA(cudaGetLastError());
+    if (derr) return fail(ctx, RJ_E_TIMEOUT, "a bounded device wait ran out (status 0x%x)", derr);
+    for (int i = 0; i < P; ++i) hs[i] = std::ldexp((double)(long long)hq[i], -ctx->sum_shift) + hnf[i];
     if (res) {
         if (res->count) for (int i = 0; i < P; ++i) res->count[i] = hc[i];
         if (res->sum) for (int i = 0; i < P; ++i) res->sum[i] = hs[i];

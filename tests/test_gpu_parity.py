@@ -361,6 +361,54 @@ def test_points_on_and_near_edges(handler, polys):
             handler.flags = 0
 
 
+def _edge_values(typ, n, rng):
+    if typ == "f":
+        special = np.array([0.0, -0.0, 1.0, -1.0, np.inf, -np.inf, np.nan, -np.nan, 1e-45, -1e-45, 1e-38,
+                            3.4e38, -3.4e38, 12.5, 50.0], np.float32)
+        vals = rng.choice(special, n).astype(np.float32)
+        return vals.view(np.uint32), special
+    if typ == "i":
+        special = np.array([0, 1, -1, 2, -2, 2**31 - 1, -2**31, 7, 8, 9], np.int64).astype(np.int32)
+        return rng.choice(special, n).astype(np.int32).view(np.uint32), special
+    special = np.array([0, 1, 2, 2**32 - 1, 2**31, 2**31 - 1, 7, 8], np.uint64).astype(np.uint32)
+    return rng.choice(special, n).astype(np.uint32), special
+
+
+@pytest.mark.parametrize("typ", ["f", "i", "u"])
+def test_predicates_on_edge_values(handler, typ):
+    """Every operator against +-0, +-inf, NaN, denormals and integer extremes."""
+    rng = np.random.default_rng(7)
+    verts, pidx = synth.voronoi_polygons(16, seed=7)
+    n = 400_000
+    xy = synth.points(n, seed=7)["xy"]
+    col, special = _edge_values(typ, n, rng)
+    at = {"f": rj.Float, "i": rj.Int, "u": rj.Uint}[typ]
+    ot = {"f": oracle.Float, "i": oracle.Int, "u": oracle.Uint}[typ]
+    dh = rj.DataHandler()
+    dh.add_column(1, rj.Location, xy)
+    dh.add_column(9, at, col.view({"f": np.float32, "i": np.int32, "u": np.uint32}[typ]))
+    dh.setPolygons(verts, pidx)
+    handler.setDataHandler(dh)
+    handler.setPolyIndexResolution(64)
+    cols = oracle.Columns({9: (ot, col.view({"f": np.float32, "i": np.int32, "u": np.uint32}[typ]))})
+    for v in special[:8]:
+        for op in (rj.EQ, rj.LT, rj.LTE, rj.GT, rj.GTE):
+            cons = [(9, op, v)]
+            dh.setQueryConstraints(cons)
+            got = handler.execute(rj.IndexJoinFn).count
+            want, _ = oracle.index_join(xy, verts, pidx, 64, f=cols.filt(cons))
+            np.testing.assert_array_equal(got, want, err_msg="op %d value %r" % (op, v))
+    # two predicates on one column intersect; an empty intersection selects nothing
+    for cons, nonempty in (([(9, rj.GTE, special[1]), (9, rj.LTE, special[2])], True),
+                           ([(9, rj.GT, special[2]), (9, rj.LT, special[2])], False)):
+        dh.setQueryConstraints(cons)
+        got = handler.execute(rj.IndexJoinFn).count
+        want, _ = oracle.index_join(xy, verts, pidx, 64, f=cols.filt(cons))
+        np.testing.assert_array_equal(got, want)
+        if not nonempty:
+            assert got.sum() == 0
+
+
 def test_errors_are_status_codes(handler, c1):
     pts, verts, pidx = c1
     dh = make_dh(pts, verts, pidx)
