@@ -221,6 +221,29 @@ RJ_API int rj_get_timings(const rj_ctx *ctx, rj_timings *out);
 /* the reference's tab-separated timing line for the last call */
 RJ_API int rj_format_time_stats(const rj_ctx *ctx, char *buf, size_t buflen);
 
+/* ---- allocation-free raster count ----------------------------------------
+ * No counterpart in the reference.  For callers that may not allocate device
+ * memory (hosts that budget every byte of GPU memory themselves, loops that
+ * must not stall on an allocation, processes already at the memory limit):
+ * the bounded raster join, count per polygon, over device-resident points and
+ * polygons, with all scratch taken from one fixed device array inside the
+ * library (about 19 MiB, held by every GPU that loads the library until the
+ * process exits).  Limits: canvas ceil(dx/cell) x ceil(dy/cell) <= 2048 x 2048
+ * (one tile), npolys <= 65536, nverts <= 262144 and d_pindex[npolys] ==
+ * nverts; larger requests return RJ_E_INVALID with a message in err.
+ * d_xy (float x,y pairs, 16-byte aligned), d_verts and d_pindex follow
+ * rj_load_points / rj_set_polygons; bbox is the polygon bounds (host, 4
+ * doubles); d_count receives npolys counts (overwritten).  Work is queued on
+ * `stream` and the call returns without waiting.  Calls share the array:
+ * calls that overlap on the GPU race and give wrong counts.  The first call
+ * on a device looks up the array's device address; make it before capturing
+ * that stream.  Results equal rj_execute's RJ_RASTER_JOIN counts with
+ * cell_size and no constraints. */
+RJ_API int rj_raster_count_noalloc(const float *d_xy, uint64_t npoints, const float *d_verts,
+                                   const int32_t *d_pindex, int32_t npolys, int32_t nverts,
+                                   const double *bbox, double cell_size, unsigned long long *d_count,
+                                   void *stream, char *err, size_t errlen);
+
 #ifdef __cplusplus
 }
 #endif

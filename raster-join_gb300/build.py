@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "librj.so")
-SOURCES = ["rj_runtime.cu", "rj_point_kernels.cu", "rj_poly_kernels.cu"]
+SOURCES = ["rj_runtime.cu", "rj_point_kernels.cu", "rj_poly_kernels.cu", "rj_noalloc.cu"]
 HEADERS = ["rj_device.cuh", "rj_launch.h", os.path.join("..", "..", "include", "rj.h")]
 
 NVCC_FLAGS = [
