@@ -682,16 +682,21 @@ __global__ void k_cls_fill_edges(ClsArgs a) {
 // of the hybrid canvas into the label map.
 __global__ void k_label_finish(uint16_t* __restrict__ label, const uint32_t* __restrict__ mask, int resx, int resy,
                                int ntiles, int words, unsigned long long* __restrict__ nonempty) {
-    const size_t tile_px = (size_t)resx * resy;
-    const size_t total = tile_px * ntiles;
+    // one thread per 32-pixel run of a row (the width of one mask word)
+    const int runs = (resx + 31) / 32;
+    const size_t total = (size_t)runs * resy * ntiles;
     unsigned long long cnt = 0;
     for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < total; g += (size_t)gridDim.x * blockDim.x) {
-        uint16_t l = label[g];
-        cnt += (l != kEmptyLabel);
-        if (mask) {
-            size_t r = g % tile_px;
-            int j = (int)(r / resx), i = (int)(r % resx);
-            if ((__ldg(mask + (size_t)j * words + (i >> 5)) >> (i & 31)) & 1u) label[g] = kBorderLabel;
+        const int w = (int)(g % runs);
+        const size_t row = g / runs;                  // tile * resy + j
+        const int j = (int)(row % resy);
+        uint16_t* l = label + row * resx + (size_t)w * 32;
+        const int n = min(32, resx - w * 32);
+        const uint32_t m = mask ? __ldg(mask + (size_t)j * words + w) : 0u;
+        for (int i = 0; i < n; ++i) {
+            const uint16_t v = l[i];
+            cnt += (v != kEmptyLabel);
+            if ((m >> i) & 1u) l[i] = kBorderLabel;
         }
     }
     cnt = warp_sum_u64(cnt);
@@ -963,7 +968,7 @@ void launch_cls_fill_edges(const ClsArgs& c, int sms, cudaStream_t st) {
 }
 void launch_label_finish(uint16_t* label, const uint32_t* mask, int resx, int resy, int ntiles, int words,
                          unsigned long long* nonempty, int sms, cudaStream_t st) {
-    size_t total = (size_t)resx * resy * ntiles;
+    size_t total = (size_t)((resx + 31) / 32) * resy * ntiles;
     int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)sms * 16);
     if (blocks < 1) blocks = 1;
     ++g_kernel_launches;

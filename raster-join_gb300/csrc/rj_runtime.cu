@@ -86,6 +86,7 @@ struct rj_ctx {
     cudaEvent_t ev[8]{};
     int* d_err = nullptr;     // device status word of bounded waits
     int sum_shift = 0;        // fixed-point scale 2^s of the current query's sums
+    unsigned long long* overlap_pending = nullptr;   // label-map counters to check after the call
 };
 
 namespace {
@@ -541,10 +542,10 @@ int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix) {
         c1.npairs = npairs1;
         c1.info = info1;
         if (npairs1 > 0) launch_cls_classify(c1, ctx->sms, ctx->stream);
-        int npairs2 = 0;
-        RJ_CUDA(cudaMemcpyAsync(&npairs2, plist_n, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
-        // level 2: fine cells of the coarse EDGE pairs
+        // level 2: fine cells of the coarse EDGE pairs.  Its pair count stays on
+        // the device; buffers are sized for the upper bound (every coarse pair
+        // refined) so no host round trip is needed before the scans.
+        const int npairs2 = (int)max_fine;
         int4* info2;
         int *ecount, *eoff;
         if ((rc = scratch_t(ctx, "cls_info2", (size_t)std::max(npairs2, 1), &info2))) return rc;
@@ -552,6 +553,7 @@ int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix) {
         if ((rc = scratch_t(ctx, "cls_eoff", (size_t)npairs2 + 1, &eoff))) return rc;
         const int ntmp = std::max(scan_tmp_ints((int)ncells), scan_tmp_ints(std::max(npairs2, 1)));
         if ((rc = scratch_t(ctx, "cls_tmp", (size_t)ntmp, &tmp))) return rc;
+        RJ_CUDA(cudaMemsetAsync(ecount, 0, sizeof(int) * (size_t)std::max(npairs2, 1), ctx->stream));
         ClsArgs c2 = c;
         c2.level = 2;
         c2.npairs = npairs2;
@@ -689,14 +691,11 @@ int label_map(rj_ctx* ctx, PolyPassArgs& a, const char* key, size_t npix, const 
     if ((rc = poly_pass(ctx, MODE_LABEL, a))) return rc;
     launch_label_finish(label, mask, a.resx, a.resy, a.T, words, cnt + 1, ctx->sms, ctx->stream);
     RJ_CUDA(cudaGetLastError());
+    // Optimistic: the polygon set is assumed not to overlap; rj_execute reads
+    // the two counters with the results and re-runs the query on the canvas
+    // path if some pixel centre lay in two polygons.
     *overlap = 0;
-    if (ctx->overlap_known != 0) {
-        unsigned long long h[2] = {0, 0};
-        RJ_CUDA(cudaMemcpyAsync(h, cnt, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
-        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
-        *overlap = h[0] != h[1];
-        ctx->overlap_known = *overlap;
-    }
+    if (ctx->overlap_known != 0) ctx->overlap_pending = cnt;
     *out = label;
     a.label = nullptr;
     return RJ_OK;
@@ -1244,31 +1243,47 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
     RJ_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
     ExecState es{oc, os, ob, &ph};
     const double t_setup = now_ms();
-    switch (q->function_type) {
-        case RJ_RASTER_JOIN: rc = exec_raster(ctx, q, es, false); break;
-        case RJ_INDEX_JOIN: rc = exec_index(ctx, q, es); break;
-        case RJ_HYBRID_JOIN: rc = exec_hybrid(ctx, q, es); break;
-        default: rc = exec_raster(ctx, q, es, true); break;
-    }
-    if (rc) {
-        cudaStreamSynchronize(ctx->stream);
-        return rc;
-    }
     std::vector<unsigned long long> hc(P), hq(P);
     std::vector<double> hs(P), hnf(P);
     std::vector<long long> hb;
-    RJ_CUDA(cudaMemcpyAsync(hc.data(), oc, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
-    RJ_CUDA(cudaMemcpyAsync(hq.data(), os, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
-    RJ_CUDA(cudaMemcpyAsync(hnf.data(), onf, P * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    if (q->function_type == RJ_RASTER_JOIN_BOUNDS && res && res->bounds) {
-        hb.resize((size_t)4 * P);
-        RJ_CUDA(cudaMemcpyAsync(hb.data(), ob, (size_t)4 * P * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
-    }
     int derr = 0;
-    RJ_CUDA(cudaMemcpyAsync(&derr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    ph.mark(5);
-    RJ_CUDA(cudaStreamSynchronize(ctx->stream));
-    RJ_CUDA(cudaGetLastError());
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        ctx->overlap_pending = nullptr;
+        switch (q->function_type) {
+            case RJ_RASTER_JOIN: rc = exec_raster(ctx, q, es, false); break;
+            case RJ_INDEX_JOIN: rc = exec_index(ctx, q, es); break;
+            case RJ_HYBRID_JOIN: rc = exec_hybrid(ctx, q, es); break;
+            default: rc = exec_raster(ctx, q, es, true); break;
+        }
+        if (rc) {
+            cudaStreamSynchronize(ctx->stream);
+            return rc;
+        }
+        RJ_CUDA(cudaMemcpyAsync(hc.data(), oc, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+        RJ_CUDA(cudaMemcpyAsync(hq.data(), os, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+        RJ_CUDA(cudaMemcpyAsync(hnf.data(), onf, P * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        if (q->function_type == RJ_RASTER_JOIN_BOUNDS && res && res->bounds) {
+            hb.resize((size_t)4 * P);
+            RJ_CUDA(cudaMemcpyAsync(hb.data(), ob, (size_t)4 * P * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        unsigned long long lc[2] = {0, 0};
+        if (ctx->overlap_pending)
+            RJ_CUDA(cudaMemcpyAsync(lc, ctx->overlap_pending, sizeof lc, cudaMemcpyDeviceToHost, ctx->stream));
+        RJ_CUDA(cudaMemcpyAsync(&derr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        ph.mark(5);
+        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        RJ_CUDA(cudaGetLastError());
+        if (!ctx->overlap_pending) break;
+        ctx->overlap_known = (lc[0] != lc[1]) ? 1 : 0;
+        if (!ctx->overlap_known) break;
+        // overlapping polygons: the label map cannot hold them, redo on the canvas path
+        RJ_CUDA(cudaMemsetAsync(oc, 0, P * sizeof(unsigned long long), ctx->stream));
+        RJ_CUDA(cudaMemsetAsync(os, 0, P * sizeof(unsigned long long), ctx->stream));
+        RJ_CUDA(cudaMemsetAsync(onf, 0, P * sizeof(double), ctx->stream));
+        RJ_CUDA(cudaMemsetAsync(ob, 0, (size_t)4 * P * sizeof(long long), ctx->stream));
+        RJ_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    }
+    ctx->overlap_pending = nullptr;
     if (derr) return fail(ctx, RJ_E_TIMEOUT, "a bounded device wait ran out (status 0x%x)", derr);
     for (int i = 0; i < P; ++i) hs[i] = std::ldexp((double)(long long)hq[i], -ctx->sum_shift) + hnf[i];
     if (res) {
