@@ -41,6 +41,7 @@ extern "C" {
 #define RJ_E_NO_DATA              -6   /* points or polygons not loaded (GLHandler.cpp:190-193) */
 #define RJ_E_UNSUPPORTED          -7   /* join type / option not supported      */
 #define RJ_E_BUSY                 -8   /* admission refused (serving queue full) */
+#define RJ_PENDING                 1   /* rj_poll: the request has not finished yet */
 
 /* ---- limits ------------------------------------------------------------- */
 #define RJ_MAX_CONSTRAINTS 10   /* std140 vec4 query[10], RasterJoin/shaders/points.vert:8-10 */
@@ -220,6 +221,88 @@ RJ_API void rj_query_init(rj_query *q);
 RJ_API int rj_get_timings(const rj_ctx *ctx, rj_timings *out);
 /* the reference's tab-separated timing line for the last call */
 RJ_API int rj_format_time_stats(const rj_ctx *ctx, char *buf, size_t buflen);
+
+/* ---- polygon sets --------------------------------------------------------
+ * A polygon collection held on the device independently of the context's own
+ * set (the reference keeps one PolyHandler per collection,
+ * RasterJoin/db/PolyHandler.cpp:20-80; setPolygonQuery DataHandler.cpp:73-75
+ * selects one).  Same arguments as rj_set_polygons.  A set belongs to the
+ * context that created it; destroy it before the context. */
+typedef struct rj_polyset rj_polyset;
+RJ_API int rj_polyset_create(rj_ctx *ctx, const float *xy, const int32_t *pindex, int32_t npolys,
+                             const double *bbox, rj_polyset **out);
+RJ_API void rj_polyset_destroy(rj_polyset *ps);
+/* make ps the polygon set of rj_execute (NULL: the set of rj_set_polygons) */
+RJ_API int rj_use_polyset(rj_ctx *ctx, rj_polyset *ps);
+
+/* ---- time index ----------------------------------------------------------
+ * Reorders the resident table's rows into nbuckets buckets of the uint32
+ * column time_attrib (a counting sort; every column moves with its row), so a
+ * query whose time range is on that column reads only the rows of the
+ * buckets it overlaps; the exact inclusive time predicate still applies.
+ * Stands in for the reference backend's time partitions
+ * (HashGridIndex.cpp:114-137), which selected whole partitions.  Results are
+ * unchanged (they do not depend on row order).  nbuckets 0 = 16384
+ * (at most 16384).  Device-attached tables are copied into library-owned
+ * buffers.  Reloading the table drops the index. */
+RJ_API int rj_build_time_index(rj_ctx *ctx, int32_t time_attrib, int32_t nbuckets);
+
+/* ---- batched execution ---------------------------------------------------
+ * No counterpart in the reference (one executeFunction per query).  Runs nq
+ * queries over the resident table; sets[i] is query i's polygon set (NULL:
+ * the context's own).  Raster joins with interval-form filters run fused: one
+ * point pass for the whole batch reads each row once for every query whose
+ * time window covers it.  Every other query (other join types,
+ * RJ_FLAG_COMPAT_FLOAT_EQ, more distinct columns than one pass stages) runs
+ * through rj_execute.  res[i] is filled like rj_execute's result; status[i]
+ * (may be NULL) receives each query's status.  Returns RJ_OK when every
+ * query succeeded, else the first failing status. */
+#define RJ_BATCH_AUTOTUNE 0x1u   /* time the point-pass block shapes on this batch and keep the fastest */
+#define RJ_BATCH_NO_FUSE  0x2u   /* run every query through rj_execute (the plain path) */
+typedef struct {
+    int32_t nqueries, fused, fallback;
+    int32_t segments;              /* row ranges covered by one set of queries */
+    uint64_t items;                /* work items of the fused point pass       */
+    uint64_t rows_read;            /* rows staged from HBM (each once)         */
+    uint64_t point_queries;        /* sum over fused queries of rows scanned   */
+    double total_ms;               /* host wall clock of the call              */
+    double setup_ms;               /* host planning                            */
+    double poly_ms;                /* label maps / canvases (CUDA events)      */
+    double point_ms;               /* fused point pass (CUDA events)           */
+    double reduce_ms;              /* canvas polygon passes (CUDA events)      */
+    int32_t threads, rows_per_item, tuned;
+    int32_t kernel_launches;
+} rj_batch_stats;
+RJ_API int rj_execute_batch(rj_ctx *ctx, int32_t nq, const rj_query *q, rj_polyset *const *sets,
+                            rj_result *res, int32_t *status, uint32_t flags, rj_batch_stats *stats);
+
+/* ---- serving -------------------------------------------------------------
+ * No counterpart in the reference.  A request loop over the context's
+ * resident table: rj_submit queues a query (copied) with its polygon set and
+ * caller-owned result buffers (valid until rj_poll reports completion).  A
+ * scheduler thread forms batches from the queued requests as slots free up,
+ * admitting requests while the batch's canvases and label maps fit the
+ * slot's memory (canvas_mb); up to `slots` batches are on the GPU at once
+ * (polygon-side work of one overlaps the point pass of another).  While a
+ * server runs, the context accepts no other calls (RJ_E_BUSY). */
+typedef struct {
+    int32_t slots;                 /* batches in flight (0 = 2)                 */
+    int64_t canvas_mb;             /* device memory per slot (0 = 8192)         */
+    int32_t max_batch;             /* requests per batch (0 = 256)              */
+    double max_wait_ms;            /* hold a batch open for more arrivals (0 = launch at once) */
+} rj_server_config;
+typedef struct {
+    double submit_ms, start_ms, done_ms;   /* steady-clock milliseconds            */
+    int32_t batch_id, batch_size, status;
+} rj_request_info;
+typedef struct rj_server rj_server;
+RJ_API int rj_server_create(rj_ctx *ctx, const rj_server_config *cfg, rj_server **out);
+RJ_API int rj_submit(rj_server *srv, const rj_query *q, rj_polyset *ps, rj_result *res, uint64_t *ticket);
+/* RJ_OK when the request is done (info filled), RJ_PENDING if it is still
+ * running after timeout_ms (< 0: wait without limit) */
+RJ_API int rj_poll(rj_server *srv, uint64_t ticket, int32_t timeout_ms, rj_request_info *info);
+/* finishes the queued requests, then stops */
+RJ_API void rj_server_destroy(rj_server *srv);
 
 /* ---- allocation-free raster count ----------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device

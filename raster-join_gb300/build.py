@@ -2,7 +2,7 @@
 
 Usage: python raster-join_gb300/build.py [--force]
 
-The three translation units compile in parallel with one -gencode
+The translation units compile in parallel with one -gencode
 (compute_103a -> sm_103a) and link into raster-join_gb300/lib/librj.so with
 the static CUDA runtime.  A stamp of the sources' modification times skips
 work when nothing changed.
@@ -19,8 +19,10 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "librj.so")
-SOURCES = ["rj_runtime.cu", "rj_point_kernels.cu", "rj_poly_kernels.cu", "rj_noalloc.cu"]
-HEADERS = ["rj_device.cuh", "rj_launch.h", os.path.join("..", "..", "include", "rj.h")]
+SOURCES = ["rj_runtime.cu", "rj_point_kernels.cu", "rj_poly_kernels.cu", "rj_noalloc.cu",
+           "rj_batch.cu", "rj_batch_kernels.cu"]
+HEADERS = ["rj_device.cuh", "rj_launch.h", "rj_internal.h", "rj_point_map.cuh",
+           os.path.join("..", "..", "include", "rj.h")]
 
 NVCC_FLAGS = [
     "-std=c++17", "-O3", "-lineinfo",

@@ -1,0 +1,166 @@
+// rj_internal.h -- host-side state shared by the runtime translation units:
+// the context behind rj_ctx, polygon sets, and the helpers that plan a query
+// (canvas geometry, filters, device allocation).
+#pragma once
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "rj_device.cuh"
+#include "rj_launch.h"
+
+namespace rjh {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct Column {
+    int attrib = -1;
+    int type = RJ_FLOAT;
+    void* d = nullptr;
+    bool owned = false;
+    float absmax = 0.f;     // largest finite |aggregate value| (sizes the fixed-point sums)
+};
+
+// Derived structures of the bound polygon set, rebuilt on demand.
+struct GridCache {
+    bool valid = false;
+    int res = 0;
+    int clamp = 0;
+    bool pair_cell = false;
+    size_t nentries = 0;
+};
+
+struct ExactCache {
+    bool valid = false;
+    int res = 0;
+    int user_res = 0;
+    size_t nentries = 0, nedges = 0;
+};
+
+// One polygon collection (PolyHandler polys / pindexes / bounds,
+// RasterJoin/db/PolyHandler.cpp:49-80) with its device copy.
+struct PolySet {
+    int P = 0, V = 0;
+    std::vector<float> h_xy;
+    std::vector<int> h_pindex;
+    std::vector<float4> h_mbr;      // per polygon (minx, miny, maxx, maxy)
+    double bbox[4] = {0, 0, 0, 0};
+    float max_abs_coord = 0.f, max_edge_dx = 0.f, max_edge_dy = 0.f;
+    DevBuf d_verts, d_pindex, d_edge_poly;
+    uint64_t version = 0;
+    int overlap_known = -1;   // -1 unknown, 0 no two polygons share a pixel centre, 1 some do
+    GridCache grid;
+    ExactCache exact;
+};
+
+// Time-bucketed row order of the resident table (rj_build_time_index): rows
+// of bucket b are [start[b], start[b+1]); bucket of t is
+// (t - tmin) * nb / (tmax - tmin + 1).
+struct TimeIndex {
+    bool valid = false;
+    int attrib = -1;
+    uint32_t tmin = 0, tmax = 0;
+    int nb = 0;
+    std::vector<uint64_t> start;   // nb + 1
+    uint32_t bucket_of(uint32_t t) const {
+        if (t <= tmin) return 0;
+        if (t >= tmax) return (uint32_t)nb - 1;
+        return (uint32_t)(((uint64_t)(t - tmin) * (uint64_t)nb) / ((uint64_t)(tmax - tmin) + 1));
+    }
+    // rows that can hold a time in [t0, t1] (a superset, multiple of 4 aligned)
+    void rows(uint32_t t0, uint32_t t1, uint64_t n, uint64_t& r0, uint64_t& r1) const {
+        if (t1 < t0 || t1 < tmin || t0 > tmax) { r0 = r1 = 0; return; }
+        r0 = start[bucket_of(t0)] & ~3ULL;
+        r1 = start[bucket_of(t1) + 1];
+        if (r1 > n) r1 = n;
+    }
+};
+
+}  // namespace rjh
+
+struct rj_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int sms = 1;
+    int64_t budget = 0;       // bytes, 0 = unlimited
+    std::atomic<size_t> used{0};
+    std::string err;
+    std::recursive_mutex mu;  // serialises calls that share the context's scratch
+
+    // point table (QueryResult columns)
+    uint64_t npts = 0;
+    int loc_attrib = -1;
+    std::vector<rjh::Column> cols;
+    rjh::TimeIndex tix;
+
+    // polygon set bound for rj_execute: the context's own (rj_set_polygons)
+    // or a caller's rj_polyset (rj_use_polyset)
+    rjh::PolySet own;
+    rjh::PolySet* ps = &own;
+    const rjh::PolySet* cache_owner = nullptr;   // set whose grid / classified grid the scratch holds
+    uint64_t cache_version = 0;
+
+    std::map<std::string, rjh::DevBuf> scratch;
+
+    rj_timings tm{};
+    cudaEvent_t ev[8]{};
+    int* d_err = nullptr;     // device status word of bounded waits
+    int sum_shift = 0;        // fixed-point scale 2^s of the current query's sums
+    uint64_t row0 = 0, row1 = ~0ULL;   // rows of the current query (time index window)
+    unsigned long long* overlap_pending = nullptr;   // label-map counters to check after the call
+    int server_running = 0;   // a serving loop owns the context
+    void* batch_engine = nullptr;   // executor of rj_execute_batch
+};
+
+struct rj_polyset {
+    rj_ctx* ctx = nullptr;
+    rjh::PolySet s;
+};
+
+namespace rjh {
+
+int fail(rj_ctx* c, int code, const char* fmt, ...);
+
+#define RJ_CUDA(call)                                                                         \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return ::rjh::fail(ctx, RJ_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                               __FILE__, __LINE__);                                           \
+    } while (0)
+
+int dev_alloc(rj_ctx* ctx, DevBuf& b, size_t bytes);
+void dev_free(rj_ctx* ctx, DevBuf& b);
+const Column* find_col(const rj_ctx* ctx, int attrib);
+double now_ms();
+
+// Raster canvas plan: RasterJoin::updateBuffers (RasterJoin.cpp:51-78) and
+// the per-tile MVP (RasterJoin.cpp:224-231, Utils.h:36-46).
+struct RasterPlan {
+    double cell = 0;
+    int actual_x = 0, actual_y = 0;
+    int splitx = 1, splity = 1;
+    int resx = 1, resy = 1;
+    std::vector<float4> colxf, rowxf;
+};
+int plan_raster_bbox(rj_ctx* ctx, const double* bbox, const rj_query* q, RasterPlan& rp);
+int build_filter(rj_ctx* ctx, const rj_query* q, rj::DevFilter& f, bool force_count, bool* empty);
+int load_polyset(rj_ctx* ctx, PolySet& s, const float* xy, const int32_t* pindex, int32_t npolys,
+                 const double* bbox);
+void free_polyset(rj_ctx* ctx, PolySet& s);
+// rows [r0, r1) of the resident table a query can touch (all rows without a
+// time index on its time attribute)
+void decode_result(int P, const unsigned long long* hc, const unsigned long long* hq, const double* hnf, int shift,
+                   const long long* hb, rj_result* res);
+void free_batch_engine(rj_ctx* ctx);
+void query_rows(const rj_ctx* ctx, const rj_query* q, uint64_t& r0, uint64_t& r1);
+
+}  // namespace rjh

@@ -174,4 +174,73 @@ void launch_label_finish(uint16_t* label, const uint32_t* mask, int resx, int re
 void launch_cls_codes(const int* cell_start, const int4* entries, uint32_t* code, int ncells, int sms,
                       cudaStream_t st);
 
+// ---------------------------------------------------------------------------
+// Batched raster join: many queries over one resident point table in one
+// launch.  Work items are blocks of rows of a "segment" (a row range that
+// the same set of queries covers); a block of rows is staged in shared memory
+// once and every query of its segment runs over it.
+constexpr int kBatchMaxCols = 6;          // distinct scalar columns one batch may read
+enum { BQ_LABEL = 0, BQ_SPLAT = 1, BQ_SKIP = 2 };
+
+struct BatchQuery {
+    uint32_t lo[kBatchMaxCols];           // interval predicate per batch column:
+    uint32_t span[kBatchMaxCols];         //   order_key(v) - lo <= span (lo 0, span ~0: none)
+    int aggr_u;                           // batch column of the aggregate, -1: count only
+    int aggr_typ;
+    float sum_scale;                      // fixed-point scale 2^(s-32)
+    int mode;                             // BQ_*
+    int P;
+    int hist_smem;                        // per-block shared-memory histogram (P <= capacity)
+    CanvasXf cx;
+    const uint16_t* label;                // BQ_LABEL: [T][resy][resx]
+    uint32_t* canvas_c;                   // BQ_SPLAT: [T][resy][resx]
+    long long* canvas_s;
+    unsigned long long* out_count;        // [P]
+    unsigned long long* out_sum;          // [P] fixed-point
+    double* out_nonfinite;                // [P]
+};
+
+struct BatchSeg {
+    uint64_t r0, r1;                      // rows
+    uint64_t item0;                       // first work item of the segment
+    int qbegin, qend;                     // queries: qlist[qbegin .. qend)
+};
+
+struct BatchArgs {
+    const float2* xy;
+    int nu;                               // batch columns
+    const uint32_t* ucol[kBatchMaxCols];
+    int utyp[kBatchMaxCols];
+    const BatchQuery* q;
+    const int* qlist;
+    const BatchSeg* seg;
+    int nseg;
+    uint64_t nitems;
+    unsigned long long* work;             // work-item counter (zeroed before the launch)
+    int rows;                             // rows per work item
+    int hist_cap;                         // shared-memory histogram entries
+};
+
+// block shape of the batched kernel (picked by the tuner)
+struct BatchShape {
+    int threads;                          // 256 or 512
+    int rows;                             // rows per work item: 2048, 4096 or 8192
+};
+size_t batch_smem_bytes(const BatchShape& s, int nu, int hist_cap);
+int batch_blocks_per_sm(const BatchShape& s, int nu, int hist_cap);
+bool launch_batch_points(const BatchArgs& a, const BatchShape& s, int sms, cudaStream_t st);
+
+// time index of the resident table
+void launch_time_minmax(const uint32_t* t, uint64_t n, unsigned* out_min, unsigned* out_max, int sms, cudaStream_t st);
+void launch_time_hist(const uint32_t* t, uint64_t n, uint32_t tmin, uint32_t tmax, int nb, unsigned* hist, int sms,
+                      cudaStream_t st);
+struct PermuteCols {
+    int ncol;
+    const void* src[RJ_MAX_ATTRIBUTES];
+    void* dst[RJ_MAX_ATTRIBUTES];
+    int esz[RJ_MAX_ATTRIBUTES];           // 4 or 8 bytes
+};
+void launch_time_scatter(const uint32_t* t, uint64_t n, uint32_t tmin, uint32_t tmax, int nb,
+                         unsigned long long* cursor, const PermuteCols& pc, int sms, cudaStream_t st);
+
 }  // namespace rj

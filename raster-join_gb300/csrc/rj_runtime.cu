@@ -16,80 +16,12 @@
 #include <vector>
 
 #include "rj_device.cuh"
+#include "rj_internal.h"
 #include "rj_launch.h"
 
 using namespace rj;
 
-namespace {
-
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-};
-
-struct Column {
-    int attrib = -1;
-    int type = RJ_FLOAT;
-    void* d = nullptr;
-    bool owned = false;
-    float absmax = 0.f;     // largest finite |aggregate value| (sizes the fixed-point sums)
-};
-
-// Derived structures of the current polygon set, rebuilt on demand.
-struct GridCache {
-    bool valid = false;
-    int res = 0;
-    int clamp = 0;
-    bool pair_cell = false;
-    size_t nentries = 0;
-};
-
-struct ExactCache {
-    bool valid = false;
-    int res = 0;
-    int user_res = 0;
-    size_t nentries = 0, nedges = 0;
-};
-
-}  // namespace
-
-struct rj_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int sms = 1;
-    int64_t budget = 0;       // bytes, 0 = unlimited
-    size_t used = 0;
-    std::string err;
-
-    // point table (QueryResult columns)
-    uint64_t npts = 0;
-    int loc_attrib = -1;
-    std::vector<Column> cols;
-
-    // polygon set (PolyHandler polys / pindexes / bounds)
-    int P = 0, V = 0;
-    std::vector<float> h_xy;
-    std::vector<int> h_pindex;
-    std::vector<float4> h_mbr;      // per polygon (minx, miny, maxx, maxy)
-    double bbox[4] = {0, 0, 0, 0};
-    float max_abs_coord = 0.f, max_edge_dx = 0.f, max_edge_dy = 0.f;
-    DevBuf d_verts, d_pindex, d_edge_poly;
-    uint64_t poly_version = 0;
-    int overlap_known = -1;   // -1 unknown, 0 no overlap, 1 overlap
-
-    GridCache grid;
-    ExactCache exact;
-    std::map<std::string, DevBuf> scratch;
-
-    rj_timings tm{};
-    cudaEvent_t ev[8]{};
-    int* d_err = nullptr;     // device status word of bounded waits
-    int sum_shift = 0;        // fixed-point scale 2^s of the current query's sums
-    unsigned long long* overlap_pending = nullptr;   // label-map counters to check after the call
-};
-
-namespace {
+namespace rjh {
 
 int fail(rj_ctx* c, int code, const char* fmt, ...) {
     char buf[512];
@@ -97,17 +29,12 @@ int fail(rj_ctx* c, int code, const char* fmt, ...) {
     va_start(ap, fmt);
     vsnprintf(buf, sizeof buf, fmt, ap);
     va_end(ap);
-    if (c) c->err = buf;
+    if (c) {
+        std::lock_guard<std::recursive_mutex> lock(c->mu);
+        c->err = buf;
+    }
     return code;
 }
-
-#define RJ_CUDA(call)                                                                         \
-    do {                                                                                      \
-        cudaError_t e_ = (call);                                                              \
-        if (e_ != cudaSuccess)                                                                \
-            return fail(ctx, RJ_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
-                        __FILE__, __LINE__);                                                  \
-    } while (0)
 
 int dev_alloc(rj_ctx* ctx, DevBuf& b, size_t bytes) {
     if (b.p && b.bytes >= bytes) return RJ_OK;
@@ -121,7 +48,7 @@ int dev_alloc(rj_ctx* ctx, DevBuf& b, size_t bytes) {
     bytes = (bytes + 255) & ~size_t(255);
     if (ctx->budget > 0 && (int64_t)(ctx->used + bytes) > ctx->budget)
         return fail(ctx, RJ_E_OOM, "device memory budget exceeded: need %zu more bytes, %zu of %lld in use",
-                    bytes, ctx->used, (long long)ctx->budget);
+                    bytes, (size_t)ctx->used.load(), (long long)ctx->budget);
     cudaError_t e = cudaMalloc(&b.p, bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -179,22 +106,11 @@ double now_ms() {
     return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
 }
 
-// ---------------------------------------------------------------------------
-// Raster canvas plan: RasterJoin::updateBuffers (RasterJoin.cpp:51-78) and the
-// per-tile MVP (RasterJoin.cpp:224-231, Utils.h:36-46).
-struct RasterPlan {
-    double cell = 0;
-    int actual_x = 0, actual_y = 0;
-    int splitx = 1, splity = 1;
-    int resx = 1, resy = 1;
-    std::vector<float4> colxf, rowxf;
-};
-
-int plan_raster(rj_ctx* ctx, const rj_query* q, RasterPlan& rp) {
+int plan_raster_bbox(rj_ctx* ctx, const double* bbox, const rj_query* q, RasterPlan& rp) {
     double ground = q->ground_resolution > 0 ? q->ground_resolution : 1.0;
     double cell = q->cell_size > 0 ? q->cell_size : (q->accuracy_m / std::sqrt(2.0)) / ground;
     if (!(cell > 0) || !std::isfinite(cell)) return fail(ctx, RJ_E_INVALID, "invalid cell size %g", cell);
-    double dx = ctx->bbox[2] - ctx->bbox[0], dy = ctx->bbox[3] - ctx->bbox[1];
+    double dx = bbox[2] - bbox[0], dy = bbox[3] - bbox[1];
     if (!(dx > 0 && dy > 0)) return fail(ctx, RJ_E_INVALID, "degenerate polygon bounds");
     double ax = std::ceil(dx / cell), ay = std::ceil(dy / cell);
     if (ax > 2e6 || ay > 2e6) return fail(ctx, RJ_E_INVALID, "canvas too large: %.0f x %.0f", ax, ay);
@@ -211,14 +127,14 @@ int plan_raster(rj_ctx* ctx, const rj_query* q, RasterPlan& rp) {
     rp.colxf.resize(rp.splitx);
     rp.rowxf.resize(rp.splity);
     for (int c = 0; c < rp.splitx; ++c) {
-        double lb = ctx->bbox[0] + c * tdx, rt = lb + tdx;
+        double lb = bbox[0] + c * tdx, rt = lb + tdx;
         double origin = (rt + lb) / 2, half = (rt - lb) / 2;
         float s = (float)(1.0 / half);
         float t = s * (float)(-origin);
         rp.colxf[c] = make_float4(s, t, rp.resx * 0.5f, (float)tdx);
     }
     for (int r = 0; r < rp.splity; ++r) {
-        double lb = ctx->bbox[1] + r * tdy, rt = lb + tdy;
+        double lb = bbox[1] + r * tdy, rt = lb + tdy;
         double origin = (rt + lb) / 2, half = (rt - lb) / 2;
         float s = (float)(1.0 / half);
         float t = s * (float)(-origin);
@@ -226,6 +142,8 @@ int plan_raster(rj_ctx* ctx, const rj_query* q, RasterPlan& rp) {
     }
     return RJ_OK;
 }
+
+int plan_raster(rj_ctx* ctx, const rj_query* q, RasterPlan& rp) { return plan_raster_bbox(ctx, ctx->ps->bbox, q, rp); }
 
 // Filter + aggregation (GLFunction::setupPoints GLFunction.cpp:199-344).
 int build_filter(rj_ctx* ctx, const rj_query* q, DevFilter& f, bool force_count, bool* empty = nullptr) {
@@ -375,10 +293,10 @@ int transform_vertices(rj_ctx* ctx, const std::vector<float4>& colxf, const std:
     if ((rc = scratch_t(ctx, "rowxf", rowxf.size(), &drow))) return rc;
     RJ_CUDA(cudaMemcpyAsync(dcol, colxf.data(), colxf.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
     RJ_CUDA(cudaMemcpyAsync(drow, rowxf.data(), rowxf.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
-    if ((rc = scratch_t(ctx, "wv", (size_t)T * ctx->V, wv))) return rc;
+    if ((rc = scratch_t(ctx, "wv", (size_t)T * ctx->ps->V, wv))) return rc;
     *wf = nullptr;
-    if (want_float && (rc = scratch_t(ctx, "wf", (size_t)T * ctx->V, wf))) return rc;
-    launch_transform_vertices((const float2*)ctx->d_verts.p, ctx->V, dcol, drow, (int)colxf.size(), T, *wv,
+    if (want_float && (rc = scratch_t(ctx, "wf", (size_t)T * ctx->ps->V, wf))) return rc;
+    launch_transform_vertices((const float2*)ctx->ps->d_verts.p, ctx->ps->V, dcol, drow, (int)colxf.size(), T, *wv,
                               want_float ? *wf : nullptr, ctx->sms, ctx->stream);
     RJ_CUDA(cudaGetLastError());
     return RJ_OK;
@@ -387,9 +305,9 @@ int transform_vertices(rj_ctx* ctx, const std::vector<float4>& colxf, const std:
 // Grid index (GLFunction::createPolyIndex GLFunction.cpp:65-156).
 int build_grid(rj_ctx* ctx, int res, int clamp, IndexArgs& ia, bool with_pair_cell = false) {
     if (res <= 0 || res > 8192) return fail(ctx, RJ_E_INVALID, "grid resolution %d out of range", res);
-    GridCache& g = ctx->grid;
-    const double dx = ctx->bbox[2] - ctx->bbox[0], dy = ctx->bbox[3] - ctx->bbox[1];
-    const float lbx = (float)ctx->bbox[0], lby = (float)ctx->bbox[1];
+    GridCache& g = ctx->ps->grid;
+    const double dx = ctx->ps->bbox[2] - ctx->ps->bbox[0], dy = ctx->ps->bbox[3] - ctx->ps->bbox[1];
+    const float lbx = (float)ctx->ps->bbox[0], lby = (float)ctx->ps->bbox[1];
     const float csx = (float)(dx / res), csy = (float)(dy / res);
     int *cell_start, *entries;
     int rc;
@@ -401,9 +319,9 @@ int build_grid(rj_ctx* ctx, int res, int clamp, IndexArgs& ia, bool with_pair_ce
         if ((rc = scratch_t(ctx, "grid_tmp", (size_t)scan_tmp_ints((int)ncells), &tmp))) return rc;
         RJ_CUDA(cudaMemsetAsync(cnt, 0, ncells * sizeof(int), ctx->stream));
         GridArgs ga{};
-        ga.verts = (const float2*)ctx->d_verts.p;
-        ga.pindex = (const int*)ctx->d_pindex.p;
-        ga.P = ctx->P;
+        ga.verts = (const float2*)ctx->ps->d_verts.p;
+        ga.pindex = (const int*)ctx->ps->d_pindex.p;
+        ga.P = ctx->ps->P;
         ga.lbx = lbx; ga.lby = lby; ga.csx = csx; ga.csy = csy;
         ga.res = res;
         ga.compat_clamp = clamp;
@@ -434,8 +352,8 @@ int build_grid(rj_ctx* ctx, int res, int clamp, IndexArgs& ia, bool with_pair_ce
         if ((rc = scratch_t(ctx, "grid_start", ncells + 1, &cell_start))) return rc;
         if ((rc = scratch_t(ctx, "grid_entries", std::max<size_t>(g.nentries, 1), &entries))) return rc;
     }
-    ia.verts = (const float2*)ctx->d_verts.p;
-    ia.pindex = (const int*)ctx->d_pindex.p;
+    ia.verts = (const float2*)ctx->ps->d_verts.p;
+    ia.pindex = (const int*)ctx->ps->d_pindex.p;
     ia.cell_start = cell_start;
     ia.entries = entries;
     ia.lbx = lbx; ia.lby = lby; ia.csx = csx; ia.csy = csy;
@@ -446,8 +364,8 @@ int build_grid(rj_ctx* ctx, int res, int clamp, IndexArgs& ia, bool with_pair_ce
 // Resolution of the classified grid: the query grid times 2^k, about 1024
 // cells across, with cells much larger than the fp32 error of the test.
 int exact_res(const rj_ctx* ctx, int res) {
-    const double ext = std::max(ctx->bbox[2] - ctx->bbox[0], ctx->bbox[3] - ctx->bbox[1]);
-    const double err = std::ldexp(1.0, -21) * (ctx->max_abs_coord + 6.0 * std::max(ctx->max_edge_dx, ctx->max_edge_dy) + 1.0);
+    const double ext = std::max(ctx->ps->bbox[2] - ctx->ps->bbox[0], ctx->ps->bbox[3] - ctx->ps->bbox[1]);
+    const double err = std::ldexp(1.0, -21) * (ctx->ps->max_abs_coord + 6.0 * std::max(ctx->ps->max_edge_dx, ctx->ps->max_edge_dy) + 1.0);
     int g = res;
     while (g * 2 <= 1024 && ext / (g * 2) > 64.0 * err) g *= 2;
     return g;
@@ -462,10 +380,10 @@ int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix) {
     int rc;
     const int G = exact_res(ctx, user_res);
     const int scale = G / user_res;
-    ExactCache& xc = ctx->exact;
+    ExactCache& xc = ctx->ps->exact;
     const size_t ncells = (size_t)G * G;
-    const double dx = ctx->bbox[2] - ctx->bbox[0], dy = ctx->bbox[3] - ctx->bbox[1];
-    const float lbx = (float)ctx->bbox[0], lby = (float)ctx->bbox[1];
+    const double dx = ctx->ps->bbox[2] - ctx->ps->bbox[0], dy = ctx->ps->bbox[3] - ctx->ps->bbox[1];
+    const float lbx = (float)ctx->ps->bbox[0], lby = (float)ctx->ps->bbox[1];
     const float csx = (float)(dx / G), csy = (float)(dy / G);
     int* start2;
     int4* entries2;
@@ -473,15 +391,15 @@ int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix) {
     if (!(xc.valid && xc.res == G && xc.user_res == user_res)) {
         // candidate ranges on the query grid, in fp32 as the reference computes them
         const float rcsx = (float)(dx / user_res), rcsy = (float)(dy / user_res);
-        const int P = ctx->P;
+        const int P = ctx->ps->P;
         std::vector<int> off(P + 1);
         std::vector<int4> rng(P);
         long long total = 0;
         for (int p = 0; p < P; ++p) {
             off[p] = (int)total;
-            const float4 m = ctx->h_mbr[p];
+            const float4 m = ctx->ps->h_mbr[p];
             int stx = 0, sty = 0, enx = 0, eny = 0;
-            if (ctx->h_pindex[p + 1] > ctx->h_pindex[p]) {
+            if (ctx->ps->h_pindex[p + 1] > ctx->ps->h_pindex[p]) {
                 volatile float ax = m.x - lbx, ay = m.y - lby, bx = m.z - lbx, by = m.w - lby;
                 volatile float qx0 = ax / rcsx, qy0 = ay / rcsy, qx1 = bx / rcsx, qy1 = by / rcsy;
                 stx = (int)qx0; sty = (int)qy0;
@@ -517,8 +435,8 @@ int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix) {
         RJ_CUDA(cudaMemsetAsync(cursor, 0, ncells * sizeof(int), ctx->stream));
         RJ_CUDA(cudaMemsetAsync(plist_n, 0, sizeof(int), ctx->stream));
         ClsArgs c{};
-        c.verts = (const float2*)ctx->d_verts.p;
-        c.pindex = (const int*)ctx->d_pindex.p;
+        c.verts = (const float2*)ctx->ps->d_verts.p;
+        c.pindex = (const int*)ctx->ps->d_pindex.p;
         c.P = P;
         c.pair_off = doff;
         c.prange = drng;
@@ -528,8 +446,8 @@ int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix) {
         c.lbx = lbx; c.lby = lby; c.csx = csx; c.csy = csy;
         c.res = G;
         const double U = std::ldexp(1.0, -24);
-        const double Mc = std::max<double>(ctx->max_abs_coord, std::max(std::fabs(ctx->bbox[0]), std::fabs(ctx->bbox[2])));
-        const double E = 8.0 * U * (Mc + 6.0 * std::max(ctx->max_edge_dx, ctx->max_edge_dy));
+        const double Mc = std::max<double>(ctx->ps->max_abs_coord, std::max(std::fabs(ctx->ps->bbox[0]), std::fabs(ctx->ps->bbox[2])));
+        const double E = 8.0 * U * (Mc + 6.0 * std::max(ctx->ps->max_edge_dx, ctx->ps->max_edge_dy));
         const double delta = 8.0 * U * (2.0 * Mc + G * std::max((double)csx, (double)csy));
         const double rel = 8.0 * U * (Mc + G * std::max((double)csx, (double)csy));
         c.margin = (float)(2.0 * (E + delta + rel) + 1e-7 * std::max(dx, dy));
@@ -609,10 +527,14 @@ int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix) {
 PointArgs make_point_args(rj_ctx* ctx, const DevFilter& f, unsigned long long* oc, unsigned long long* os) {
     PointArgs pa{};
     const Column* loc = find_col(ctx, ctx->loc_attrib);
-    pa.xy = (const float2*)loc->d;
-    pa.n = ctx->npts;
+    // rows the query can touch (time index window; the exact time predicate still applies)
+    const uint64_t r0 = std::min(ctx->row0, ctx->npts), r1 = std::max(r0, std::min(ctx->row1, ctx->npts));
+    pa.xy = (const float2*)loc->d + r0;
+    pa.n = r1 - r0;
     pa.f = f;
-    pa.P = ctx->P;
+    for (int c = 0; c < pa.f.ncol; ++c) pa.f.col[c] += r0;
+    if (pa.f.aggr_col) pa.f.aggr_col += r0;
+    pa.P = ctx->ps->P;
     pa.out_count = oc;
     pa.out_sum = os;
     pa.out_nonfinite = (double*)ctx->scratch["out_nonfinite"].p;
@@ -628,8 +550,8 @@ CanvasXf make_canvas_xf(rj_ctx* ctx, const RasterPlan& rp, const float4* dcol, c
     cx.splity = rp.splity;
     cx.resx = rp.resx;
     cx.resy = rp.resy;
-    cx.lbx = (float)ctx->bbox[0];
-    cx.lby = (float)ctx->bbox[1];
+    cx.lbx = (float)ctx->ps->bbox[0];
+    cx.lby = (float)ctx->ps->bbox[1];
     cx.tdx = rp.colxf[0].w;
     cx.tdy = rp.rowxf[0].w;
     cx.col0 = rp.colxf[0];
@@ -695,7 +617,7 @@ int label_map(rj_ctx* ctx, PolyPassArgs& a, const char* key, size_t npix, const 
     // the two counters with the results and re-runs the query on the canvas
     // path if some pixel centre lay in two polygons.
     *overlap = 0;
-    if (ctx->overlap_known != 0) ctx->overlap_pending = cnt;
+    if (ctx->ps->overlap_known != 0) ctx->overlap_pending = cnt;
     *out = label;
     a.label = nullptr;
     return RJ_OK;
@@ -724,9 +646,9 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
     PolyPassArgs a{};
     a.wv = wv;
     a.wf = wf;
-    a.pindex = (const int*)ctx->d_pindex.p;
-    a.P = ctx->P;
-    a.V = ctx->V;
+    a.pindex = (const int*)ctx->ps->d_pindex.p;
+    a.P = ctx->ps->P;
+    a.V = ctx->ps->V;
     a.T = T;
     a.resx = rp.resx;
     a.resy = rp.resy;
@@ -735,8 +657,8 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
     a.out_bounds = es.out_bounds;
     a.line_filter = (q->flags & RJ_FLAG_LINE_FILTER) ? 1 : 0;
 
-    bool use_label = !bounds && !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->overlap_known != 1 &&
-                     ctx->P <= kMaxLabelPolys;
+    bool use_label = !bounds && !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->ps->overlap_known != 1 &&
+                     ctx->ps->P <= kMaxLabelPolys;
     if (use_label) {
         uint16_t* label;
         int overlap = 0;
@@ -816,15 +738,15 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     if ((rc = build_exact(ctx, q->grid_res, ix))) return rc;
 
     // canvas: getResolution(bbox, fboSize) (HybridJoin.cpp:62-66, Utils.h:29-34)
-    const double dx = ctx->bbox[2] - ctx->bbox[0], dy = ctx->bbox[3] - ctx->bbox[1];
+    const double dx = ctx->ps->bbox[2] - ctx->ps->bbox[0], dy = ctx->ps->bbox[3] - ctx->ps->bbox[1];
     const int fbo = q->hybrid_canvas > 0 ? q->hybrid_canvas : 4096;
     const float cellf = (float)std::max(dx / fbo, dy / fbo);
     const int resx = std::max(1, (int)std::fabs(std::ceil(dx / cellf)));
     const int resy = std::max(1, (int)std::fabs(std::ceil(dy / cellf)));
     HybXf h{};
     {
-        float lbx = (float)ctx->bbox[0], lby = (float)ctx->bbox[1];
-        float rtx = (float)ctx->bbox[2], rty = (float)ctx->bbox[3];
+        float lbx = (float)ctx->ps->bbox[0], lby = (float)ctx->ps->bbox[1];
+        float rtx = (float)ctx->ps->bbox[2], rty = (float)ctx->ps->bbox[3];
         volatile float sx = rtx + lbx, sy = rty + lby, qx = rtx - lbx, qy = rty - lby;
         h.ox = sx / 2.0f;
         h.oy = sy / 2.0f;
@@ -842,19 +764,19 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     if ((rc = scratch_t(ctx, "hyb_mask", (size_t)words * resy, &mask))) return rc;
     RJ_CUDA(cudaMemsetAsync(mraw, 0, (size_t)words * resy * 4, ctx->stream));
     const double pix_w = std::min(dx / resx, dy / resy);
-    const double err_world = std::ldexp(1.0, -21) * (ctx->max_abs_coord + 6.0 * std::max(ctx->max_edge_dx, ctx->max_edge_dy) + 1.0);
+    const double err_world = std::ldexp(1.0, -21) * (ctx->ps->max_abs_coord + 6.0 * std::max(ctx->ps->max_edge_dx, ctx->ps->max_edge_dy) + 1.0);
     const int radius = std::max(1, (int)std::ceil(err_world / pix_w + 0.05));
     if (radius > 31) return fail(ctx, RJ_E_UNSUPPORTED, "hybrid canvas too fine for fp32 coordinates (radius %d)", radius);
-    launch_outline_mask((const float2*)ctx->d_verts.p, (const int*)ctx->d_pindex.p, ctx->P,
-                        (const int*)ctx->d_edge_poly.p, ctx->V, h, 0.05f, mraw, words, ctx->sms, ctx->stream);
+    launch_outline_mask((const float2*)ctx->ps->d_verts.p, (const int*)ctx->ps->d_pindex.p, ctx->ps->P,
+                        (const int*)ctx->ps->d_edge_poly.p, ctx->ps->V, h, 0.05f, mraw, words, ctx->sms, ctx->stream);
     launch_dilate_mask(mraw, mask, resx, resy, words, radius, ctx->sms, ctx->stream);
     RJ_CUDA(cudaGetLastError());
 
     // polygon coverage of the hybrid canvas (getMVP(bbox), HybridJoin.cpp:63)
     std::vector<float4> colxf(1), rowxf(1);
     {
-        double ox = (ctx->bbox[2] + ctx->bbox[0]) / 2, hx = (ctx->bbox[2] - ctx->bbox[0]) / 2;
-        double oy = (ctx->bbox[3] + ctx->bbox[1]) / 2, hy = (ctx->bbox[3] - ctx->bbox[1]) / 2;
+        double ox = (ctx->ps->bbox[2] + ctx->ps->bbox[0]) / 2, hx = (ctx->ps->bbox[2] - ctx->ps->bbox[0]) / 2;
+        double oy = (ctx->ps->bbox[3] + ctx->ps->bbox[1]) / 2, hy = (ctx->ps->bbox[3] - ctx->ps->bbox[1]) / 2;
         float sx = (float)(1.0 / hx), sy = (float)(1.0 / hy);
         colxf[0] = make_float4(sx, sx * (float)(-ox), resx * 0.5f, (float)dx);
         rowxf[0] = make_float4(sy, sy * (float)(-oy), resy * 0.5f, (float)dy);
@@ -864,9 +786,9 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     if ((rc = transform_vertices(ctx, colxf, rowxf, &wv, &wf, false))) return rc;
     PolyPassArgs a{};
     a.wv = wv;
-    a.pindex = (const int*)ctx->d_pindex.p;
-    a.P = ctx->P;
-    a.V = ctx->V;
+    a.pindex = (const int*)ctx->ps->d_pindex.p;
+    a.P = ctx->ps->P;
+    a.V = ctx->ps->V;
     a.T = 1;
     a.resx = resx;
     a.resy = resy;
@@ -878,7 +800,7 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     ha.h = h;
     ha.border = mask;
     ha.words = words;
-    bool use_label = !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->overlap_known != 1 && ctx->P <= kMaxLabelPolys;
+    bool use_label = !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->ps->overlap_known != 1 && ctx->ps->P <= kMaxLabelPolys;
     if (use_label) {
         uint16_t* label;
         int overlap = 0;
@@ -921,7 +843,116 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     return RJ_OK;
 }
 
-}  // namespace
+// Polygon collection -> PolySet (PolyHandler::addPolygonCollection
+// PolyHandler.cpp:49-80; bounds as readPolygons PolyHandler.cpp:178-186).
+int load_polyset(rj_ctx* ctx, PolySet& s, const float* xy, const int32_t* pindex, int32_t npolys,
+                 const double* bbox) {
+    if (npolys <= 0 || !pindex || !xy) return fail(ctx, RJ_E_INVALID, "empty polygon set");
+    if (pindex[0] != 0) return fail(ctx, RJ_E_INVALID, "pindex[0] must be 0");
+    for (int i = 0; i < npolys; ++i)
+        if (pindex[i + 1] < pindex[i]) return fail(ctx, RJ_E_INVALID, "pindex not monotone at %d", i);
+    const int V = pindex[npolys];
+    double bb[4] = {INFINITY, INFINITY, -INFINITY, -INFINITY};
+    float maxabs = 0.f, mdx = 0.f, mdy = 0.f;
+    for (int i = 0; i < npolys; ++i) {
+        const int v0 = pindex[i], n = pindex[i + 1] - v0;
+        for (int k = 0; k < n; ++k) {
+            float x = xy[2 * (v0 + k)], y = xy[2 * (v0 + k) + 1];
+            if (!std::isfinite(x) || !std::isfinite(y)) return fail(ctx, RJ_E_INVALID, "non-finite vertex in polygon %d", i);
+            bb[0] = std::min(bb[0], (double)x); bb[1] = std::min(bb[1], (double)y);
+            bb[2] = std::max(bb[2], (double)x); bb[3] = std::max(bb[3], (double)y);
+            maxabs = std::max(maxabs, std::max(std::fabs(x), std::fabs(y)));
+            int kn = (k + 1 == n) ? 0 : k + 1;
+            mdx = std::max(mdx, std::fabs(xy[2 * (v0 + kn)] - x));
+            mdy = std::max(mdy, std::fabs(xy[2 * (v0 + kn) + 1] - y));
+        }
+    }
+    if (bbox) {
+        for (int i = 0; i < 4; ++i) bb[i] = bbox[i];
+        maxabs = std::max(maxabs, (float)std::max(std::max(std::fabs(bb[0]), std::fabs(bb[1])),
+                                                   std::max(std::fabs(bb[2]), std::fabs(bb[3]))));
+    }
+    if (!(bb[2] > bb[0] && bb[3] > bb[1]))
+        return fail(ctx, RJ_E_INVALID, "polygon bounds are empty");   // CPUJoin.cpp:51-54
+    cudaSetDevice(ctx->device);
+    int rc;
+    if ((rc = dev_alloc(ctx, s.d_verts, (size_t)V * 8))) return rc;
+    if ((rc = dev_alloc(ctx, s.d_pindex, (size_t)(npolys + 1) * 4))) return rc;
+    if ((rc = dev_alloc(ctx, s.d_edge_poly, (size_t)V * 4))) return rc;
+    std::vector<int> edge_poly(V);
+    for (int i = 0; i < npolys; ++i)
+        for (int k = pindex[i]; k < pindex[i + 1]; ++k) edge_poly[k] = i;
+    s.h_xy.assign(xy, xy + 2 * (size_t)V);
+    s.h_pindex.assign(pindex, pindex + npolys + 1);
+    s.h_mbr.assign(npolys, make_float4(0.f, 0.f, 0.f, 0.f));
+    for (int i = 0; i < npolys; ++i) {
+        float a = INFINITY, b = INFINITY, c = -INFINITY, d = -INFINITY;
+        for (int k = pindex[i]; k < pindex[i + 1]; ++k) {
+            a = std::min(a, xy[2 * k]); c = std::max(c, xy[2 * k]);
+            b = std::min(b, xy[2 * k + 1]); d = std::max(d, xy[2 * k + 1]);
+        }
+        s.h_mbr[i] = make_float4(a, b, c, d);
+    }
+    RJ_CUDA(cudaMemcpyAsync(s.d_verts.p, xy, (size_t)V * 8, cudaMemcpyHostToDevice, ctx->stream));
+    RJ_CUDA(cudaMemcpyAsync(s.d_pindex.p, pindex, (size_t)(npolys + 1) * 4, cudaMemcpyHostToDevice, ctx->stream));
+    RJ_CUDA(cudaMemcpyAsync(s.d_edge_poly.p, edge_poly.data(), (size_t)V * 4, cudaMemcpyHostToDevice, ctx->stream));
+    RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    s.P = npolys;
+    s.V = V;
+    for (int i = 0; i < 4; ++i) s.bbox[i] = bb[i];
+    s.max_abs_coord = maxabs;
+    s.max_edge_dx = mdx;
+    s.max_edge_dy = mdy;
+    static std::atomic<uint64_t> g_set_version{0};
+    s.version = ++g_set_version;
+    s.overlap_known = -1;
+    s.grid.valid = false;
+    s.exact.valid = false;
+    return RJ_OK;
+}
+
+void free_polyset(rj_ctx* ctx, PolySet& s) {
+    dev_free(ctx, s.d_verts);
+    dev_free(ctx, s.d_pindex);
+    dev_free(ctx, s.d_edge_poly);
+    s.P = s.V = 0;
+}
+
+void query_rows(const rj_ctx* ctx, const rj_query* q, uint64_t& r0, uint64_t& r1) {
+    r0 = 0;
+    r1 = ctx->npts;
+    if (ctx->tix.valid && q->time_attrib >= 0 && q->time_attrib == ctx->tix.attrib)
+        ctx->tix.rows(q->t_start, q->t_end, ctx->npts, r0, r1);
+}
+
+// Per-polygon device outputs -> rj_result: exact counts, sums decoded from
+// int64 fixed point (2^-shift) plus the fp64 sum of non-finite values, the
+// reference's int32[3P] layout and the int32[4P] bounds.
+void decode_result(int P, const unsigned long long* hc, const unsigned long long* hq, const double* hnf, int shift,
+                   const long long* hb, rj_result* res) {
+    if (!res) return;
+    if (res->count) for (int i = 0; i < P; ++i) res->count[i] = hc[i];
+    if (res->sum || res->compat3) {
+        for (int i = 0; i < P; ++i) {
+            const double s = std::ldexp((double)(long long)hq[i], -shift) + hnf[i];
+            if (res->sum) res->sum[i] = s;
+            if (res->compat3) {
+                // [count | sum/100 | decimal*10], decodable by printResults (main.cpp:206-208)
+                const double hi = std::trunc(s / 100.0);
+                const double lo = std::nearbyint((s - 100.0 * hi) * 10.0);
+                res->compat3[i] = (int32_t)std::min<unsigned long long>(hc[i], 0x7fffffffULL);
+                res->compat3[P + i] = (int32_t)std::max(-2147483647.0, std::min(2147483647.0, hi));
+                res->compat3[2 * P + i] = (int32_t)lo;
+            }
+        }
+    }
+    if (res->bounds)
+        for (size_t i = 0; i < (size_t)4 * P; ++i) res->bounds[i] = hb ? (int32_t)std::min<long long>(hb[i], 0x7fffffffLL) : 0;
+}
+
+}  // namespace rjh
+
+using namespace rjh;
 
 // ===========================================================================
 // C ABI
@@ -986,10 +1017,9 @@ void rj_destroy(rj_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_batch_engine(ctx);
     free_points(ctx);
-    dev_free(ctx, ctx->d_verts);
-    dev_free(ctx, ctx->d_pindex);
-    dev_free(ctx, ctx->d_edge_poly);
+    free_polyset(ctx, ctx->own);
     for (auto& kv : ctx->scratch) dev_free(ctx, kv.second);
     for (auto& ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
@@ -1057,7 +1087,10 @@ static int load_points_impl(rj_ctx* ctx, const rj_column* cols, int32_t ncols, u
             return fail(ctx, RJ_E_INVALID, "column %d: device pointer not 16-byte aligned", i);
     }
     if (nloc != 1) return fail(ctx, RJ_E_INVALID, "location attribute %d not among the columns", loc);
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    if (ctx->server_running) return fail(ctx, RJ_E_BUSY, "a serving loop owns the context");
     cudaSetDevice(ctx->device);
+    ctx->tix.valid = false;
     // same layout as the resident table: copy into the existing buffers
     bool same = !device && (int)ctx->cols.size() == ncols && ctx->npts == npoints && ctx->loc_attrib == loc;
     for (int i = 0; same && i < ncols; ++i)
@@ -1126,6 +1159,9 @@ int rj_attach_points_device(rj_ctx* ctx, const rj_column* cols, int32_t ncols, u
 
 int rj_free_points(rj_ctx* ctx) {
     if (!ctx) return RJ_E_INVALID;
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    if (ctx->server_running) return fail(ctx, RJ_E_BUSY, "a serving loop owns the context");
+    ctx->tix.valid = false;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (Column& c : ctx->cols) {
@@ -1142,87 +1178,41 @@ int rj_free_points(rj_ctx* ctx) {
 
 int rj_set_polygons(rj_ctx* ctx, const float* xy, const int32_t* pindex, int32_t npolys, const double* bbox) {
     if (!ctx) return RJ_E_INVALID;
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
     ctx->err.clear();
-    if (npolys <= 0 || !pindex || !xy) return fail(ctx, RJ_E_INVALID, "empty polygon set");
-    if (pindex[0] != 0) return fail(ctx, RJ_E_INVALID, "pindex[0] must be 0");
-    for (int i = 0; i < npolys; ++i)
-        if (pindex[i + 1] < pindex[i]) return fail(ctx, RJ_E_INVALID, "pindex not monotone at %d", i);
-    const int V = pindex[npolys];
-    double bb[4] = {INFINITY, INFINITY, -INFINITY, -INFINITY};
-    float maxabs = 0.f, mdx = 0.f, mdy = 0.f;
-    for (int i = 0; i < npolys; ++i) {
-        const int v0 = pindex[i], n = pindex[i + 1] - v0;
-        for (int k = 0; k < n; ++k) {
-            float x = xy[2 * (v0 + k)], y = xy[2 * (v0 + k) + 1];
-            if (!std::isfinite(x) || !std::isfinite(y)) return fail(ctx, RJ_E_INVALID, "non-finite vertex in polygon %d", i);
-            bb[0] = std::min(bb[0], (double)x); bb[1] = std::min(bb[1], (double)y);
-            bb[2] = std::max(bb[2], (double)x); bb[3] = std::max(bb[3], (double)y);
-            maxabs = std::max(maxabs, std::max(std::fabs(x), std::fabs(y)));
-            int kn = (k + 1 == n) ? 0 : k + 1;
-            mdx = std::max(mdx, std::fabs(xy[2 * (v0 + kn)] - x));
-            mdy = std::max(mdy, std::fabs(xy[2 * (v0 + kn) + 1] - y));
-        }
-    }
-    if (bbox) {
-        for (int i = 0; i < 4; ++i) bb[i] = bbox[i];
-        maxabs = std::max(maxabs, (float)std::max(std::max(std::fabs(bb[0]), std::fabs(bb[1])),
-                                                   std::max(std::fabs(bb[2]), std::fabs(bb[3]))));
-    }
-    if (!(bb[2] > bb[0] && bb[3] > bb[1]))
-        return fail(ctx, RJ_E_INVALID, "polygon bounds are empty");   // CPUJoin.cpp:51-54
-    cudaSetDevice(ctx->device);
-    int rc;
-    if ((rc = dev_alloc(ctx, ctx->d_verts, (size_t)V * 8))) return rc;
-    if ((rc = dev_alloc(ctx, ctx->d_pindex, (size_t)(npolys + 1) * 4))) return rc;
-    if ((rc = dev_alloc(ctx, ctx->d_edge_poly, (size_t)V * 4))) return rc;
-    std::vector<int> edge_poly(V);
-    for (int i = 0; i < npolys; ++i)
-        for (int k = pindex[i]; k < pindex[i + 1]; ++k) edge_poly[k] = i;
-    ctx->h_xy.assign(xy, xy + 2 * (size_t)V);
-    ctx->h_pindex.assign(pindex, pindex + npolys + 1);
-    ctx->h_mbr.assign(npolys, make_float4(0.f, 0.f, 0.f, 0.f));
-    for (int i = 0; i < npolys; ++i) {
-        float a = INFINITY, b = INFINITY, c = -INFINITY, d = -INFINITY;
-        for (int k = pindex[i]; k < pindex[i + 1]; ++k) {
-            a = std::min(a, xy[2 * k]); c = std::max(c, xy[2 * k]);
-            b = std::min(b, xy[2 * k + 1]); d = std::max(d, xy[2 * k + 1]);
-        }
-        ctx->h_mbr[i] = make_float4(a, b, c, d);
-    }
-    RJ_CUDA(cudaMemcpyAsync(ctx->d_verts.p, xy, (size_t)V * 8, cudaMemcpyHostToDevice, ctx->stream));
-    RJ_CUDA(cudaMemcpyAsync(ctx->d_pindex.p, pindex, (size_t)(npolys + 1) * 4, cudaMemcpyHostToDevice, ctx->stream));
-    RJ_CUDA(cudaMemcpyAsync(ctx->d_edge_poly.p, edge_poly.data(), (size_t)V * 4, cudaMemcpyHostToDevice, ctx->stream));
-    RJ_CUDA(cudaStreamSynchronize(ctx->stream));
-    ctx->P = npolys;
-    ctx->V = V;
-    for (int i = 0; i < 4; ++i) ctx->bbox[i] = bb[i];
-    ctx->max_abs_coord = maxabs;
-    ctx->max_edge_dx = mdx;
-    ctx->max_edge_dy = mdy;
-    ctx->poly_version++;
-    ctx->overlap_known = -1;
-    ctx->grid.valid = false;
-    ctx->exact.valid = false;
+    if (ctx->server_running) return fail(ctx, RJ_E_BUSY, "a serving loop owns the context");
+    int rc = load_polyset(ctx, ctx->own, xy, pindex, npolys, bbox);
+    if (rc) return rc;
+    ctx->ps = &ctx->own;
     return RJ_OK;
 }
 
 int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
     if (!ctx || !q) return RJ_E_INVALID;
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
     ctx->err.clear();
     const double t0 = now_ms();
     if (ctx->npts == 0 && ctx->cols.empty()) return fail(ctx, RJ_E_NO_DATA, "point table not loaded");
-    if (ctx->P == 0) return fail(ctx, RJ_E_NO_DATA, "polygons not set");
-    if (res && res->npolys != 0 && res->npolys != ctx->P)
-        return fail(ctx, RJ_E_INVALID, "result sized for %d polygons, polygon set has %d", res->npolys, ctx->P);
+    if (ctx->ps->P == 0) return fail(ctx, RJ_E_NO_DATA, "polygons not set");
+    if (res && res->npolys != 0 && res->npolys != ctx->ps->P)
+        return fail(ctx, RJ_E_INVALID, "result sized for %d polygons, polygon set has %d", res->npolys, ctx->ps->P);
     if (q->function_type < RJ_RASTER_JOIN || q->function_type > RJ_RASTER_JOIN_BOUNDS)
         return fail(ctx, RJ_E_UNSUPPORTED, "function type %d not supported", q->function_type);   // GLHandler.cpp:201
     cudaSetDevice(ctx->device);
     int rc;
-    const int P = ctx->P;
+    const int P = ctx->ps->P;
+    if (ctx->cache_owner != ctx->ps || ctx->cache_version != ctx->ps->version) {
+        // the scratch holds another polygon set's grid structures
+        ctx->ps->grid.valid = false;
+        ctx->ps->exact.valid = false;
+        ctx->cache_owner = ctx->ps;
+        ctx->cache_version = ctx->ps->version;
+    }
+    query_rows(ctx, q, ctx->row0, ctx->row1);
     if (q->flags & RJ_FLAG_NO_CACHE) {
-        ctx->grid.valid = false;
-        ctx->exact.valid = false;
-        ctx->overlap_known = -1;
+        ctx->ps->grid.valid = false;
+        ctx->ps->exact.valid = false;
+        ctx->ps->overlap_known = -1;
     }
     g_kernel_launches = 0;
     unsigned long long* oc;
@@ -1244,7 +1234,7 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
     ExecState es{oc, os, ob, &ph};
     const double t_setup = now_ms();
     std::vector<unsigned long long> hc(P), hq(P);
-    std::vector<double> hs(P), hnf(P);
+    std::vector<double> hnf(P);
     std::vector<long long> hb;
     int derr = 0;
     for (int attempt = 0; attempt < 2; ++attempt) {
@@ -1274,8 +1264,8 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
         RJ_CUDA(cudaStreamSynchronize(ctx->stream));
         RJ_CUDA(cudaGetLastError());
         if (!ctx->overlap_pending) break;
-        ctx->overlap_known = (lc[0] != lc[1]) ? 1 : 0;
-        if (!ctx->overlap_known) break;
+        ctx->ps->overlap_known = (lc[0] != lc[1]) ? 1 : 0;
+        if (!ctx->ps->overlap_known) break;
         // overlapping polygons: the label map cannot hold them, redo on the canvas path
         RJ_CUDA(cudaMemsetAsync(oc, 0, P * sizeof(unsigned long long), ctx->stream));
         RJ_CUDA(cudaMemsetAsync(os, 0, P * sizeof(unsigned long long), ctx->stream));
@@ -1285,25 +1275,7 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
     }
     ctx->overlap_pending = nullptr;
     if (derr) return fail(ctx, RJ_E_TIMEOUT, "a bounded device wait ran out (status 0x%x)", derr);
-    for (int i = 0; i < P; ++i) hs[i] = std::ldexp((double)(long long)hq[i], -ctx->sum_shift) + hnf[i];
-    if (res) {
-        if (res->count) for (int i = 0; i < P; ++i) res->count[i] = hc[i];
-        if (res->sum) for (int i = 0; i < P; ++i) res->sum[i] = hs[i];
-        if (res->compat3) {
-            for (int i = 0; i < P; ++i) {
-                // [count | sum/100 | decimal*10], decodable by printResults (main.cpp:206-208)
-                double s = hs[i];
-                double hi = std::trunc(s / 100.0);
-                double lo = std::nearbyint((s - 100.0 * hi) * 10.0);
-                res->compat3[i] = (int32_t)std::min<unsigned long long>(hc[i], 0x7fffffffULL);
-                res->compat3[P + i] = (int32_t)std::max(-2147483647.0, std::min(2147483647.0, hi));
-                res->compat3[2 * P + i] = (int32_t)lo;
-            }
-        }
-        if (res->bounds) {
-            for (size_t i = 0; i < (size_t)4 * P; ++i) res->bounds[i] = hb.empty() ? 0 : (int32_t)std::min<long long>(hb[i], 0x7fffffffLL);
-        }
-    }
+    decode_result(P, hc.data(), hq.data(), hnf.data(), ctx->sum_shift, hb.empty() ? nullptr : hb.data(), res);
     // timings (GLHandler::printTimeStats fields)
     rj_timings& t = ctx->tm;
     std::memset(&t, 0, sizeof t);

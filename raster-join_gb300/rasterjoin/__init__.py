@@ -31,7 +31,10 @@ Location, Uint, Int, Float = 0, 1, 2, 3
 RJ_OK = 0
 STATUS = {0: "RJ_OK", -1: "RJ_E_INVALID", -2: "RJ_E_OOM", -3: "RJ_E_TOO_MANY_CONSTRAINTS",
           -4: "RJ_E_TIMEOUT", -5: "RJ_E_CUDA", -6: "RJ_E_NO_DATA", -7: "RJ_E_UNSUPPORTED",
-          -8: "RJ_E_BUSY"}
+          -8: "RJ_E_BUSY", 1: "RJ_PENDING"}
+RJ_PENDING = 1
+BATCH_AUTOTUNE = 0x1
+BATCH_NO_FUSE = 0x2
 MAX_CONSTRAINTS = 10
 
 FLAG_COMPAT_INDEX_CLAMP = 0x1
@@ -90,6 +93,24 @@ class Timings(C.Structure):
                 ("kernel_launches", C.c_int32)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("nqueries", C.c_int32), ("fused", C.c_int32), ("fallback", C.c_int32), ("segments", C.c_int32),
+                ("items", C.c_uint64), ("rows_read", C.c_uint64), ("point_queries", C.c_uint64),
+                ("total_ms", C.c_double), ("setup_ms", C.c_double), ("poly_ms", C.c_double),
+                ("point_ms", C.c_double), ("reduce_ms", C.c_double), ("threads", C.c_int32),
+                ("rows_per_item", C.c_int32), ("tuned", C.c_int32), ("kernel_launches", C.c_int32)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_int32), ("canvas_mb", C.c_int64), ("max_batch", C.c_int32),
+                ("max_wait_ms", C.c_double)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("submit_ms", C.c_double), ("start_ms", C.c_double), ("done_ms", C.c_double),
+                ("batch_id", C.c_int32), ("batch_size", C.c_int32), ("status", C.c_int32)]
+
+
 _lib = None
 
 
@@ -116,6 +137,17 @@ def load_library(path=LIB_PATH):
         "rj_execute": (C.c_int, [C.c_void_p, P(Query), P(Result)]),
         "rj_get_timings": (C.c_int, [C.c_void_p, P(Timings)]),
         "rj_format_time_stats": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
+        "rj_polyset_create": (C.c_int, [C.c_void_p, P(C.c_float), P(C.c_int32), C.c_int32, P(C.c_double),
+                                        P(C.c_void_p)]),
+        "rj_polyset_destroy": (None, [C.c_void_p]),
+        "rj_use_polyset": (C.c_int, [C.c_void_p, C.c_void_p]),
+        "rj_build_time_index": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+        "rj_execute_batch": (C.c_int, [C.c_void_p, C.c_int32, P(Query), P(C.c_void_p), P(Result), P(C.c_int32),
+                                       C.c_uint32, P(BatchStats)]),
+        "rj_server_create": (C.c_int, [C.c_void_p, P(ServerConfig), P(C.c_void_p)]),
+        "rj_submit": (C.c_int, [C.c_void_p, P(Query), C.c_void_p, P(Result), P(C.c_uint64)]),
+        "rj_poll": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int32, P(RequestInfo)]),
+        "rj_server_destroy": (None, [C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -159,6 +191,94 @@ class JoinResult:
     def avg(self):
         with np.errstate(invalid="ignore", divide="ignore"):
             return np.where(self.count > 0, self.sum / np.maximum(self.count, 1), 0.0)
+
+
+class _ResultBuffers:
+    """Host result arrays of one query and the rj_result pointing at them."""
+
+    def __init__(self, P, bounds=False):
+        self.count = np.zeros(P, np.uint64)
+        self.sum = np.zeros(P, np.float64)
+        self.compat3 = np.zeros(3 * P, np.int32)
+        self.bounds = np.zeros(4 * P, np.int32) if bounds else None
+        self.r = Result(P, self.count.ctypes.data_as(C.POINTER(C.c_uint64)),
+                        self.sum.ctypes.data_as(C.POINTER(C.c_double)),
+                        self.compat3.ctypes.data_as(C.POINTER(C.c_int32)),
+                        self.bounds.ctypes.data_as(C.POINTER(C.c_int32)) if bounds else None)
+
+    def result(self):
+        return JoinResult(self.count, self.sum, self.compat3, self.bounds)
+
+
+class PolySet:
+    """A polygon collection resident on the device (rj_polyset)."""
+
+    def __init__(self, handler, xy, pindex, bbox=None):
+        self.handler = handler
+        self.xy = np.ascontiguousarray(xy, dtype=np.float32).reshape(-1, 2)
+        self.pindex = np.ascontiguousarray(pindex, dtype=np.int32)
+        self.P = len(self.pindex) - 1
+        h = C.c_void_p()
+        bb = None if bbox is None else (C.c_double * 4)(*bbox)
+        handler._check(handler.lib.rj_polyset_create(handler.ctx, self.xy.ctypes.data_as(C.POINTER(C.c_float)),
+                                                     self.pindex.ctypes.data_as(C.POINTER(C.c_int32)), self.P,
+                                                     bb, C.byref(h)))
+        self.ptr = h
+
+    def close(self):
+        if getattr(self, "ptr", None) and getattr(self.handler, "ctx", None):
+            self.handler.lib.rj_polyset_destroy(self.ptr)
+        self.ptr = None
+
+
+class Server:
+    """Request loop over the handler's resident table (rj_server_*).
+
+    submit(query, polyset) -> ticket; poll(ticket, timeout_ms) -> (JoinResult,
+    info dict) or None while pending."""
+
+    def __init__(self, handler, slots=0, canvas_mb=0, max_batch=0, max_wait_ms=0.0):
+        self.handler = handler
+        self.lib = handler.lib
+        cfg = ServerConfig(slots, canvas_mb, max_batch, max_wait_ms)
+        h = C.c_void_p()
+        handler._check(self.lib.rj_server_create(handler.ctx, C.byref(cfg), C.byref(h)))
+        self.ptr = h
+        self._pending = {}
+
+    def submit(self, query, polyset=None):
+        P = polyset.P if polyset is not None else len(self.handler.dataHandler.polys[1]) - 1
+        buf = _ResultBuffers(P)
+        t = C.c_uint64()
+        q = Query()
+        C.pointer(q)[0] = query
+        rc = self.lib.rj_submit(self.ptr, C.byref(q), polyset.ptr if polyset is not None else None,
+                                C.byref(buf.r), C.byref(t))
+        if rc != RJ_OK:
+            raise RJError(rc, "rj_submit failed")
+        self._pending[t.value] = (buf, q)
+        return t.value
+
+    def poll(self, ticket, timeout_ms=-1):
+        info = RequestInfo()
+        rc = self.lib.rj_poll(self.ptr, ticket, timeout_ms, C.byref(info))
+        if rc == RJ_PENDING:
+            return None
+        buf, _ = self._pending.pop(ticket)
+        if rc != RJ_OK:
+            raise RJError(rc, "request %d failed" % ticket)
+        return buf.result(), {f: getattr(info, f) for f, _ in RequestInfo._fields_}
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            self.lib.rj_server_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class DataHandler:
@@ -235,6 +355,7 @@ class GLHandler:
         self._loaded_polys = None
         self.bounds = None
         self.last = None
+        self._bound = None               # PolySet bound by usePolySet
 
     @classmethod
     def getInstance(cls, gpuMemMB=2048, inMemory=True):
@@ -302,6 +423,7 @@ class GLHandler:
                                                  pidx.ctypes.data_as(C.POINTER(C.c_int32)), len(pidx) - 1,
                                                  bb))
             self._loaded_polys = pkey
+            self._bound = None
 
     def make_query(self, fn):
         dh = self.dataHandler
@@ -330,7 +452,7 @@ class GLHandler:
         """Run one join; returns JoinResult with exact arrays."""
         self.upload()
         q = query if query is not None else self.make_query(fn)
-        P = len(self.dataHandler.polys[1]) - 1
+        P = self._bound.P if self._bound is not None else len(self.dataHandler.polys[1]) - 1
         count = np.zeros(P, np.uint64)
         sum_ = np.zeros(P, np.float64)
         compat3 = np.zeros(3 * P, np.int32)
@@ -351,6 +473,46 @@ class GLHandler:
         if fn == RasterJoinBoundFn and self.bounds is not None:
             return self.bounds
         return np.zeros(0, np.int32)
+
+    # ---- polygon sets, time index, batches ----
+    def polyset(self, xy, pindex, bbox=None):
+        return PolySet(self, xy, pindex, bbox)
+
+    def usePolySet(self, ps):
+        self.upload()
+        self._check(self.lib.rj_use_polyset(self.ctx, ps.ptr if ps is not None else None))
+        self._bound = ps
+
+    def buildTimeIndex(self, attrib_id, nbuckets=0):
+        self.upload()
+        self._check(self.lib.rj_build_time_index(self.ctx, attrib_id, nbuckets))
+
+    def execute_batch(self, queries, polysets, flags=0, raise_on_error=True):
+        """Run queries[i] on polysets[i] (None: the handler's polygons) in one
+        batch; returns (list of JoinResult, status array, stats dict)."""
+        n = len(queries)
+        qa = (Query * max(n, 1))()
+        for i, q in enumerate(queries):
+            qa[i] = q
+        sa = (C.c_void_p * max(n, 1))()
+        bufs = []
+        for i, ps in enumerate(polysets):
+            sa[i] = ps.ptr if ps is not None else None
+            P = ps.P if ps is not None else len(self.dataHandler.polys[1]) - 1
+            bufs.append(_ResultBuffers(P))
+        ra = (Result * max(n, 1))()
+        for i, b in enumerate(bufs):
+            ra[i] = b.r
+        st = (C.c_int32 * max(n, 1))()
+        stats = BatchStats()
+        rc = self.lib.rj_execute_batch(self.ctx, n, qa, sa, ra, st, flags, C.byref(stats))
+        if rc != RJ_OK and raise_on_error:
+            self._check(rc)
+        return ([b.result() for b in bufs], np.array(st[:n], np.int32),
+                {f: getattr(stats, f) for f, _ in BatchStats._fields_})
+
+    def server(self, **kw):
+        return Server(self, **kw)
 
     def timings(self):
         t = Timings()

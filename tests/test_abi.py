@@ -43,8 +43,10 @@ def test_struct_layouts_match_binding(tmp_path):
 #include <stddef.h>
 #include "rj.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(rj_constraint), sizeof(rj_query), sizeof(rj_result),
-         sizeof(rj_config), sizeof(rj_column), sizeof(rj_timings), offsetof(rj_query, flags));
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(rj_constraint), sizeof(rj_query), sizeof(rj_result),
+         sizeof(rj_config), sizeof(rj_column), sizeof(rj_timings), offsetof(rj_query, flags),
+         sizeof(rj_batch_stats), sizeof(rj_server_config), sizeof(rj_request_info),
+         offsetof(rj_batch_stats, kernel_launches));
   return 0;
 }
 ''')
@@ -58,6 +60,10 @@ int main(void) {
     assert vals[4] == C.sizeof(rj.Column)
     assert vals[5] == C.sizeof(rj.Timings)
     assert vals[6] == rj.Query.flags.offset
+    assert vals[7] == C.sizeof(rj.BatchStats)
+    assert vals[8] == C.sizeof(rj.ServerConfig)
+    assert vals[9] == C.sizeof(rj.RequestInfo)
+    assert vals[10] == rj.BatchStats.kernel_launches.offset
 
 
 def test_query_defaults(built):
@@ -88,5 +94,9 @@ def test_create_without_gpu_returns_status(built):
     # calls on a null context are rejected, not crashing
     assert lib.rj_execute(None, None, None) == -1
     assert lib.rj_set_polygons(None, None, None, 0, None) == -1
+    assert lib.rj_execute_batch(None, 0, None, None, None, None, 0, None) == -1
+    assert lib.rj_build_time_index(None, 0, 0) == -1
+    assert lib.rj_submit(None, None, None, None, None) == -1
+    assert lib.rj_poll(None, 0, 0, None) == -1
     with pytest.raises(rj.RJError):
         rj.GLHandler()
