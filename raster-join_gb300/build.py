@@ -50,8 +50,28 @@ def _stamp():
     return h.hexdigest()
 
 
+CPP = os.path.join(HERE, "cpp")
+CLI = os.path.join(LIBDIR, "rj_cli")
+
+
+def build_cli(force=False):
+    """The command-line driver (cpp/rj_cli.cpp, host C++ only) against librj.so."""
+    src = os.path.join(CPP, "rj_cli.cpp")
+    hdrs = [os.path.join(CPP, "rasterjoin.hpp"), os.path.join(HERE, "..", "include", "rj.h")]
+    newest = max(os.path.getmtime(f) for f in [src, LIB] + hdrs)
+    if not force and os.path.exists(CLI) and os.path.getmtime(CLI) >= newest:
+        return CLI
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-I", os.path.join(HERE, "..", "include"), src, "-o", CLI + ".tmp",
+           "-L", LIBDIR, "-lrj", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("rj_cli build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(CLI + ".tmp", CLI)
+    return CLI
+
+
 def build(force=False, verbose=False):
-    """Compile and link librj.so; returns its path."""
+    """Compile and link librj.so (and the CLI); returns the library path."""
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     stamp_file = os.path.join(OBJ, "stamp")
@@ -59,6 +79,7 @@ def build(force=False, verbose=False):
     if not force and os.path.exists(LIB) and os.path.exists(stamp_file):
         with open(stamp_file) as fh:
             if fh.read().strip() == stamp:
+                build_cli()
                 return LIB
     nvcc = _nvcc()
 
@@ -82,6 +103,7 @@ def build(force=False, verbose=False):
     os.replace(tmp, LIB)
     with open(stamp_file, "w") as fh:
         fh.write(stamp)
+    build_cli(force=True)
     return LIB
 
 
