@@ -47,6 +47,13 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--count-only", action="store_true", help="count instead of avg(a) (diagnostic)")
+    ap.add_argument("--table-points", type=int, default=1_000_000_000,
+                    help="resident table of the batched and served runs")
+    ap.add_argument("--batch-queries", type=int, default=512)
+    ap.add_argument("--served-requests", type=int, default=2000)
+    ap.add_argument("--served-qps", type=float, default=500.0)
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
     return ap.parse_args()
 
 
@@ -201,6 +208,156 @@ def run_reference(args):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+
+# ---------------------------------------------------------------------------
+# Batched and served configurations over one resident table generated on the
+# device (1B points: x, y, t, a), reordered into time buckets.
+def resident_table(rj, torch, n, seed, stream):
+    from rasterjoin import workloads as W
+    tab = W.device_table(n, seed)
+    torch.cuda.synchronize()
+    # rows per second of the year (exact row counts of any time window)
+    secs = torch.bincount((tab["t"].to(torch.int64) - W.T0), minlength=W.YEAR)
+    cum = torch.zeros(W.YEAR + 1, dtype=torch.int64, device="cuda")
+    cum[1:] = torch.cumsum(secs, 0)
+    cum = cum.cpu().numpy()
+    del secs
+    h = rj.GLHandler(stream=stream.cuda_stream)
+    h.attachDevice([(1, rj.Location, tab["xy"].data_ptr()), (2, rj.Uint, tab["t"].data_ptr()),
+                    (3, rj.Float, tab["a"].data_ptr())], n, 1)
+    h.buildTimeIndex(2)            # copies the table into bucket order
+    del tab
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return h, cum
+
+
+def window_rows(cum, t0, t1):
+    from rasterjoin.synth import T0
+    a = max(0, t0 - T0)
+    b = min(len(cum) - 1, t1 - T0 + 1)
+    return int(cum[b] - cum[a]) if b > a else 0
+
+
+def make_raster_query(rj, cell, window, avg):
+    q = rj.default_query()
+    q.function_type = rj.RasterJoinFn
+    q.cell_size = cell
+    q.time_attrib, q.t_start, q.t_end = 2, int(window[0]), int(window[1])
+    if avg:
+        q.aggregation, q.aggr_attrib = rj.Avg, 3
+    return q
+
+
+def run_batched(rj, h, cum, n, nq):
+    from rasterjoin import workloads as W
+    work = W.batched_queries(nq, n)
+    sets = [h.polyset(xy, p) for xy, p, _, _, _ in work]
+    qs = [make_raster_query(rj, cell, win, avg) for _, _, cell, win, avg in work]
+    pq = sum(window_rows(cum, *win) for _, _, _, win, _ in work)
+    # warm-up: overlap checks of the new polygon sets and the block-shape tuner
+    h.execute_batch(qs, sets, flags=rj.BATCH_AUTOTUNE)
+    fused_ms, stats = [], None
+    for _ in range(3):
+        t0 = time.perf_counter()
+        res, status, stats = h.execute_batch(qs, sets)
+        fused_ms.append((time.perf_counter() - t0) * 1e3)
+    plain_ms = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        res2, status2, stats2 = h.execute_batch(qs, sets, flags=rj.BATCH_NO_FUSE)
+        plain_ms.append((time.perf_counter() - t0) * 1e3)
+    same = all(np.array_equal(a.count, b.count) and np.array_equal(a.sum, b.sum) for a, b in zip(res, res2))
+    for s in sets:
+        s.close()
+    f, pl = float(np.median(fused_ms)), float(np.median(plain_ms))
+    return {
+        "workload": "%d raster queries over a %d-point resident table; per query 1-5000 star polygons "
+                    "(4-2000 vertices), eps log-uniform 1-1000 m, time window of 1e4-5e8 points, "
+                    "count or avg" % (nq, n),
+        "point_queries": pq, "fused_ms": f, "plain_ms": pl,
+        "fused_gpoints_s": pq / f / 1e6, "plain_gpoints_s": pq / pl / 1e6, "speedup": pl / f,
+        "rows_read": stats["rows_read"], "segments": stats["segments"], "point_pass_ms": stats["point_ms"],
+        "polygon_side_ms": stats["poly_ms"], "canvas_reduce_ms": stats["reduce_ms"],
+        "shape": [stats["threads"], stats["rows_per_item"]], "kernel_launches": stats["kernel_launches"],
+        "status_ok": bool((status == 0).all() and (status2 == 0).all()), "same_result": bool(same),
+        "plain": "each query through rj_execute in turn (one query per launch sequence)",
+    }
+
+
+def run_served(rj, h, cum, n, nreq, qps):
+    from rasterjoin import workloads as W
+    reqs = W.served_requests(nreq, qps)
+    rows = [window_rows(cum, *r[4]) for r in reqs]
+    qs = [make_raster_query(rj, cell, win, False) for _, _, _, cell, win in reqs]
+    # ---- plain: one request at a time through rj_execute, FIFO
+    service = []
+    for (arr, xy, p, cell, win), q in zip(reqs, qs):
+        t0 = time.perf_counter()
+        ps = h.polyset(xy, p)
+        h.usePolySet(ps)
+        h.execute(rj.RasterJoinFn, query=q)
+        service.append(time.perf_counter() - t0)
+        h.usePolySet(None)
+        ps.close()
+    arrivals = np.array([r[0] for r in reqs])
+    done = np.zeros(nreq)
+    free_at = 0.0
+    for i in range(nreq):
+        start = max(arrivals[i], free_at)
+        done[i] = start + service[i]
+        free_at = done[i]
+    plain_lat = (done - arrivals) * 1e3
+    # ---- served: requests submitted at their arrival times
+    srv = h.server(slots=2, canvas_mb=16384, max_batch=64)
+    tickets = [None] * nreq
+    arrive_ms = np.zeros(nreq)
+    live = []
+
+    def submitter():
+        base = time.monotonic()
+        for i, ((arr, xy, p, cell, win), q) in enumerate(zip(reqs, qs)):
+            now = time.monotonic() - base
+            if arr > now:
+                time.sleep(arr - now)
+            arrive_ms[i] = time.monotonic() * 1e3
+            ps = h.polyset(xy, p)            # the request's polygons go to the device on arrival
+            live.append(ps)
+            tickets[i] = srv.submit(q, ps)
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    lat, sizes, last_done = [], [], 0.0
+    for i in range(nreq):
+        while tickets[i] is None:
+            time.sleep(0.0002)
+        r, info = srv.poll(tickets[i], -1)
+        lat.append(info["done_ms"] - arrive_ms[i])
+        sizes.append(info["batch_size"])
+        last_done = max(last_done, info["done_ms"])
+    th.join()
+    srv.close()
+    for ps in live:
+        ps.close()
+    span_s = (last_done - arrive_ms[0]) / 1e3
+    lat = np.array(lat)
+    pct = lambda a, q: float(np.percentile(a, q))
+    return {
+        "workload": "Poisson arrivals at %g qps, %d requests over a %d-point resident table; per request "
+                    "1-50 star polygons (8-300 vertices, radius 200 m-10 km), eps in {1,10,100,1000} m, "
+                    "time window 1 h-30 days, count" % (qps, nreq, n),
+        "p50_ms": pct(lat, 50), "p95_ms": pct(lat, 95), "p99_ms": pct(lat, 99),
+        "achieved_qps": nreq / span_s, "gpoints_s": sum(rows) / span_s / 1e9,
+        "mean_batch": float(np.mean(sizes)),
+        "plain": {"p50_ms": pct(plain_lat, 50), "p95_ms": pct(plain_lat, 95), "p99_ms": pct(plain_lat, 99),
+                  "mean_service_ms": float(np.mean(service)) * 1e3,
+                  "max_qps": 1.0 / float(np.mean(service)),
+                  "method": "each request alone through rj_execute (polygons uploaded, join, results read); "
+                            "latency from a FIFO queue over the same arrival times"},
+        "latency": "arrival (before the polygon upload) to results in host memory",
+    }
 
 
 # ---------------------------------------------------------------------------
@@ -363,9 +520,17 @@ def run_gb300(args):
                                 "sample": "CPUJoin restatement (grid 1024 build %.2fs + join %.2fs) over the first "
                                           "%d points of the same table, config-2 filters and avg as a labelled "
                                           "extension" % (tb, tj, s_n)}
+    h.close()
+    if rank == 0 and world == 1 and not (args.no_batched and args.no_served):
+        stream2 = torch.cuda.Stream()
+        h2, cum = resident_table(rj, torch, args.table_points, 20261206, stream2)
+        if not args.no_batched:
+            line["batched"] = run_batched(rj, h2, cum, args.table_points, args.batch_queries)
+        if not args.no_served:
+            line["served"] = run_served(rj, h2, cum, args.table_points, args.served_requests, args.served_qps)
+        h2.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
-    h.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0

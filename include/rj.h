@@ -198,6 +198,15 @@ RJ_API int rj_load_points(rj_ctx *ctx, const rj_column *cols, int32_t ncols,
  * caller keeps alive; nothing is copied */
 RJ_API int rj_attach_points_device(rj_ctx *ctx, const rj_column *cols, int32_t ncols,
                             uint64_t npoints, int32_t loc_attrib);
+/* Out-of-core table: the data pointers are HOST pointers that the caller
+ * keeps alive; nothing is copied at load.  Every query streams the columns
+ * it reads through the device in chunks of chunk_points rows (0: sized from
+ * the memory budget), copying chunk k+1 while chunk k is processed (the
+ * reference's memory passes, GLFunction.cpp:330-337, RasterJoin.cpp:215-236;
+ * rj_timings.no_pt_passes counts the chunks).  Pinned host memory lets the
+ * copies overlap the point pass.  Batches run such a table query by query. */
+RJ_API int rj_attach_points_host(rj_ctx *ctx, const rj_column *cols, int32_t ncols,
+                                 uint64_t npoints, int32_t loc_attrib, uint64_t chunk_points);
 RJ_API int rj_free_points(rj_ctx *ctx);
 
 /* ---- polygons: PolyHandler::addPolygonCollection (PolyHandler.cpp:49-80).

@@ -48,6 +48,10 @@ struct Arena {
 
 size_t al256(size_t b) { return (std::max<size_t>(b, 1) + 255) & ~size_t(255); }
 
+// per-block shared histogram entries of the fused point pass (polygons of a
+// label-map query, or pixels of a small splat canvas)
+constexpr int kBatchHistCap = 4096;
+
 struct Engine {
     rj_ctx* ctx = nullptr;
     cudaStream_t st = nullptr;
@@ -116,6 +120,7 @@ struct QPlan {
     int T = 1;
     size_t npix = 0;
     bool check_overlap = false;
+    uint64_t canvas = 0;         // canvas geometry (overlap status is per canvas)
     size_t out_off = 0;          // first polygon of the query in the output block
     uint16_t* label = nullptr;
     uint32_t* cc = nullptr;
@@ -133,7 +138,7 @@ size_t canvas_bytes(const QPlan& p) {
 // plans report errors through the context).
 void plan_query(rj_ctx* ctx, QPlan& p, bool no_fuse) {
     const rj_query* q = p.q;
-    if (no_fuse || q->function_type != RJ_RASTER_JOIN) return;   // plain path
+    if (no_fuse || q->function_type != RJ_RASTER_JOIN || ctx->streamed) return;   // plain path
     int rc = plan_raster_bbox(ctx, p.ps->bbox, q, p.rp);
     if (rc) { p.status = rc; return; }
     bool empty = false;
@@ -150,7 +155,8 @@ void plan_query(rj_ctx* ctx, QPlan& p, bool no_fuse) {
         return;
     }
     const bool label_ok = !(q->flags & RJ_FLAG_FORCE_CANVAS) && p.ps->P <= kMaxLabelPolys;
-    const int known = (q->flags & RJ_FLAG_NO_CACHE) ? -1 : p.ps->overlap_known;
+    p.canvas = canvas_key(p.rp.colxf, p.rp.rowxf, p.rp.resx, p.rp.resy);
+    const int known = p.ps->overlap_on(p.canvas);
     p.mode = (label_ok && known != 1) ? BQ_LABEL : BQ_SPLAT;
     p.check_overlap = p.mode == BQ_LABEL && known != 0;
 }
@@ -286,7 +292,7 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
         if (avail == 0) {
             size_t fr = 0, tot = 0;
             cudaMemGetInfo(&fr, &tot);
-            avail = (size_t)(0.85 * (double)(fr + e.ar.buf.bytes));
+            avail = (size_t)(0.5 * (double)(fr + e.ar.buf.bytes));
             if (ctx->budget > 0) avail = std::min<size_t>(avail, (size_t)std::max<int64_t>(ctx->budget - (int64_t)ctx->used + (int64_t)e.ar.buf.bytes, 0));
         }
         for (; next < todo.size(); ++next) {
@@ -389,7 +395,7 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
                 const bool overlap = hl[2 * i] != hl[2 * i + 1];
                 {
                     std::lock_guard<std::recursive_mutex> lock(ctx->mu);
-                    p->ps->overlap_known = overlap ? 1 : 0;
+                    p->ps->overlap[p->canvas] = overlap ? 1 : 0;
                 }
                 if (!overlap) continue;
                 p->mode = BQ_SPLAT;
@@ -457,11 +463,21 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
             d.label = p->label;
             d.canvas_c = p->cc;
             d.canvas_s = p->cs;
-            if (p->mode == BQ_LABEL && d.P <= 4096) max_hist = std::max(max_hist, d.P);
+            if (p->mode == BQ_LABEL && d.P <= kBatchHistCap) max_hist = std::max(max_hist, d.P);
+            if (p->mode == BQ_SPLAT && p->T == 1 && p->npix <= (size_t)kBatchHistCap) {
+                // small canvas: splat into the block's shared histogram (indexed by
+                // pixel) and flush into the canvas
+                d.P = (int)p->npix;
+                d.out_count = nullptr;
+                d.out_count32 = p->cc;
+                d.out_sum = reinterpret_cast<unsigned long long*>(p->cs);
+                max_hist = std::max(max_hist, d.P);
+            }
             act.push_back(p);
         }
         const int hist_cap = (max_hist + 1) & ~1;
-        for (size_t i = 0; i < nw; ++i) hq[i].hist_smem = (hq[i].mode == BQ_LABEL && hq[i].P <= hist_cap) ? 1 : 0;
+        for (size_t i = 0; i < nw; ++i)
+            hq[i].hist_smem = (hq[i].mode == BQ_LABEL || hq[i].out_count32) && hq[i].P <= hist_cap ? 1 : 0;
         ba.nu = (int)ucols.size();
         for (int u = 0; u < ba.nu; ++u) {
             ba.ucol[u] = ucols[u];
@@ -818,6 +834,7 @@ int rj_build_time_index(rj_ctx* ctx, int32_t attrib, int32_t nbuckets) {
     ctx->err.clear();
     if (ctx->server_running) return fail(ctx, RJ_E_BUSY, "a serving loop owns the context");
     if (ctx->cols.empty()) return fail(ctx, RJ_E_NO_DATA, "point table not loaded");
+    if (ctx->streamed) return fail(ctx, RJ_E_UNSUPPORTED, "a streamed (host-resident) table has no time index");
     const Column* tc = find_col(ctx, attrib);
     if (!tc || tc->type != RJ_UINT) return fail(ctx, RJ_E_INVALID, "time attribute %d is not a loaded uint column", attrib);
     const int nb = nbuckets > 0 ? nbuckets : 16384;
@@ -931,6 +948,8 @@ int rj_execute_batch(rj_ctx* ctx, int32_t nq, const rj_query* q, rj_polyset* con
         }
     }
     int rc = execute_batch(*e, nq, q, nullptr, sets, res, nullptr, status, flags, stats);
+    // a large arena (label maps / canvases of a big batch) is not kept between calls
+    if (e->ar.buf.bytes > ((size_t)1 << 30)) dev_free(ctx, e->ar.buf);
     return rc;
 }
 

@@ -83,16 +83,30 @@ __device__ __forceinline__ void batch_query(const BatchArgs& a, const BatchQuery
             for (int k = 0; k < 4; ++k) m.consume(ok[k], key[k], x[k], y[k], v[k], h, dq);
         }
     } else {
-        const SplatMapper m{cx, Q->canvas_c, Q->canvas_s, Q->sum_scale, Q->out_nonfinite};
-        for (int r = tid; r < nrows; r += BLOCK) {
-            const float2 p = s_xy[r];
-            bool ok = true;
+        const SplatMapper m{cx, Q->canvas_c, Q->canvas_s, Q->sum_scale, Q->out_nonfinite, SMEM ? 1 : 0};
+        for (int base = 0; base < nrows; base += 4 * BLOCK) {
+            float x[4], y[4], v[4];
+            bool ok[4];
+            SplatMapper::Key key[4];
             #pragma unroll
-            for (int u = 0; u < kBatchMaxCols; ++u)
-                if (u < a.nu) ok = ok && (order_key(a.utyp[u], s_col[u * a.rows + r]) - lo[u] <= span[u]);
-            if (!ok) continue;
-            const float v = AGG ? agg_value(aggr_typ, s_col[aggr_u * a.rows + r]) : 0.f;
-            m.map(p.x, p.y, v, h, dq);
+            for (int k = 0; k < 4; ++k) {
+                const int r = base + k * BLOCK + tid;
+                ok[k] = r < nrows;
+                x[k] = y[k] = v[k] = 0.f;
+                key[k] = SplatMapper::kNone;
+                if (ok[k]) {
+                    const float2 p = s_xy[r];
+                    x[k] = p.x;
+                    y[k] = p.y;
+                    #pragma unroll
+                    for (int u = 0; u < kBatchMaxCols; ++u)
+                        if (u < a.nu) ok[k] = ok[k] && (order_key(a.utyp[u], s_col[u * a.rows + r]) - lo[u] <= span[u]);
+                    if (AGG && ok[k]) v[k] = agg_value(aggr_typ, s_col[aggr_u * a.rows + r]);
+                    if (ok[k]) key[k] = m.lookup(x[k], y[k]);
+                }
+            }
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) m.consume(ok[k], key[k], x[k], y[k], v[k], h, dq);
         }
     }
     if (SMEM) {
@@ -100,7 +114,8 @@ __device__ __forceinline__ void batch_query(const BatchArgs& a, const BatchQuery
         for (int b = tid; b < P; b += BLOCK) {
             const uint32_t c = s_cnt[b];
             if (c) {
-                atomicAdd(Q->out_count + b, (unsigned long long)c);
+                if (Q->out_count32) atomicAdd(Q->out_count32 + b, c);   // private splat canvas
+                else atomicAdd(Q->out_count + b, (unsigned long long)c);
                 if (AGG) atomicAdd(Q->out_sum + b, s_sum[b]);
             }
         }

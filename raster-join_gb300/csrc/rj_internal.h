@@ -23,7 +23,7 @@ struct DevBuf {
 struct Column {
     int attrib = -1;
     int type = RJ_FLOAT;
-    void* d = nullptr;
+    void* d = nullptr;           // device data, or host data of a streamed table
     bool owned = false;
     float absmax = 0.f;     // largest finite |aggregate value| (sizes the fixed-point sums)
 };
@@ -55,7 +55,14 @@ struct PolySet {
     float max_abs_coord = 0.f, max_edge_dx = 0.f, max_edge_dy = 0.f;
     DevBuf d_verts, d_pindex, d_edge_poly;
     uint64_t version = 0;
-    int overlap_known = -1;   // -1 unknown, 0 no two polygons share a pixel centre, 1 some do
+    // Whether two polygons share a pixel centre, per canvas geometry (a set
+    // whose coverage is disjoint on one canvas can overlap on a finer one):
+    // absent = unknown, 0 = disjoint, 1 = overlapping.
+    std::map<uint64_t, int> overlap;
+    int overlap_on(uint64_t canvas) const {
+        auto it = overlap.find(canvas);
+        return it == overlap.end() ? -1 : it->second;
+    }
     GridCache grid;
     ExactCache exact;
 };
@@ -100,6 +107,14 @@ struct rj_ctx {
     int loc_attrib = -1;
     std::vector<rjh::Column> cols;
     rjh::TimeIndex tix;
+    // streamed (host-resident) table: chunks of `chunk` rows copied per query
+    bool streamed = false;
+    uint64_t chunk = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copied[2]{}, consumed[2]{}, copy_t0{}, copy_t1{};
+    rjh::DevBuf sbuf[2];
+    int passes = 1;                  // point passes of the last query
+    double copy_ms = 0;              // host->device copy time of the last query
 
     // polygon set bound for rj_execute: the context's own (rj_set_polygons)
     // or a caller's rj_polyset (rj_use_polyset)
@@ -115,7 +130,6 @@ struct rj_ctx {
     int* d_err = nullptr;     // device status word of bounded waits
     int sum_shift = 0;        // fixed-point scale 2^s of the current query's sums
     uint64_t row0 = 0, row1 = ~0ULL;   // rows of the current query (time index window)
-    unsigned long long* overlap_pending = nullptr;   // label-map counters to check after the call
     int server_running = 0;   // a serving loop owns the context
     void* batch_engine = nullptr;   // executor of rj_execute_batch
 };
@@ -152,6 +166,8 @@ struct RasterPlan {
     std::vector<float4> colxf, rowxf;
 };
 int plan_raster_bbox(rj_ctx* ctx, const double* bbox, const rj_query* q, RasterPlan& rp);
+// identity of a canvas geometry (tiles, resolution, per-tile transforms)
+uint64_t canvas_key(const std::vector<float4>& colxf, const std::vector<float4>& rowxf, int resx, int resy);
 int build_filter(rj_ctx* ctx, const rj_query* q, rj::DevFilter& f, bool force_count, bool* empty);
 int load_polyset(rj_ctx* ctx, PolySet& s, const float* xy, const int32_t* pindex, int32_t npolys,
                  const double* bbox);

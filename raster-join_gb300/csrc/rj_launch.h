@@ -113,6 +113,7 @@ struct PointArgs {
     unsigned long long* out_sum; // fixed-point sums (int64 two's complement)
     double* out_nonfinite;       // fp64 sums of the non-finite aggregate values
     int* err;                    // bit0: a bounded pipeline wait ran out
+    uint32_t* out_count32;       // when set, the shared histogram flushes counts here (a u32 canvas)
 };
 
 // Exact point-in-polygon index (CSR over a uniform grid).
@@ -198,6 +199,7 @@ struct BatchQuery {
     unsigned long long* out_count;        // [P]
     unsigned long long* out_sum;          // [P] fixed-point
     double* out_nonfinite;                // [P]
+    uint32_t* out_count32;                // private splat: counts flushed into the u32 canvas
 };
 
 struct BatchSeg {

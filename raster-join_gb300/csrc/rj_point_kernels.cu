@@ -26,6 +26,8 @@
 namespace rj {
 
 constexpr int kPointThreads = 512;
+// canvases up to this many pixels are splatted into a per-block shared copy
+constexpr int kSplatPrivPixels = 8192;
 // deferred-point queue: < kPointThreads left over + 4 per thread per iteration
 constexpr int kQueueCap = kPointThreads * 5;
 
@@ -367,7 +369,10 @@ k_points_pipe(PointArgs pa, M mp, int stages) {
         named_sync(1, kPipeConsumers);
         for (int b = tid; b < pa.P; b += kPipeConsumers) {
             uint32_t c = s_cnt[b];
-            if (c) atomicAdd(pa.out_count + b, (unsigned long long)c);
+            if (c) {
+                if (pa.out_count32) atomicAdd(pa.out_count32 + b, c);
+                else atomicAdd(pa.out_count + b, (unsigned long long)c);
+            }
             if (AGG) {
                 unsigned long long sv = s_sum[b];
                 if (c) atomicAdd(pa.out_sum + b, sv);
@@ -485,7 +490,10 @@ k_points(PointArgs pa, M mp) {
         __syncthreads();
         for (int b = threadIdx.x; b < pa.P; b += BLOCK) {
             uint32_t c = s_cnt[b];
-            if (c) atomicAdd(pa.out_count + b, (unsigned long long)c);
+            if (c) {
+                if (pa.out_count32) atomicAdd(pa.out_count32 + b, c);
+                else atomicAdd(pa.out_count + b, (unsigned long long)c);
+            }
             if (AGG) {
                 unsigned long long sv = s_sum[b];
                 if (c) atomicAdd(pa.out_sum + b, sv);
@@ -589,9 +597,21 @@ static void launch_points(const PointArgs& pa, const M& mp, int sms, cudaStream_
 
 void launch_raster_splat(const PointArgs& pa, const CanvasXf& cx, uint32_t* canvas_c, long long* canvas_s,
                          int sms, cudaStream_t st) {
-    SplatMapper m{cx, canvas_c, canvas_s, pa.f.sum_scale, pa.out_nonfinite};
-    // the splat writes the canvas directly: no per-polygon histogram
+    const size_t npix = (size_t)cx.resx * cx.resy;
     PointArgs p2 = pa;
+    if (cx.splitx == 1 && cx.splity == 1 && npix <= (size_t)kSplatPrivPixels) {
+        // small canvas: per-block private canvas in shared memory, flushed once
+        SplatMapper m{cx, canvas_c, canvas_s, pa.f.sum_scale, pa.out_nonfinite, 1};
+        p2.P = (int)npix;
+        p2.out_count = nullptr;
+        p2.out_count32 = canvas_c;
+        p2.out_sum = reinterpret_cast<unsigned long long*>(canvas_s);
+        if (pa.f.aggr) launch_points_t<SplatMapper, true, true>(p2, m, sms, st);
+        else launch_points_t<SplatMapper, false, true>(p2, m, sms, st);
+        return;
+    }
+    // the splat writes the canvas directly: no per-polygon histogram
+    SplatMapper m{cx, canvas_c, canvas_s, pa.f.sum_scale, pa.out_nonfinite, 0};
     p2.P = 0;
     if (pa.f.aggr) launch_points_t<SplatMapper, true, false>(p2, m, sms, st);
     else launch_points_t<SplatMapper, false, false>(p2, m, sms, st);

@@ -7,6 +7,25 @@
 
 namespace rj {
 
+// Sum of a 64-bit value over the lanes of `peers` (a __match_any_sync group
+// inside `active`); the result is meaningful at the group's lowest lane.
+__device__ __forceinline__ long long group_sum(unsigned active, unsigned peers, long long q) {
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    long long sum = q;
+    unsigned rest = (lane == leader) ? (peers & (peers - 1u)) : 0u;
+    while (__any_sync(active, rest != 0u)) {
+        const int src = rest ? __ffs(rest) - 1 : lane;
+        const long long o = __shfl_sync(active, q, src);
+        if (rest) {
+            sum += o;
+            rest &= rest - 1u;
+        }
+    }
+    return sum;
+}
+
+
 // ---------------------------------------------------------------------------
 template <bool AGG, bool SMEM>
 struct Hist {
@@ -42,19 +61,7 @@ struct Hist {
         const unsigned peers = __match_any_sync(active, p);
         const int leader = __ffs(peers) - 1;
         long long sum = 0;
-        if (AGG) {
-            const long long q = fixq(p, v);
-            sum = q;
-            unsigned rest = (lane == leader) ? (peers & (peers - 1u)) : 0u;
-            while (__any_sync(active, rest != 0u)) {
-                const int src = rest ? __ffs(rest) - 1 : lane;
-                const long long o = __shfl_sync(active, q, src);
-                if (rest) {
-                    sum += o;
-                    rest &= rest - 1u;
-                }
-            }
-        }
+        if (AGG) sum = group_sum(active, peers, fixq(p, v));
         if (lane == leader) {
             const unsigned c = (unsigned)__popc(peers);
             if (SMEM) {
@@ -128,14 +135,56 @@ struct DeferQ {
 };
 
 // ---------------------------------------------------------------------------
+// Additive splat of points into a canvas (point count u32 and fixed-point
+// sum per pixel).  Single-tile canvases: the pixel is looked up first, lanes
+// of a warp on the same pixel are merged, and the group's leader adds once;
+// with `priv` the adds go to the block's shared histogram, indexed by pixel,
+// which the kernel flushes into the canvas (small canvases, where global
+// atomics on a few thousand pixels would serialise).  Multi-tile canvases:
+// one add per tile whose window holds the point.
 struct SplatMapper {
     static constexpr bool kDefer = false;
-    static constexpr bool kTwoPhase = false;
+    static constexpr bool kTwoPhase = true;
     CanvasXf cx;
     uint32_t* canvas_c;
     long long* canvas_s;    // fixed-point sums (non-finite values are not representable on a canvas)
     float scale;
     double* nonfinite;
+    int priv;
+    using Key = uint32_t;
+    static constexpr Key kNone = 0xFFFFFFFFu;
+    static constexpr Key kMulti = 0xFFFFFFFEu;
+    __device__ __forceinline__ Key lookup(float x, float y) const {
+        if (cx.splitx != 1 || cx.splity != 1) return kMulti;
+        float wx = win_coord(x, cx.col0.x, cx.col0.y, cx.col0.z);
+        float wy = win_coord(y, cx.row0.x, cx.row0.y, cx.row0.z);
+        if (!(wx > -1.0f && wx < (float)cx.resx + 1.0f && wy > -1.0f && wy < (float)cx.resy + 1.0f)) return kNone;
+        int px = pix_of(snap_win(wx)), py = pix_of(snap_win(wy));
+        if (px < 0 || px >= cx.resx || py < 0 || py >= cx.resy) return kNone;
+        return (Key)py * (Key)cx.resx + (Key)px;
+    }
+    template <class H>
+    __device__ __forceinline__ void consume(bool valid, Key k, float x, float y, float v, const H& h,
+                                            const DeferQ& dq) const {
+        const bool one = valid && k < kMulti;
+        const unsigned active = __ballot_sync(0xffffffffu, one);
+        if (one) {
+            const long long q = (canvas_s && isfinite(v)) ? fixed_value(v, scale) : 0ll;
+            const unsigned peers = __match_any_sync(active, k);
+            const long long sum = group_sum(active, peers, q);
+            if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) {
+                const unsigned c = (unsigned)__popc(peers);
+                if (priv) {
+                    atomicAdd(h.s_cnt + k, c);
+                    if (canvas_s) atomicAdd(h.s_sum + k, (unsigned long long)sum);
+                } else {
+                    atomicAdd(canvas_c + k, c);
+                    if (canvas_s) atomicAdd(reinterpret_cast<unsigned long long*>(canvas_s + k), (unsigned long long)sum);
+                }
+            }
+        }
+        if (valid && k == kMulti) map(x, y, v, h, dq);
+    }
     template <class H>
     __device__ __forceinline__ void map(float x, float y, float v, const H&, const DeferQ&) const {
         const size_t tile_px = (size_t)cx.resx * cx.resy;

@@ -130,7 +130,35 @@ __device__ bool compute_fraction(float x0, float y0, float x1, float y1,
 constexpr int kPolyWarps = 8;
 constexpr int kBand = 16;          // pixel rows per work item
 constexpr int kBandCap = 256;      // staged edges per warp
-constexpr int kCrossCap = 64;      // crossings per row per warp
+constexpr int kCrossCap = 512;     // crossings per row per warp (sorted into spans)
+// dynamic shared memory of k_poly_pass: per warp the staged edges, their
+// indices and one row's crossings
+constexpr size_t kPolySmem = (size_t)kPolyWarps * (kBandCap * (sizeof(int4) + sizeof(int)) + kCrossCap * sizeof(int));
+
+// Ascending sort of buf[0, m) by one warp (bitonic network in shared memory,
+// m padded to a power of two with INT_MAX).
+__device__ __forceinline__ void warp_sort_ints(int* buf, int m, int lane) {
+    int mp = 2;
+    while (mp < m) mp <<= 1;
+    for (int i = m + lane; i < mp; i += 32) buf[i] = INT_MAX;
+    __syncwarp();
+    for (int k = 2; k <= mp; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < mp; i += 32) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const int x = buf[i], y = buf[ixj];
+                    const bool up = (i & k) == 0;
+                    if ((x > y) == up) {
+                        buf[i] = y;
+                        buf[ixj] = x;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
 
 // Per (tile, polygon): pixel column range that can be covered, rows to visit
 // and rows whose centre line the polygon can cross; number of row bands.
@@ -193,16 +221,15 @@ __global__ void k_poly_info(PolyPassArgs a) {
 template <int MODE>
 __global__ void __launch_bounds__(kPolyWarps * 32)
 k_poly_pass(PolyPassArgs a) {
-    __shared__ int4 s_edge[kPolyWarps][kBandCap];
-    __shared__ int s_eidx[kPolyWarps][kBandCap];
-    __shared__ int s_cross[kPolyWarps][kCrossCap];
+    extern __shared__ int4 s_poly[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned FULL = 0xffffffffu;
     const int TP = a.T * a.P;
     const int total = a.band_start[TP];
-    int4* my_edge = s_edge[warp];
-    int* my_eidx = s_eidx[warp];
-    int* my_cross = s_cross[warp];
+    int4* my_edge = s_poly + (size_t)warp * kBandCap;
+    int* my_eidx = reinterpret_cast<int*>(s_poly + (size_t)kPolyWarps * kBandCap) + (size_t)warp * kBandCap;
+    int* my_cross = reinterpret_cast<int*>(s_poly + (size_t)kPolyWarps * kBandCap) + (size_t)kPolyWarps * kBandCap +
+                    (size_t)warp * kCrossCap;
 
     for (;;) {
         int item = 0, tp = 0;
@@ -263,44 +290,41 @@ k_poly_pass(PolyPassArgs a) {
 
         for (int j = jb; j <= je; ++j) {
             const int32_t cy = j * kSub + kSub / 2;
-            // crossings of this row's centre line
+            // crossings of this row's centre line: from the staged edges, or
+            // from all edges of the polygon when the band held too many
             int m = 0;
-            bool cover_slow = overflow;
-            if (!overflow) {
-                for (int e0 = 0; e0 < nb; e0 += 32) {
-                    int e = e0 + lane;
-                    bool c = false;
-                    int L = 0;
-                    if (e < nb) {
-                        int4 q = my_edge[e];
-                        if (cross_row(q.y, q.w, cy)) { c = true; L = cross_L(q.x, q.y, q.z, q.w, cy); }
+            const int ne = overflow ? n : nb;
+            for (int e0 = 0; e0 < ne; e0 += 32) {
+                const int e = e0 + lane;
+                bool c = false;
+                int L = 0;
+                if (e < ne) {
+                    int4 q;
+                    if (!overflow) {
+                        q = my_edge[e];
+                    } else {
+                        const int2 A = pv[e];
+                        const int2 B = pv[(e + 1 == n) ? 0 : e + 1];
+                        q = make_int4(A.x, A.y, B.x, B.y);
                     }
-                    unsigned bm = __ballot_sync(FULL, c);
-                    int pos = m + __popc(bm & ((1u << lane) - 1u));
-                    if (c && pos < kCrossCap) my_cross[pos] = L;
-                    m += __popc(bm);
+                    if (cross_row(q.y, q.w, cy)) { c = true; L = cross_L(q.x, q.y, q.z, q.w, cy); }
                 }
-                if (m > kCrossCap) cover_slow = true;
+                const unsigned bm = __ballot_sync(FULL, c);
+                const int pos = m + __popc(bm & ((1u << lane) - 1u));
+                if (c && pos < kCrossCap) my_cross[pos] = L;
+                m += __popc(bm);
             }
+            const bool cover_slow = m > kCrossCap;
             __syncwarp();
             const bool centre_row = (j >= j_lo && j <= j_hi);
-            if (centre_row && (m > 0 || cover_slow)) {
-                for (int i = i_lo + lane; i <= i_hi; i += 32) {
-                    bool inside = false;
-                    if (!cover_slow) {
-                        for (int k = 0; k < m; ++k) inside ^= (i < my_cross[k]);
-                    } else {
-                        for (int k = 0; k < n; ++k) {
-                            int2 A = pv[k];
-                            int2 B = pv[(k + 1 == n) ? 0 : k + 1];
-                            if (cross_row(A.y, B.y, cy)) inside ^= (i < cross_L(A.x, A.y, B.x, B.y, cy));
-                        }
-                    }
-                    if (!inside) continue;
+            if (centre_row && m > 0) {
+                // pixel i is covered when an odd number of crossings lie at or
+                // left of it: with the crossings sorted, [c0, c1), [c2, c3), ...
+                auto visit = [&](int i) {
                     const size_t pix = tile_off + (size_t)j * a.resx + i;
                     if (a.border) {
                         uint32_t w = __ldg(a.border + ((size_t)j * a.border_words + (i >> 5)));
-                        if ((w >> (i & 31)) & 1u) continue;
+                        if ((w >> (i & 31)) & 1u) return;
                     }
                     if (MODE == MODE_LABEL) {
                         a.label[pix] = (uint16_t)p;   // overlaps detected by counting, see k_label_finish
@@ -309,13 +333,29 @@ k_poly_pass(PolyPassArgs a) {
                         acc_c += __ldg(a.canvas_c + pix);
                         if (a.canvas_s) acc_s += __ldg(a.canvas_s + pix);
                     }
+                };
+                if (!cover_slow) {
+                    warp_sort_ints(my_cross, m, lane);
+                    for (int s2 = 0; s2 + 1 < m; s2 += 2) {
+                        const int L = max(my_cross[s2], i_lo), R = min(my_cross[s2 + 1], i_hi + 1);
+                        for (int i = L + lane; i < R; i += 32) visit(i);
+                    }
+                } else {
+                    for (int i = i_lo + lane; i <= i_hi; i += 32) {
+                        bool inside = false;
+                        for (int k = 0; k < n; ++k) {
+                            int2 A = pv[k];
+                            int2 B = pv[(k + 1 == n) ? 0 : k + 1];
+                            if (cross_row(A.y, B.y, cy)) inside ^= (i < cross_L(A.x, A.y, B.x, B.y, cy));
+                        }
+                        if (inside) visit(i);
+                    }
                 }
             }
             if (MODE == MODE_BOUNDS) {
                 // Outline pass: every edge of the polygon touching this pixel
                 // row, every pixel of the row the edge clips.
                 const float ylo = (float)j, yhi = (float)(j + 1);
-                const int ne = overflow ? n : nb;
                 for (int e0 = 0; e0 < ne; e0 += 32) {
                     int e = e0 + lane;
                     if (e >= ne) continue;
@@ -884,13 +924,25 @@ void launch_poly_info(int mode, const PolyPassArgs& a, int sms, cudaStream_t st)
     else k_poly_info<MODE_REDUCE><<<blocks, 256, 0, st>>>(a);
 }
 
+template <int MODE>
+static void launch_poly_pass_t(const PolyPassArgs& a, int sms, cudaStream_t st) {
+    static bool attr_set = false;   // per template instance
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_poly_pass<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPolySmem);
+        attr_set = true;
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_poly_pass<MODE>, kPolyWarps * 32, kPolySmem);
+    const int blocks = sms * std::max(per_sm, 1);
+    k_poly_pass<MODE><<<blocks, kPolyWarps * 32, kPolySmem, st>>>(a);
+}
+
 void launch_poly_pass(int mode, const PolyPassArgs& a, int sms, cudaStream_t st) {
-    int blocks = sms * 4;
     ++g_kernel_launches;
     switch (mode) {
-        case MODE_REDUCE: k_poly_pass<MODE_REDUCE><<<blocks, kPolyWarps * 32, 0, st>>>(a); break;
-        case MODE_LABEL: k_poly_pass<MODE_LABEL><<<blocks, kPolyWarps * 32, 0, st>>>(a); break;
-        default: k_poly_pass<MODE_BOUNDS><<<blocks, kPolyWarps * 32, 0, st>>>(a); break;
+        case MODE_REDUCE: launch_poly_pass_t<MODE_REDUCE>(a, sms, st); break;
+        case MODE_LABEL: launch_poly_pass_t<MODE_LABEL>(a, sms, st); break;
+        default: launch_poly_pass_t<MODE_BOUNDS>(a, sms, st); break;
     }
 }
 

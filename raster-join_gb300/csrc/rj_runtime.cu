@@ -11,8 +11,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "rj_device.cuh"
@@ -144,6 +146,18 @@ int plan_raster_bbox(rj_ctx* ctx, const double* bbox, const rj_query* q, RasterP
 }
 
 int plan_raster(rj_ctx* ctx, const rj_query* q, RasterPlan& rp) { return plan_raster_bbox(ctx, ctx->ps->bbox, q, rp); }
+
+uint64_t canvas_key(const std::vector<float4>& colxf, const std::vector<float4>& rowxf, int resx, int resy) {
+    uint64_t h = 1469598103934665603ULL;   // FNV-1a
+    auto mix = [&](const void* p, size_t n) {
+        for (size_t i = 0; i < n; ++i) h = (h ^ ((const unsigned char*)p)[i]) * 1099511628211ULL;
+    };
+    const int dims[4] = {(int)colxf.size(), (int)rowxf.size(), resx, resy};
+    mix(dims, sizeof dims);
+    mix(colxf.data(), colxf.size() * sizeof(float4));
+    mix(rowxf.data(), rowxf.size() * sizeof(float4));
+    return h;
+}
 
 // Filter + aggregation (GLFunction::setupPoints GLFunction.cpp:199-344).
 int build_filter(rj_ctx* ctx, const rj_query* q, DevFilter& f, bool force_count, bool* empty = nullptr) {
@@ -542,6 +556,82 @@ PointArgs make_point_args(rj_ctx* ctx, const DevFilter& f, unsigned long long* o
     return pa;
 }
 
+// The point pass of one query: one launch over the resident table, or, for a
+// streamed table, one launch per chunk of rows, each chunk's columns copied
+// into one of two device buffers on a copy stream while the previous chunk
+// is processed (the reference's memory passes, GLFunction.cpp:330-337 and
+// RasterJoin.cpp:215-236).
+template <class Launch>
+int point_pass(rj_ctx* ctx, const DevFilter& f, unsigned long long* oc, unsigned long long* os, Launch&& launch) {
+    ctx->passes = 1;
+    ctx->copy_ms = 0;
+    PointArgs pa = make_point_args(ctx, f, oc, os);
+    if (!ctx->streamed) {
+        launch(pa);
+        return RJ_OK;
+    }
+    // host columns the query reads: location, filter columns, aggregate
+    std::vector<const char*> src;
+    std::vector<size_t> esz;
+    auto slot = [&](const void* p, size_t e) {
+        for (size_t i = 0; i < src.size(); ++i)
+            if (src[i] == (const char*)p) return (int)i;
+        src.push_back((const char*)p);
+        esz.push_back(e);
+        return (int)src.size() - 1;
+    };
+    const Column* loc = find_col(ctx, ctx->loc_attrib);
+    slot(loc->d, 8);
+    int cslot[kMaxFilters];
+    for (int c = 0; c < f.ncol; ++c) cslot[c] = slot(f.col[c], 4);
+    const int aslot = f.aggr_col ? slot(f.aggr_col, 4) : -1;
+    size_t rec = 0;
+    for (size_t e : esz) rec += e;
+    const uint64_t n = ctx->npts;
+    const uint64_t chunk = std::max<uint64_t>(4, ctx->chunk & ~3ULL);
+    int rc;
+    for (int b = 0; b < 2; ++b)
+        if ((rc = dev_alloc(ctx, ctx->sbuf[b], chunk * rec + 256 * src.size()))) return rc;
+    if (!ctx->copy_stream) {
+        RJ_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; ++b) {
+            RJ_CUDA(cudaEventCreateWithFlags(&ctx->copied[b], cudaEventDisableTiming));
+            RJ_CUDA(cudaEventCreateWithFlags(&ctx->consumed[b], cudaEventDisableTiming));
+        }
+        RJ_CUDA(cudaEventCreate(&ctx->copy_t0));
+        RJ_CUDA(cudaEventCreate(&ctx->copy_t1));
+    }
+    // buffers are free once the work queued so far on the stream has run
+    for (int b = 0; b < 2; ++b) RJ_CUDA(cudaEventRecord(ctx->consumed[b], ctx->stream));
+    RJ_CUDA(cudaEventRecord(ctx->copy_t0, ctx->copy_stream));
+    int passes = 0;
+    for (uint64_t r0 = 0; r0 < n; r0 += chunk, ++passes) {
+        const int b = passes & 1;
+        const uint64_t rows = std::min(chunk, n - r0);
+        RJ_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->consumed[b], 0));
+        std::vector<char*> dst(src.size());
+        char* base = (char*)ctx->sbuf[b].p;
+        for (size_t i = 0; i < src.size(); ++i) {
+            dst[i] = base;
+            base += ((chunk * esz[i]) + 255) & ~(size_t)255;
+            RJ_CUDA(cudaMemcpyAsync(dst[i], src[i] + r0 * esz[i], rows * esz[i], cudaMemcpyHostToDevice, ctx->copy_stream));
+        }
+        RJ_CUDA(cudaEventRecord(ctx->copied[b], ctx->copy_stream));
+        RJ_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->copied[b], 0));
+        PointArgs pc = pa;
+        pc.xy = (const float2*)dst[0];
+        pc.n = rows;
+        for (int c = 0; c < f.ncol; ++c) pc.f.col[c] = (const uint32_t*)dst[cslot[c]];
+        if (aslot >= 0) pc.f.aggr_col = (const uint32_t*)dst[aslot];
+        launch(pc);
+        RJ_CUDA(cudaEventRecord(ctx->consumed[b], ctx->stream));
+    }
+    RJ_CUDA(cudaEventRecord(ctx->copy_t1, ctx->copy_stream));
+    ctx->passes = std::max(passes, 1);
+    RJ_CUDA(cudaGetLastError());
+    return RJ_OK;
+}
+
 CanvasXf make_canvas_xf(rj_ctx* ctx, const RasterPlan& rp, const float4* dcol, const float4* drow) {
     CanvasXf cx{};
     cx.colxf = dcol;
@@ -600,7 +690,7 @@ int poly_pass(rj_ctx* ctx, int mode, PolyPassArgs& a) {
 // some pixel centre lies in two polygons (the label map cannot represent the
 // set; the canvas path is used instead).
 int label_map(rj_ctx* ctx, PolyPassArgs& a, const char* key, size_t npix, const uint32_t* mask, int words,
-              uint16_t** out, int* overlap) {
+              uint64_t canvas, uint16_t** out, int* overlap) {
     int rc;
     uint16_t* label;
     unsigned long long* cnt;
@@ -613,11 +703,16 @@ int label_map(rj_ctx* ctx, PolyPassArgs& a, const char* key, size_t npix, const 
     if ((rc = poly_pass(ctx, MODE_LABEL, a))) return rc;
     launch_label_finish(label, mask, a.resx, a.resy, a.T, words, cnt + 1, ctx->sms, ctx->stream);
     RJ_CUDA(cudaGetLastError());
-    // Optimistic: the polygon set is assumed not to overlap; rj_execute reads
-    // the two counters with the results and re-runs the query on the canvas
-    // path if some pixel centre lay in two polygons.
-    *overlap = 0;
-    if (ctx->ps->overlap_known != 0) ctx->overlap_pending = cnt;
+    // The first label map of a polygon set decides whether its coverage
+    // overlaps (every covered pixel centre counted once per polygon vs the
+    // labelled pixels); the answer is kept with the set.
+    if (ctx->ps->overlap_on(canvas) == -1) {
+        unsigned long long lc[2] = {0, 0};
+        RJ_CUDA(cudaMemcpyAsync(lc, cnt, sizeof lc, cudaMemcpyDeviceToHost, ctx->stream));
+        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        ctx->ps->overlap[canvas] = (lc[0] != lc[1]) ? 1 : 0;
+    }
+    *overlap = ctx->ps->overlap_on(canvas) == 1 ? 1 : 0;
     *out = label;
     a.label = nullptr;
     return RJ_OK;
@@ -657,16 +752,19 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
     a.out_bounds = es.out_bounds;
     a.line_filter = (q->flags & RJ_FLAG_LINE_FILTER) ? 1 : 0;
 
-    bool use_label = !bounds && !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->ps->overlap_known != 1 &&
+    const uint64_t ckey = canvas_key(rp.colxf, rp.rowxf, rp.resx, rp.resy);
+    bool use_label = !bounds && !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->ps->overlap_on(ckey) != 1 &&
                      ctx->ps->P <= kMaxLabelPolys;
     if (use_label) {
         uint16_t* label;
         int overlap = 0;
-        if ((rc = label_map(ctx, a, "label", npix, nullptr, 0, &label, &overlap))) return rc;
+        if ((rc = label_map(ctx, a, "label", npix, nullptr, 0, ckey, &label, &overlap))) return rc;
         es.ph->mark(2);
         if (!overlap) {
-            PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
-            launch_raster_label(pa, cx, label, ctx->sms, ctx->stream);
+            if ((rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
+                     launch_raster_label(pa, cx, label, ctx->sms, ctx->stream);
+                 })))
+                return rc;
             RJ_CUDA(cudaGetLastError());
             es.ph->mark(3);
             es.ph->mark(4);
@@ -684,8 +782,10 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
         if ((rc = scratch_t(ctx, "canvas_s", npix, &canvas_s))) return rc;
         RJ_CUDA(cudaMemsetAsync(canvas_s, 0, npix * sizeof(long long), ctx->stream));
     }
-    PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
-    launch_raster_splat(pa, cx, canvas_c, canvas_s, ctx->sms, ctx->stream);
+    if ((rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
+             launch_raster_splat(pa, cx, canvas_c, canvas_s, ctx->sms, ctx->stream);
+         })))
+        return rc;
     RJ_CUDA(cudaGetLastError());
     es.ph->mark(3);
     a.canvas_c = canvas_c;
@@ -706,17 +806,22 @@ int exec_index(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     if (q->grid_res <= 0 || q->grid_res > 8192) return fail(ctx, RJ_E_INVALID, "grid resolution %d out of range", q->grid_res);
     es.ph->mark(1);
     const bool plain = (q->flags & (RJ_FLAG_NO_CELL_CLASSIFY | RJ_FLAG_COMPAT_INDEX_CLAMP)) != 0;
-    PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
     if (plain) {
         IndexArgs ia{};
         if ((rc = build_grid(ctx, q->grid_res, (q->flags & RJ_FLAG_COMPAT_INDEX_CLAMP) ? 1 : 0, ia))) return rc;
         es.ph->mark(2);
-        launch_index_points(pa, ia, ctx->sms, ctx->stream);
+        if ((rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
+                 launch_index_points(pa, ia, ctx->sms, ctx->stream);
+             })))
+            return rc;
     } else {
         ExactIndex ix{};
         if ((rc = build_exact(ctx, q->grid_res, ix))) return rc;
         es.ph->mark(2);
-        launch_exact_points(pa, ix, ctx->sms, ctx->stream);
+        if ((rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
+                 launch_exact_points(pa, ix, ctx->sms, ctx->stream);
+             })))
+            return rc;
     }
     RJ_CUDA(cudaGetLastError());
     es.ph->mark(3);
@@ -800,18 +905,21 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     ha.h = h;
     ha.border = mask;
     ha.words = words;
-    bool use_label = !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->ps->overlap_known != 1 && ctx->ps->P <= kMaxLabelPolys;
+    const uint64_t ckey = canvas_key(colxf, rowxf, resx, resy);
+    bool use_label = !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->ps->overlap_on(ckey) != 1 && ctx->ps->P <= kMaxLabelPolys;
     if (use_label) {
         uint16_t* label;
         int overlap = 0;
-        if ((rc = label_map(ctx, a, "hyb_label", npix, mask, words, &label, &overlap))) return rc;
+        if ((rc = label_map(ctx, a, "hyb_label", npix, mask, words, ckey, &label, &overlap))) return rc;
         if (overlap) use_label = false;
         else ha.label = label;
     }
     es.ph->mark(2);
-    PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
     if (use_label) {
-        launch_hybrid_points(pa, ix, ha, ctx->sms, ctx->stream);
+        if ((rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
+                 launch_hybrid_points(pa, ix, ha, ctx->sms, ctx->stream);
+             })))
+            return rc;
         RJ_CUDA(cudaGetLastError());
         es.ph->mark(3);
         es.ph->mark(4);
@@ -829,7 +937,10 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     ha.canvas_s = canvas_s;
     ha.scale = f.sum_scale;
     ha.label = nullptr;
-    launch_hybrid_points(pa, ix, ha, ctx->sms, ctx->stream);
+    if ((rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
+             launch_hybrid_points(pa, ix, ha, ctx->sms, ctx->stream);
+         })))
+        return rc;
     RJ_CUDA(cudaGetLastError());
     es.ph->mark(3);
     // polygon-inside pass over non-border pixels (polygon-inside.frag:30-57)
@@ -905,7 +1016,7 @@ int load_polyset(rj_ctx* ctx, PolySet& s, const float* xy, const int32_t* pindex
     s.max_edge_dy = mdy;
     static std::atomic<uint64_t> g_set_version{0};
     s.version = ++g_set_version;
-    s.overlap_known = -1;
+    s.overlap.clear();
     s.grid.valid = false;
     s.exact.valid = false;
     return RJ_OK;
@@ -1019,6 +1130,17 @@ void rj_destroy(rj_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_batch_engine(ctx);
     free_points(ctx);
+    for (auto& b : ctx->sbuf) dev_free(ctx, b);
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
+        for (int b = 0; b < 2; ++b) {
+            cudaEventDestroy(ctx->copied[b]);
+            cudaEventDestroy(ctx->consumed[b]);
+        }
+        cudaEventDestroy(ctx->copy_t0);
+        cudaEventDestroy(ctx->copy_t1);
+    }
     free_polyset(ctx, ctx->own);
     for (auto& kv : ctx->scratch) dev_free(ctx, kv.second);
     for (auto& ev : ctx->ev)
@@ -1065,8 +1187,38 @@ static int column_stats(rj_ctx* ctx) {
     return RJ_OK;
 }
 
+// Largest finite |value| of every scalar column of a host-resident table
+// (several threads over row ranges).
+static void column_stats_host(rj_ctx* ctx) {
+    const uint64_t n = ctx->npts;
+    for (Column& c : ctx->cols) {
+        if (c.type == RJ_LOCATION || n == 0) continue;
+        const int nt = (int)std::max<uint64_t>(1, std::min<uint64_t>(16, n / (1 << 20)));
+        std::vector<float> part(nt, 0.f);
+        std::vector<std::thread> th;
+        for (int k = 0; k < nt; ++k) {
+            th.emplace_back([&, k] {
+                const uint64_t a = n * k / nt, b = n * (k + 1) / nt;
+                const uint32_t* v = (const uint32_t*)c.d;
+                float m = 0.f;
+                for (uint64_t i = a; i < b; ++i) {
+                    float x;
+                    if (c.type == RJ_FLOAT) std::memcpy(&x, v + i, 4);
+                    else if (c.type == RJ_INT) x = (float)(int32_t)v[i];
+                    else x = (float)v[i];
+                    x = std::fabs(x);
+                    if (std::isfinite(x)) m = std::max(m, x);
+                }
+                part[k] = m;
+            });
+        }
+        for (auto& t : th) t.join();
+        c.absmax = *std::max_element(part.begin(), part.end());
+    }
+}
+
 static int load_points_impl(rj_ctx* ctx, const rj_column* cols, int32_t ncols, uint64_t npoints, int32_t loc,
-                            bool device) {
+                            bool device, bool streamed = false, uint64_t chunk = 0) {
     if (!ctx) return RJ_E_INVALID;
     ctx->err.clear();
     if (!cols || ncols <= 0 || ncols > RJ_MAX_ATTRIBUTES)
@@ -1091,8 +1243,11 @@ static int load_points_impl(rj_ctx* ctx, const rj_column* cols, int32_t ncols, u
     if (ctx->server_running) return fail(ctx, RJ_E_BUSY, "a serving loop owns the context");
     cudaSetDevice(ctx->device);
     ctx->tix.valid = false;
+    const bool was_streamed = ctx->streamed;
+    ctx->streamed = false;
     // same layout as the resident table: copy into the existing buffers
-    bool same = !device && (int)ctx->cols.size() == ncols && ctx->npts == npoints && ctx->loc_attrib == loc;
+    bool same = !device && !streamed && !was_streamed && (int)ctx->cols.size() == ncols && ctx->npts == npoints &&
+                ctx->loc_attrib == loc;
     for (int i = 0; same && i < ncols; ++i)
         same = ctx->cols[i].owned && ctx->cols[i].attrib == cols[i].attrib_id && ctx->cols[i].type == cols[i].type;
     if (same) {
@@ -1118,7 +1273,7 @@ static int load_points_impl(rj_ctx* ctx, const rj_column* cols, int32_t ncols, u
         c.attrib = cols[i].attrib_id;
         c.type = cols[i].type;
         const size_t esz = c.type == RJ_LOCATION ? 8 : 4;
-        if (device) {
+        if (device || streamed) {
             c.d = const_cast<void*>(cols[i].data);
             c.owned = false;
         } else {
@@ -1145,6 +1300,23 @@ static int load_points_impl(rj_ctx* ctx, const rj_column* cols, int32_t ncols, u
     ctx->npts = npoints;
     ctx->loc_attrib = loc;
     RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (streamed) {
+        ctx->streamed = true;
+        uint64_t c = chunk;
+        if (c == 0) {
+            // two chunk buffers of every column within half the free budget
+            size_t rec = 0;
+            for (const Column& col : ctx->cols) rec += col.type == RJ_LOCATION ? 8 : 4;
+            size_t fr = 0, tot = 0;
+            cudaMemGetInfo(&fr, &tot);
+            size_t room = fr / 4;
+            if (ctx->budget > 0) room = std::min<size_t>(room, (size_t)std::max<int64_t>(ctx->budget - (int64_t)ctx->used, 0) / 2);
+            c = std::max<uint64_t>(1 << 20, std::min<uint64_t>(1ULL << 28, room / 2 / std::max<size_t>(rec, 1)));
+        }
+        ctx->chunk = std::max<uint64_t>(4, c & ~3ULL);
+        column_stats_host(ctx);
+        return RJ_OK;
+    }
     return column_stats(ctx);
 }
 
@@ -1155,6 +1327,11 @@ int rj_load_points(rj_ctx* ctx, const rj_column* cols, int32_t ncols, uint64_t n
 int rj_attach_points_device(rj_ctx* ctx, const rj_column* cols, int32_t ncols, uint64_t npoints,
                             int32_t loc_attrib) {
     return load_points_impl(ctx, cols, ncols, npoints, loc_attrib, true);
+}
+
+int rj_attach_points_host(rj_ctx* ctx, const rj_column* cols, int32_t ncols, uint64_t npoints, int32_t loc_attrib,
+                          uint64_t chunk_points) {
+    return load_points_impl(ctx, cols, ncols, npoints, loc_attrib, false, true, chunk_points);
 }
 
 int rj_free_points(rj_ctx* ctx) {
@@ -1173,6 +1350,7 @@ int rj_free_points(rj_ctx* ctx) {
     ctx->cols.clear();
     ctx->npts = 0;
     ctx->loc_attrib = -1;
+    ctx->streamed = false;
     return RJ_OK;
 }
 
@@ -1212,7 +1390,6 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
     if (q->flags & RJ_FLAG_NO_CACHE) {
         ctx->ps->grid.valid = false;
         ctx->ps->exact.valid = false;
-        ctx->ps->overlap_known = -1;
     }
     g_kernel_launches = 0;
     unsigned long long* oc;
@@ -1237,43 +1414,27 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
     std::vector<double> hnf(P);
     std::vector<long long> hb;
     int derr = 0;
-    for (int attempt = 0; attempt < 2; ++attempt) {
-        ctx->overlap_pending = nullptr;
-        switch (q->function_type) {
-            case RJ_RASTER_JOIN: rc = exec_raster(ctx, q, es, false); break;
-            case RJ_INDEX_JOIN: rc = exec_index(ctx, q, es); break;
-            case RJ_HYBRID_JOIN: rc = exec_hybrid(ctx, q, es); break;
-            default: rc = exec_raster(ctx, q, es, true); break;
-        }
-        if (rc) {
-            cudaStreamSynchronize(ctx->stream);
-            return rc;
-        }
-        RJ_CUDA(cudaMemcpyAsync(hc.data(), oc, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
-        RJ_CUDA(cudaMemcpyAsync(hq.data(), os, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
-        RJ_CUDA(cudaMemcpyAsync(hnf.data(), onf, P * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-        if (q->function_type == RJ_RASTER_JOIN_BOUNDS && res && res->bounds) {
-            hb.resize((size_t)4 * P);
-            RJ_CUDA(cudaMemcpyAsync(hb.data(), ob, (size_t)4 * P * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
-        }
-        unsigned long long lc[2] = {0, 0};
-        if (ctx->overlap_pending)
-            RJ_CUDA(cudaMemcpyAsync(lc, ctx->overlap_pending, sizeof lc, cudaMemcpyDeviceToHost, ctx->stream));
-        RJ_CUDA(cudaMemcpyAsync(&derr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-        ph.mark(5);
-        RJ_CUDA(cudaStreamSynchronize(ctx->stream));
-        RJ_CUDA(cudaGetLastError());
-        if (!ctx->overlap_pending) break;
-        ctx->ps->overlap_known = (lc[0] != lc[1]) ? 1 : 0;
-        if (!ctx->ps->overlap_known) break;
-        // overlapping polygons: the label map cannot hold them, redo on the canvas path
-        RJ_CUDA(cudaMemsetAsync(oc, 0, P * sizeof(unsigned long long), ctx->stream));
-        RJ_CUDA(cudaMemsetAsync(os, 0, P * sizeof(unsigned long long), ctx->stream));
-        RJ_CUDA(cudaMemsetAsync(onf, 0, P * sizeof(double), ctx->stream));
-        RJ_CUDA(cudaMemsetAsync(ob, 0, (size_t)4 * P * sizeof(long long), ctx->stream));
-        RJ_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    switch (q->function_type) {
+        case RJ_RASTER_JOIN: rc = exec_raster(ctx, q, es, false); break;
+        case RJ_INDEX_JOIN: rc = exec_index(ctx, q, es); break;
+        case RJ_HYBRID_JOIN: rc = exec_hybrid(ctx, q, es); break;
+        default: rc = exec_raster(ctx, q, es, true); break;
     }
-    ctx->overlap_pending = nullptr;
+    if (rc) {
+        cudaStreamSynchronize(ctx->stream);
+        return rc;
+    }
+    RJ_CUDA(cudaMemcpyAsync(hc.data(), oc, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    RJ_CUDA(cudaMemcpyAsync(hq.data(), os, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    RJ_CUDA(cudaMemcpyAsync(hnf.data(), onf, P * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (q->function_type == RJ_RASTER_JOIN_BOUNDS && res && res->bounds) {
+        hb.resize((size_t)4 * P);
+        RJ_CUDA(cudaMemcpyAsync(hb.data(), ob, (size_t)4 * P * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    RJ_CUDA(cudaMemcpyAsync(&derr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ph.mark(5);
+    RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    RJ_CUDA(cudaGetLastError());
     if (derr) return fail(ctx, RJ_E_TIMEOUT, "a bounded device wait ran out (status 0x%x)", derr);
     decode_result(P, hc.data(), hq.data(), hnf.data(), ctx->sum_shift, hb.empty() ? nullptr : hb.data(), res);
     // timings (GLHandler::printTimeStats fields)
@@ -1282,13 +1443,18 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
     t.pts_size = ctx->npts;
     t.poly_size = P;
     t.function = q->function_type;
-    t.no_pt_passes = 1;
+    t.no_pt_passes = ctx->passes;
     t.no_constraints = q->n_constraints;
     t.setup_ms = t_setup - t0;
     t.poly_index_ms = (q->function_type == RJ_INDEX_JOIN || q->function_type == RJ_HYBRID_JOIN) ? ph.ms(1, 2) : 0.0;
     t.poly_render_ms = (q->function_type == RJ_INDEX_JOIN || q->function_type == RJ_HYBRID_JOIN) ? ph.ms(3, 4) : ph.ms(1, 2) + ph.ms(3, 4);
     t.pt_render_ms = ph.ms(2, 3);
     t.poly_mem_ms = ph.ms(4, 5);
+    if (ctx->streamed && ctx->copy_t0) {
+        float cm = 0.f;
+        if (cudaEventElapsedTime(&cm, ctx->copy_t0, ctx->copy_t1) == cudaSuccess) t.pt_mem_ms = cm;
+        else cudaGetLastError();
+    }
     t.execute_ms = now_ms() - t0;
     t.accuracy = (q->function_type == RJ_RASTER_JOIN) ? (int)q->accuracy_m : 0;
     t.kernel_launches = g_kernel_launches;

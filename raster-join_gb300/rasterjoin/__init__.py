@@ -133,6 +133,7 @@ def load_library(path=LIB_PATH):
         "rj_load_points": (C.c_int, [C.c_void_p, P(Column), C.c_int32, C.c_uint64, C.c_int32]),
         "rj_attach_points_device": (C.c_int, [C.c_void_p, P(Column), C.c_int32, C.c_uint64, C.c_int32]),
         "rj_free_points": (C.c_int, [C.c_void_p]),
+        "rj_attach_points_host": (C.c_int, [C.c_void_p, P(Column), C.c_int32, C.c_uint64, C.c_int32, C.c_uint64]),
         "rj_set_polygons": (C.c_int, [C.c_void_p, P(C.c_float), P(C.c_int32), C.c_int32, P(C.c_double)]),
         "rj_execute": (C.c_int, [C.c_void_p, P(Query), P(Result)]),
         "rj_get_timings": (C.c_int, [C.c_void_p, P(Timings)]),
@@ -294,6 +295,7 @@ class DataHandler:
         self.aggr = Count
         self.aggr_attrib = -1
         self.time_range = None     # (attrib, start, end)
+        self.types = {}            # attribute types of a table loaded elsewhere (device / host attach)
 
     def add_column(self, attrib_id, attr_type, data):
         if attr_type == Location:
@@ -323,8 +325,14 @@ class DataHandler:
     def setTimeRange(self, attrib_id, start, end):
         self.time_range = None if attrib_id is None else (attrib_id, start, end)
 
+    def declare(self, attrib_id, attr_type):
+        """Type of a column held outside this DataHandler (attachDevice / attachHost)."""
+        self.types[attrib_id] = attr_type
+
     def attr_type(self, attrib_id):
-        return self.columns[attrib_id][0]
+        if attrib_id in self.columns:
+            return self.columns[attrib_id][0]
+        return self.types.get(attrib_id, Uint)
 
 
 class GLHandler:
@@ -399,7 +407,7 @@ class GLHandler:
         if dh is None:
             raise RJError(-6, "DataHandler not set")
         key = tuple((k, id(v[1])) for k, v in sorted(dh.columns.items()))
-        if force or key != self._loaded_points:
+        if dh.columns and (force or key != self._loaded_points):
             cols = (Column * len(dh.columns))()
             n = None
             for i, (aid, (typ, arr)) in enumerate(sorted(dh.columns.items())):
@@ -436,7 +444,7 @@ class GLHandler:
         else:
             q.n_constraints = len(dh.constraints)
             for i, (aid, ct, val) in enumerate(dh.constraints):
-                q.constraints[i] = constraint(aid, ct, val, dh.attr_type(aid) if aid in dh.columns else Uint)
+                q.constraints[i] = constraint(aid, ct, val, dh.attr_type(aid))
         q.accuracy_m = self.accuracy
         q.cell_size = self.cell_size
         q.ground_resolution = self.ground_resolution
@@ -450,7 +458,8 @@ class GLHandler:
 
     def execute(self, fn, query=None):
         """Run one join; returns JoinResult with exact arrays."""
-        self.upload()
+        if self.dataHandler is not None:
+            self.upload()
         q = query if query is not None else self.make_query(fn)
         P = self._bound.P if self._bound is not None else len(self.dataHandler.polys[1]) - 1
         count = np.zeros(P, np.uint64)
@@ -474,17 +483,47 @@ class GLHandler:
             return self.bounds
         return np.zeros(0, np.int32)
 
+    def attachDevice(self, columns, npoints, loc_attrib):
+        """Use device-resident columns as the point table without a copy.
+        columns: [(attrib_id, type, device_pointer)], 16-byte aligned, kept
+        alive by the caller."""
+        cols = (Column * len(columns))()
+        for i, (aid, typ, ptr) in enumerate(columns):
+            cols[i].attrib_id = aid
+            cols[i].type = typ
+            cols[i].data = ptr
+        self._check(self.lib.rj_attach_points_device(self.ctx, cols, len(columns), npoints, loc_attrib))
+        self._loaded_points = ("device", tuple(columns), npoints)
+
+    def attachHost(self, columns, npoints, loc_attrib, chunk_points=0):
+        """Out-of-core table: host arrays (kept alive by the caller) streamed
+        through the device in chunks of chunk_points rows by every query."""
+        cols = (Column * len(columns))()
+        keep = []
+        for i, (aid, typ, arr) in enumerate(columns):
+            arr = np.ascontiguousarray(arr)
+            keep.append(arr)
+            cols[i].attrib_id = aid
+            cols[i].type = typ
+            cols[i].data = arr.ctypes.data
+        self._check(self.lib.rj_attach_points_host(self.ctx, cols, len(columns), npoints, loc_attrib, chunk_points))
+        self._host_table = keep
+        self._loaded_points = ("host", tuple(id(a) for a in keep), npoints)
+
     # ---- polygon sets, time index, batches ----
     def polyset(self, xy, pindex, bbox=None):
         return PolySet(self, xy, pindex, bbox)
 
     def usePolySet(self, ps):
-        self.upload()
+        if self.dataHandler is not None:
+            self.upload()
         self._check(self.lib.rj_use_polyset(self.ctx, ps.ptr if ps is not None else None))
         self._bound = ps
 
     def buildTimeIndex(self, attrib_id, nbuckets=0):
-        self.upload()
+        if self.dataHandler is not None and not (isinstance(self._loaded_points, tuple)
+                                                 and self._loaded_points[:1] == ("device",)):
+            self.upload()
         self._check(self.lib.rj_build_time_index(self.ctx, attrib_id, nbuckets))
 
     def execute_batch(self, queries, polysets, flags=0, raise_on_error=True):

@@ -444,3 +444,77 @@ def test_timing_line(handler, c1):
     assert len(fields) == 15 and int(fields[0]) == len(pts["xy"]) and int(fields[2]) == 0
     t = handler.timings()
     assert t["pt_render_ms"] > 0
+
+
+def test_overlap_status_is_per_canvas(handler):
+    """Two squares sharing a 0.1-wide strip: no pixel centre of a 10-unit
+    canvas falls in the strip (label map), every 0.05-unit canvas has some
+    (the canvas path must take over after the coarse query)."""
+    rng = np.random.default_rng(3)
+    xy = np.c_[rng.uniform(0, 200, 200_000), rng.uniform(0, 100, 200_000)].astype(np.float32)
+    xy[:20_000, 0] = rng.uniform(99.9, 100.0, 20_000).astype(np.float32)
+    verts = np.array([[0, 0], [100, 0], [100, 100], [0, 100],
+                      [99.9, 0], [200, 0], [200, 100], [99.9, 100]], np.float32)
+    pidx = np.array([0, 4, 8], np.int32)
+    dh = rj.DataHandler()
+    dh.add_column(1, rj.Location, xy)
+    dh.setPolygons(verts, pidx)
+    handler.setDataHandler(dh)
+    for cell in (10.0, 0.05, 10.0):
+        handler.setCellSize(cell)
+        got = handler.execute(rj.RasterJoinFn)
+        want, _, _ = oracle.raster_join(xy, verts, pidx, cell)
+        np.testing.assert_array_equal(got.count, want)
+
+
+@pytest.mark.parametrize("cell", [800.0, 450.0, 120.0])
+def test_canvas_splat_small_and_large_canvases(handler, c1, cell):
+    """Canvas path (forced): shared-memory private canvases (<= 8192 pixels)
+    and warp-merged global splats give the oracle's counts and sums."""
+    pts, verts, pidx = c1
+    dh = make_dh(pts, verts, pidx)
+    dh.setAggregation(rj.Avg, 3)
+    handler.setDataHandler(dh)
+    handler.setCellSize(cell)
+    handler.flags = rj.FLAG_FORCE_CANVAS
+    try:
+        got = handler.execute(rj.RasterJoinFn)
+    finally:
+        handler.flags = 0
+    cols = ocols(pts)
+    want = oracle.raster_join(pts["xy"], verts, pidx, cell, f=cols.filt(aggr_attrib=3))
+    np.testing.assert_array_equal(got.count, want[0])
+    check_sums(got.sum, want[1])
+
+
+@pytest.mark.parametrize("fn", [rj.RasterJoinFn, rj.IndexJoinFn, rj.HybridJoinFn, rj.RasterJoinBoundFn])
+def test_streamed_host_table_matches_resident(c1, fn, built):
+    """A host-resident table streamed in chunks gives the resident table's
+    results; the timing line counts the passes."""
+    pts, verts, pidx = c1
+    res = {}
+    for mode in ("resident", "streamed"):
+        h = rj.GLHandler()
+        try:
+            if mode == "resident":
+                dh = make_dh(pts, verts, pidx)
+            else:
+                dh = rj.DataHandler()
+                dh.setPolygons(verts, pidx)
+                for aid, typ in ((2, rj.Uint), (3, rj.Float), (4, rj.Int), (5, rj.Int)):
+                    dh.declare(aid, typ)
+                h.attachHost([(1, rj.Location, pts["xy"]), (2, rj.Uint, pts["t"]), (3, rj.Float, pts["a"]),
+                              (4, rj.Int, pts["f1"]), (5, rj.Int, pts["f2"])], len(pts["t"]), 1, 100_000)
+            c2_query(dh)
+            h.setDataHandler(dh)
+            h.setCellSize(40.0)
+            h.setPolyIndexResolution(256)
+            r = h.execute(fn)
+            res[mode] = (r.count.copy(), r.sum.copy(), None if r.bounds is None else r.bounds.copy())
+            if mode == "streamed":
+                assert h.timings()["no_pt_passes"] == (len(pts["t"]) + 99_999) // 100_000
+        finally:
+            h.close()
+    for a, b in zip(res["resident"], res["streamed"]):
+        if a is not None:
+            np.testing.assert_array_equal(a, b)
