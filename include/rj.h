@@ -94,6 +94,9 @@ typedef struct {
 #define RJ_FLAG_NO_CACHE           0x40u /* rebuild every polygon-side structure
                                            (grid, labels, masks) for this call,
                                            as each reference execute() does */
+#define RJ_FLAG_FLAT_CANVAS        0x80u /* raster: one entry per pixel even for
+                                           large canvases (no 16 x 16 block
+                                           tiers; same results)              */
 
 /* One query: everything GLHandler + DataHandler held between calls
  * (setAccuracyDistance GLHandler.cpp:250, setPolyIndexResolution :259,
@@ -255,6 +258,16 @@ RJ_API int rj_use_polyset(rj_ctx *ctx, rj_polyset *ps);
  * (at most 16384).  Device-attached tables are copied into library-owned
  * buffers.  Reloading the table drops the index. */
 RJ_API int rj_build_time_index(rj_ctx *ctx, int32_t time_attrib, int32_t nbuckets);
+/* Clustered row order: rows sorted by time bucket (when time_attrib >= 0,
+ * which also builds the time index above) and, inside a bucket, by the
+ * Z-order of a 2^cell_bits x 2^cell_bits grid over the location bounds
+ * (cell_bits 0..12; buckets x cells <= 2^24).  Neighbouring rows then map to
+ * neighbouring pixels: label gathers hit the cache and a warp's points merge
+ * into few histogram updates.  The reference's backend stores points in
+ * spatio-temporal partitions for the same reason (HashGridIndex.cpp:98-113).
+ * time_attrib < 0: spatial order only (no time index).  Results are
+ * unchanged. */
+RJ_API int rj_cluster_points(rj_ctx *ctx, int32_t time_attrib, int32_t nbuckets, int32_t cell_bits);
 
 /* ---- batched execution ---------------------------------------------------
  * No counterpart in the reference (one executeFunction per query).  Runs nq
@@ -279,7 +292,9 @@ typedef struct {
     double poly_ms;                /* label maps / canvases (CUDA events)      */
     double point_ms;               /* fused point pass (CUDA events)           */
     double reduce_ms;              /* canvas polygon passes (CUDA events)      */
-    int32_t threads, rows_per_item, tuned;
+    int32_t threads, rows_per_item;   /* block shape of the fused point pass  */
+    int32_t direct;                   /* 1: rows streamed per query from L2, 0: staged in shared memory */
+    int32_t tuned;
     int32_t kernel_launches;
 } rj_batch_stats;
 RJ_API int rj_execute_batch(rj_ctx *ctx, int32_t nq, const rj_query *q, rj_polyset *const *sets,

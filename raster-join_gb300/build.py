@@ -20,7 +20,7 @@ OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "librj.so")
 SOURCES = ["rj_runtime.cu", "rj_point_kernels.cu", "rj_poly_kernels.cu", "rj_noalloc.cu",
-           "rj_batch.cu", "rj_batch_kernels.cu"]
+           "rj_batch.cu", "rj_batch_kernels.cu", "rj_tier_kernels.cu"]
 HEADERS = ["rj_device.cuh", "rj_launch.h", "rj_internal.h", "rj_point_map.cuh",
            os.path.join("..", "..", "include", "rj.h")]
 

@@ -61,7 +61,7 @@ struct Engine {
     cudaEvent_t ev[6]{};
     void* h_pin = nullptr;
     size_t h_pin_bytes = 0;
-    BatchShape shape{256, 4096};
+    BatchShape shape{256, 16384, 1};
     bool tuned = false;
 };
 
@@ -146,10 +146,17 @@ void plan_query(rj_ctx* ctx, QPlan& p, bool no_fuse) {
     if (rc) { p.status = rc; return; }
     p.shift = p.f.aggr ? ctx->sum_shift : 0;
     if (p.f.general && !empty) return;                             // per-predicate filters: plain path
-    p.fused = true;
     p.T = p.rp.splitx * p.rp.splity;
     p.npix = (size_t)p.rp.resx * p.rp.resy * p.T;
+    // large canvases take the single-query path, whose tiered canvas does
+    // per-block work instead of per-pixel work
+    if (p.npix >= kTierMinPixels && !(q->flags & RJ_FLAG_FLAT_CANVAS)) return;
+    p.fused = true;
     query_rows(ctx, q, p.r0, p.r1);
+    // row ranges on multiples of four rows (aligned 128-bit loads in the fused
+    // pass); the rows added are outside the time window and fail its predicate
+    p.r0 &= ~3ULL;
+    p.r1 = std::min<uint64_t>(ctx->npts, (p.r1 + 3) & ~3ULL);
     if (empty || p.r1 <= p.r0) {
         p.mode = BQ_SKIP;
         return;
@@ -463,6 +470,14 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
             d.label = p->label;
             d.canvas_c = p->cc;
             d.canvas_s = p->cs;
+            {
+                // canvas extent plus two pixels: a location outside it maps to
+                // no pixel of any tile (window range test and snapping)
+                const double mx = 2.0 * (p->ps->bbox[2] - p->ps->bbox[0]) / p->rp.actual_x + 1e-3;
+                const double my = 2.0 * (p->ps->bbox[3] - p->ps->bbox[1]) / p->rp.actual_y + 1e-3;
+                d.box = make_float4((float)(p->ps->bbox[0] - mx), (float)(p->ps->bbox[1] - my),
+                                    (float)(p->ps->bbox[2] + mx), (float)(p->ps->bbox[3] + my));
+            }
             if (p->mode == BQ_LABEL && d.P <= kBatchHistCap) max_hist = std::max(max_hist, d.P);
             if (p->mode == BQ_SPLAT && p->T == 1 && p->npix <= (size_t)kBatchHistCap) {
                 // small canvas: splat into the block's shared histogram (indexed by
@@ -529,7 +544,9 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
                 }
         };
         if ((flags & RJ_BATCH_AUTOTUNE) && !e.tuned && nitems > 0) {
-            static const BatchShape cands[] = {{256, 2048}, {256, 4096}, {256, 8192}, {512, 2048}, {512, 4096}, {512, 8192}};
+            static const BatchShape cands[] = {{256, 2048, 0},  {256, 4096, 0},  {256, 8192, 0},  {512, 4096, 0},
+                                               {256, 8192, 1},  {256, 16384, 1}, {256, 32768, 1}, {512, 16384, 1},
+                                               {512, 32768, 1}};
             float best = 1e30f;
             BatchShape bs = shape;
             for (const BatchShape& c : cands) {
@@ -551,7 +568,7 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
             bo.tuned = 1;
             zero_outputs();
         }
-        if (batch_blocks_per_sm(shape, ba.nu, hist_cap) < 1) shape = {256, 2048};
+        if (batch_blocks_per_sm(shape, ba.nu, hist_cap) < 1) shape = {256, 2048, 0};
         set_shape(shape);
         RJ_CUDA(cudaMemsetAsync(work, 0, 8, st));
         if (!launch_batch_points(ba, shape, ctx->sms, st))
@@ -660,6 +677,7 @@ int execute_batch(Engine& e, int nq, const rj_query* qs, const rj_query* const* 
         stats->reduce_ms = bo.reduce_ms;
         stats->threads = e.shape.threads;
         stats->rows_per_item = e.shape.rows;
+        stats->direct = e.shape.direct;
         stats->tuned = bo.tuned;
         stats->kernel_launches = launches_fused + plain_launches;
     }
@@ -829,57 +847,110 @@ int rj_use_polyset(rj_ctx* ctx, rj_polyset* ps) {
 }
 
 int rj_build_time_index(rj_ctx* ctx, int32_t attrib, int32_t nbuckets) {
+    return rj_cluster_points(ctx, attrib, nbuckets, 0);
+}
+
+int rj_cluster_points(rj_ctx* ctx, int32_t attrib, int32_t nbuckets, int32_t cell_bits) {
     if (!ctx) return RJ_E_INVALID;
     std::lock_guard<std::recursive_mutex> lock(ctx->mu);
     ctx->err.clear();
     if (ctx->server_running) return fail(ctx, RJ_E_BUSY, "a serving loop owns the context");
     if (ctx->cols.empty()) return fail(ctx, RJ_E_NO_DATA, "point table not loaded");
-    if (ctx->streamed) return fail(ctx, RJ_E_UNSUPPORTED, "a streamed (host-resident) table has no time index");
-    const Column* tc = find_col(ctx, attrib);
-    if (!tc || tc->type != RJ_UINT) return fail(ctx, RJ_E_INVALID, "time attribute %d is not a loaded uint column", attrib);
-    const int nb = nbuckets > 0 ? nbuckets : 16384;
-    if (nb > 16384) return fail(ctx, RJ_E_INVALID, "at most 16384 time buckets");
+    if (ctx->streamed) return fail(ctx, RJ_E_UNSUPPORTED, "a streamed (host-resident) table cannot be reordered");
+    const Column* tc = nullptr;
+    if (attrib >= 0) {
+        tc = find_col(ctx, attrib);
+        if (!tc || tc->type != RJ_UINT)
+            return fail(ctx, RJ_E_INVALID, "time attribute %d is not a loaded uint column", attrib);
+    }
+    if (cell_bits < 0 || cell_bits > 12) return fail(ctx, RJ_E_INVALID, "cell_bits must be 0..12");
+    if (!tc && cell_bits == 0) return fail(ctx, RJ_E_INVALID, "nothing to order by (no time attribute, no cells)");
+    const int nbt = tc ? (nbuckets > 0 ? nbuckets : 16384) : 1;
+    if (nbt > (1 << 24)) return fail(ctx, RJ_E_INVALID, "too many time buckets");
+    const uint64_t nkeys = (uint64_t)nbt << (2 * cell_bits);
+    if (nkeys > (1ULL << 24)) return fail(ctx, RJ_E_INVALID, "time buckets x cells exceed 2^24 keys");
     cudaSetDevice(ctx->device);
     const uint64_t n = ctx->npts;
     cudaStream_t st = ctx->stream;
+    const Column* loc = find_col(ctx, ctx->loc_attrib);
     TimeIndex tix;
     tix.attrib = attrib;
-    tix.nb = nb;
-    tix.start.assign(nb + 1, 0);
+    tix.nb = nbt;
+    tix.start.assign(nbt + 1, 0);
     if (n == 0) {
-        tix.valid = true;
+        tix.valid = tc != nullptr;
         ctx->tix = tix;
         return RJ_OK;
     }
-    DevBuf mm, hist, cursor;
+    ClusterKey key{};
+    key.nbt = nbt;
+    key.cb = cell_bits;
+    key.xy = (const float2*)loc->d;
+    DevBuf mm;
     int rc;
-    if ((rc = dev_alloc(ctx, mm, 8))) return rc;
+    if ((rc = dev_alloc(ctx, mm, 32))) return rc;
     unsigned* dmm = (unsigned*)mm.p;
-    cudaMemsetAsync(dmm, 0xFF, 4, st);
-    cudaMemsetAsync(dmm + 1, 0, 4, st);
-    launch_time_minmax((const uint32_t*)tc->d, n, dmm, dmm + 1, ctx->sms, st);
-    unsigned hmm[2];
-    cudaMemcpyAsync(hmm, dmm, 8, cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) {
-        dev_free(ctx, mm);
-        return fail(ctx, RJ_E_CUDA, "time range reduction failed");
-    }
-    dev_free(ctx, mm);
-    tix.tmin = hmm[0];
-    tix.tmax = hmm[1];
-    if ((rc = dev_alloc(ctx, hist, (size_t)nb * 4))) return rc;
-    cudaMemsetAsync(hist.p, 0, (size_t)nb * 4, st);
-    launch_time_hist((const uint32_t*)tc->d, n, tix.tmin, tix.tmax, nb, (unsigned*)hist.p, ctx->sms, st);
-    std::vector<unsigned> hh(nb);
-    cudaMemcpyAsync(hh.data(), hist.p, (size_t)nb * 4, cudaMemcpyDeviceToHost, st);
+    unsigned hmm[6] = {0xFFFFFFFFu, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u};
+    cudaMemcpyAsync(dmm, hmm, sizeof hmm, cudaMemcpyHostToDevice, st);
+    if (tc) launch_time_minmax((const uint32_t*)tc->d, n, dmm, dmm + 1, ctx->sms, st);
+    if (cell_bits) launch_xy_bounds((const float2*)loc->d, n, dmm + 2, ctx->sms, st);
+    cudaMemcpyAsync(hmm, dmm, sizeof hmm, cudaMemcpyDeviceToHost, st);
     cudaError_t ce = cudaStreamSynchronize(st);
+    dev_free(ctx, mm);
+    if (ce != cudaSuccess) return fail(ctx, RJ_E_CUDA, "bounds reduction failed: %s", cudaGetErrorString(ce));
+    if (tc) {
+        key.t = (const uint32_t*)tc->d;
+        key.tmin = tix.tmin = hmm[0];
+        key.tmax = tix.tmax = hmm[1];
+    }
+    if (cell_bits) {
+        auto unorder = [](unsigned u) {
+            const unsigned b = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+            float f;
+            std::memcpy(&f, &b, 4);
+            return f;
+        };
+        const float lx = unorder(hmm[2]), ly = unorder(hmm[3]), hx = unorder(hmm[4]), hy = unorder(hmm[5]);
+        const double cells = (double)(1 << cell_bits);
+        key.x0 = std::isfinite(lx) ? lx : 0.f;
+        key.y0 = std::isfinite(ly) ? ly : 0.f;
+        key.sx = (std::isfinite(hx) && hx > lx) ? (float)(cells / ((double)hx - lx)) : 0.f;
+        key.sy = (std::isfinite(hy) && hy > ly) ? (float)(cells / ((double)hy - ly)) : 0.f;
+    }
+    // key histogram -> row offsets
+    DevBuf hist, cursor;
+    if ((rc = dev_alloc(ctx, hist, nkeys * 4))) return rc;
+    cudaMemsetAsync(hist.p, 0, nkeys * 4, st);
+    launch_cluster_hist(key, n, (unsigned*)hist.p, ctx->sms, st);
+    std::vector<unsigned> hh(nkeys);
+    cudaMemcpyAsync(hh.data(), hist.p, nkeys * 4, cudaMemcpyDeviceToHost, st);
+    ce = cudaStreamSynchronize(st);
     dev_free(ctx, hist);
-    if (ce != cudaSuccess) return fail(ctx, RJ_E_CUDA, "time histogram failed: %s", cudaGetErrorString(ce));
-    for (int b = 0; b < nb; ++b) tix.start[b + 1] = tix.start[b] + hh[b];
-    if (tix.start[nb] != n) return fail(ctx, RJ_E_CUDA, "time histogram does not add up");
-    if ((rc = dev_alloc(ctx, cursor, (size_t)nb * 8))) return rc;
-    cudaMemcpyAsync(cursor.p, tix.start.data(), (size_t)nb * 8, cudaMemcpyHostToDevice, st);
-    // new column buffers in bucket order
+    if (ce != cudaSuccess) return fail(ctx, RJ_E_CUDA, "key histogram failed: %s", cudaGetErrorString(ce));
+    std::vector<uint64_t> start(nkeys + 1, 0);
+    for (uint64_t b = 0; b < nkeys; ++b) start[b + 1] = start[b] + hh[b];
+    if (start[nkeys] != n) return fail(ctx, RJ_E_CUDA, "key histogram does not add up");
+    for (int b = 0; b <= nbt; ++b) tix.start[b] = start[(uint64_t)b << (2 * cell_bits)];
+    if (tc && cell_bits == 0) {
+        // a table already in bucket order keeps its row order
+        DevBuf flag;
+        if ((rc = dev_alloc(ctx, flag, 8))) return rc;
+        cudaMemsetAsync(flag.p, 0, 8, st);
+        launch_time_unsorted((const uint32_t*)tc->d, n, tix.tmin, tix.tmax, nbt, (unsigned long long*)flag.p, ctx->sms, st);
+        unsigned long long unsorted = 1;
+        cudaMemcpyAsync(&unsorted, flag.p, 8, cudaMemcpyDeviceToHost, st);
+        ce = cudaStreamSynchronize(st);
+        dev_free(ctx, flag);
+        if (ce != cudaSuccess) return fail(ctx, RJ_E_CUDA, "time order check failed: %s", cudaGetErrorString(ce));
+        if (unsorted == 0) {
+            tix.valid = true;
+            ctx->tix = tix;
+            return RJ_OK;
+        }
+    }
+    if ((rc = dev_alloc(ctx, cursor, nkeys * 8))) return rc;
+    cudaMemcpyAsync(cursor.p, start.data(), nkeys * 8, cudaMemcpyHostToDevice, st);
+    // new column buffers in key order
     PermuteCols pc{};
     pc.ncol = (int)ctx->cols.size();
     std::vector<void*> fresh(pc.ncol, nullptr);
@@ -901,13 +972,12 @@ int rj_build_time_index(rj_ctx* ctx, int32_t attrib, int32_t nbuckets) {
         pc.dst[c] = fresh[c];
         pc.esz[c] = (int)esz;
     }
-    launch_time_scatter((const uint32_t*)tc->d, n, tix.tmin, tix.tmax, nb, (unsigned long long*)cursor.p, pc,
-                        ctx->sms, st);
+    launch_cluster_scatter(key, n, (unsigned long long*)cursor.p, pc, ctx->sms, st);
     ce = cudaStreamSynchronize(st);
     dev_free(ctx, cursor);
     if (ce != cudaSuccess) {
         for (void* p : fresh) cudaFree(p);
-        return fail(ctx, RJ_E_CUDA, "time scatter failed: %s", cudaGetErrorString(ce));
+        return fail(ctx, RJ_E_CUDA, "reorder scatter failed: %s", cudaGetErrorString(ce));
     }
     for (int c = 0; c < pc.ncol; ++c) {
         Column& col = ctx->cols[c];
@@ -921,8 +991,9 @@ int rj_build_time_index(rj_ctx* ctx, int32_t attrib, int32_t nbuckets) {
         col.owned = true;
         ctx->used += bytes;
     }
-    tix.valid = true;
+    tix.valid = tc != nullptr;
     ctx->tix = tix;
+    ctx->zones_valid = false;   // rows moved
     return RJ_OK;
 }
 

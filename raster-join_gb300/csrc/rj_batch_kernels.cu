@@ -28,7 +28,7 @@
 namespace rj {
 
 size_t batch_smem_bytes(const BatchShape& s, int nu, int hist_cap) {
-    return (size_t)hist_cap * 12 + (size_t)s.rows * (8 + 4 * (size_t)nu);
+    return (size_t)hist_cap * 12 + (s.direct ? 0 : (size_t)s.rows * (8 + 4 * (size_t)nu));
 }
 
 template <bool AGG, bool SMEM, int BLOCK>
@@ -131,6 +131,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch_points(BatchArgs a) {
     uint32_t* s_col = reinterpret_cast<uint32_t*>(s_xy + a.rows);
     __shared__ unsigned long long s_item;
     __shared__ int s_seg;
+    __shared__ float4 s_box[BLOCK / 32 + 1];
     const int tid = threadIdx.x;
     for (;;) {
         if (tid == 0) {
@@ -157,8 +158,16 @@ __global__ void __launch_bounds__(BLOCK) k_batch_points(BatchArgs a) {
         const uint64_t rend = r0 + (uint64_t)a.rows < sg.r1 ? r0 + (uint64_t)a.rows : sg.r1;
         const int nrows = (int)(rend - r0);
         // stage the item's rows (read once per batch: evict-first)
+        // (and the item's location bounds: queries whose canvas lies apart
+        // from them skip the item; clustered tables make items compact)
+        float bx0 = INFINITY, by0 = INFINITY, bx1 = -INFINITY, by1 = -INFINITY;
         #pragma unroll 4
-        for (int i = tid; i < nrows; i += BLOCK) s_xy[i] = __ldcs(a.xy + r0 + i);
+        for (int i = tid; i < nrows; i += BLOCK) {
+            const float2 p = __ldcs(a.xy + r0 + i);
+            s_xy[i] = p;
+            bx0 = fminf(bx0, p.x); bx1 = fmaxf(bx1, p.x);
+            by0 = fminf(by0, p.y); by1 = fmaxf(by1, p.y);
+        }
         #pragma unroll
         for (int u = 0; u < kBatchMaxCols; ++u) {
             if (u >= a.nu) break;
@@ -167,11 +176,26 @@ __global__ void __launch_bounds__(BLOCK) k_batch_points(BatchArgs a) {
             #pragma unroll 4
             for (int i = tid; i < nrows; i += BLOCK) dst[i] = __ldcs(col + i);
         }
+        bx0 = warp_minf(bx0); bx1 = warp_maxf(bx1);
+        by0 = warp_minf(by0); by1 = warp_maxf(by1);
+        if ((tid & 31) == 0) s_box[tid >> 5] = make_float4(bx0, by0, bx1, by1);
         __syncthreads();
+        if (tid == 0) {
+            float4 b = s_box[0];
+            for (int w = 1; w < BLOCK / 32; ++w) {
+                const float4 o = s_box[w];
+                b = make_float4(fminf(b.x, o.x), fminf(b.y, o.y), fmaxf(b.z, o.z), fmaxf(b.w, o.w));
+            }
+            s_box[BLOCK / 32] = b;
+        }
+        __syncthreads();
+        const float4 ibox = s_box[BLOCK / 32];   // NaN coordinates drop out of fminf / fmaxf
         for (int qi = sg.qbegin; qi < sg.qend; ++qi) {
             const BatchQuery* Q = a.q + __ldg(a.qlist + qi);
             const int mode = Q->mode;
             if (mode == BQ_SKIP) continue;
+            const float4 qb = Q->box;
+            if (ibox.z < qb.x || ibox.x > qb.z || ibox.w < qb.y || ibox.y > qb.w) continue;   // uniform
             const bool agg = Q->aggr_u >= 0;
             const bool smem = Q->hist_smem != 0;
             if (agg) {
@@ -186,12 +210,167 @@ __global__ void __launch_bounds__(BLOCK) k_batch_points(BatchArgs a) {
     }
 }
 
+// Direct variant: no staging.  Each query of an item streams the item's rows
+// straight into registers with 128-bit loads (four rows per thread), as the
+// single-query point pass does; the first query brings the block of rows into
+// L2 and the others of the segment hit it there (the last one reads with
+// evict-first).  Items are longer (more rows per histogram flush); segment
+// boundaries are multiples of four rows, so the vector loads stay aligned.
+template <bool AGG, bool SMEM, int BLOCK>
+__device__ __forceinline__ void direct_query(const BatchArgs& a, const BatchQuery* __restrict__ Q, uint64_t r0,
+                                             uint64_t r1, bool last, uint32_t* s_cnt, unsigned long long* s_sum) {
+    const int tid = threadIdx.x;
+    const int mode = Q->mode;
+    const int P = Q->P;
+    uint32_t lo[kBatchMaxCols], span[kBatchMaxCols];
+    bool used[kBatchMaxCols];
+    const int aggr_u = Q->aggr_u;
+    #pragma unroll
+    for (int u = 0; u < kBatchMaxCols; ++u) {
+        lo[u] = Q->lo[u];
+        span[u] = Q->span[u];
+        used[u] = u < a.nu && (lo[u] != 0u || span[u] != 0xFFFFFFFFu || u == aggr_u);
+    }
+    const int aggr_typ = Q->aggr_typ;
+    if (SMEM) {
+        for (int b = tid; b < P; b += BLOCK) {
+            s_cnt[b] = 0u;
+            if (AGG) s_sum[b] = 0ull;
+        }
+        __syncthreads();
+    }
+    Hist<AGG, SMEM> h{s_cnt, s_sum, Q->out_count, Q->out_sum, Q->out_nonfinite, Q->sum_scale};
+    const DeferQ dq{nullptr, nullptr, nullptr, nullptr};
+    const CanvasXf cx = Q->cx;
+    const LabelMapper lm{cx, Q->label};
+    const SplatMapper sm{cx, Q->canvas_c, Q->canvas_s, Q->sum_scale, Q->out_nonfinite, SMEM ? 1 : 0};
+    for (uint64_t tb = r0; tb < r1; tb += (uint64_t)BLOCK * 4) {
+        const uint64_t base = tb + (uint64_t)tid * 4;
+        float x[4], y[4], v[4];
+        uint32_t mask = 0u;
+        if (base + 4 <= r1) {
+            const float4 p0 = last ? __ldcs(reinterpret_cast<const float4*>(a.xy + base))
+                                   : __ldcg(reinterpret_cast<const float4*>(a.xy + base));
+            const float4 p1 = last ? __ldcs(reinterpret_cast<const float4*>(a.xy + base + 2))
+                                   : __ldcg(reinterpret_cast<const float4*>(a.xy + base + 2));
+            x[0] = p0.x; y[0] = p0.y; x[1] = p0.z; y[1] = p0.w;
+            x[2] = p1.x; y[2] = p1.y; x[3] = p1.z; y[3] = p1.w;
+            v[0] = v[1] = v[2] = v[3] = 0.f;
+            mask = 0xFu;
+            #pragma unroll
+            for (int u = 0; u < kBatchMaxCols; ++u) {
+                if (!used[u]) continue;
+                const uint4 c = last ? __ldcs(reinterpret_cast<const uint4*>(a.ucol[u] + base))
+                                     : __ldcg(reinterpret_cast<const uint4*>(a.ucol[u] + base));
+                const int t = a.utyp[u];
+                mask &= ((order_key(t, c.x) - lo[u] <= span[u]) ? 1u : 0u) | ((order_key(t, c.y) - lo[u] <= span[u]) ? 2u : 0u) |
+                        ((order_key(t, c.z) - lo[u] <= span[u]) ? 4u : 0u) | ((order_key(t, c.w) - lo[u] <= span[u]) ? 8u : 0u);
+                if (AGG && u == aggr_u) {
+                    v[0] = agg_value(aggr_typ, c.x); v[1] = agg_value(aggr_typ, c.y);
+                    v[2] = agg_value(aggr_typ, c.z); v[3] = agg_value(aggr_typ, c.w);
+                }
+            }
+        } else {
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint64_t i = base + k;
+                x[k] = y[k] = v[k] = 0.f;
+                if (i >= r1) continue;
+                const float2 p = a.xy[i];
+                x[k] = p.x;
+                y[k] = p.y;
+                bool ok = true;
+                #pragma unroll
+                for (int u = 0; u < kBatchMaxCols; ++u) {
+                    if (!used[u]) continue;
+                    const uint32_t c = a.ucol[u][i];
+                    ok = ok && (order_key(a.utyp[u], c) - lo[u] <= span[u]);
+                    if (AGG && u == aggr_u) v[k] = agg_value(aggr_typ, c);
+                }
+                if (ok) mask |= 1u << k;
+            }
+        }
+        if (mode == BQ_LABEL) {
+            LabelMapper::Key key[4];
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) key[k] = ((mask >> k) & 1u) ? lm.lookup(x[k], y[k]) : LabelMapper::kNone;
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) lm.consume(((mask >> k) & 1u) != 0u, key[k], x[k], y[k], v[k], h, dq);
+        } else {
+            SplatMapper::Key key[4];
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) key[k] = ((mask >> k) & 1u) ? sm.lookup(x[k], y[k]) : SplatMapper::kNone;
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) sm.consume(((mask >> k) & 1u) != 0u, key[k], x[k], y[k], v[k], h, dq);
+        }
+    }
+    if (SMEM) {
+        __syncthreads();
+        for (int b = tid; b < P; b += BLOCK) {
+            const uint32_t c = s_cnt[b];
+            if (c) {
+                if (Q->out_count32) atomicAdd(Q->out_count32 + b, c);
+                else atomicAdd(Q->out_count + b, (unsigned long long)c);
+                if (AGG) atomicAdd(Q->out_sum + b, s_sum[b]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 template <int BLOCK>
-static int blocks_per_sm_t(size_t smem) {
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(k_batch_points<BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+__global__ void __launch_bounds__(BLOCK) k_batch_direct(BatchArgs a) {
+    extern __shared__ unsigned long long smem_b[];
+    unsigned long long* s_sum = smem_b;
+    uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_sum + a.hist_cap);
+    __shared__ unsigned long long s_item;
+    __shared__ int s_seg;
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) {
+            const unsigned long long it = atomicAdd(a.work, 1ull);
+            int seg = 0;
+            if (it < a.nitems) {
+                int lo = 0, hi = a.nseg - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (a.seg[mid].item0 <= it) lo = mid;
+                    else hi = mid - 1;
+                }
+                seg = lo;
+            }
+            s_item = it;
+            s_seg = seg;
+        }
+        __syncthreads();
+        const unsigned long long item = s_item;
+        if (item >= a.nitems) break;
+        const BatchSeg sg = a.seg[s_seg];
+        const uint64_t r0 = sg.r0 + (item - sg.item0) * (uint64_t)a.rows;
+        const uint64_t r1 = r0 + (uint64_t)a.rows < sg.r1 ? r0 + (uint64_t)a.rows : sg.r1;
+        for (int qi = sg.qbegin; qi < sg.qend; ++qi) {
+            const BatchQuery* Q = a.q + __ldg(a.qlist + qi);
+            if (Q->mode == BQ_SKIP) continue;
+            const bool last = qi + 1 == sg.qend;
+            const bool agg = Q->aggr_u >= 0;
+            const bool smem = Q->hist_smem != 0;
+            if (agg) {
+                if (smem) direct_query<true, true, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum);
+                else direct_query<true, false, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum);
+            } else {
+                if (smem) direct_query<false, true, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum);
+                else direct_query<false, false, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum);
+            }
+        }
+        __syncthreads();   // s_item is rewritten for the next item
+    }
+}
+
+template <class K>
+static int blocks_per_sm_k(K kernel, int block, size_t smem) {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_points<BLOCK>, BLOCK, smem) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
@@ -200,7 +379,9 @@ static int blocks_per_sm_t(size_t smem) {
 
 int batch_blocks_per_sm(const BatchShape& s, int nu, int hist_cap) {
     const size_t smem = batch_smem_bytes(s, nu, hist_cap);
-    return s.threads == 512 ? blocks_per_sm_t<512>(smem) : blocks_per_sm_t<256>(smem);
+    if (s.direct)
+        return s.threads == 512 ? blocks_per_sm_k(k_batch_direct<512>, 512, smem) : blocks_per_sm_k(k_batch_direct<256>, 256, smem);
+    return s.threads == 512 ? blocks_per_sm_k(k_batch_points<512>, 512, smem) : blocks_per_sm_k(k_batch_points<256>, 256, smem);
 }
 
 bool launch_batch_points(const BatchArgs& a, const BatchShape& s, int sms, cudaStream_t st) {
@@ -210,8 +391,13 @@ bool launch_batch_points(const BatchArgs& a, const BatchShape& s, int sms, cudaS
     if (per_sm < 1) return false;
     uint64_t blocks = (uint64_t)sms * per_sm;
     if (blocks > a.nitems) blocks = a.nitems;
-    if (s.threads == 512) k_batch_points<512><<<(unsigned)blocks, 512, smem, st>>>(a);
-    else k_batch_points<256><<<(unsigned)blocks, 256, smem, st>>>(a);
+    if (s.direct) {
+        if (s.threads == 512) k_batch_direct<512><<<(unsigned)blocks, 512, smem, st>>>(a);
+        else k_batch_direct<256><<<(unsigned)blocks, 256, smem, st>>>(a);
+    } else {
+        if (s.threads == 512) k_batch_points<512><<<(unsigned)blocks, 512, smem, st>>>(a);
+        else k_batch_points<256><<<(unsigned)blocks, 256, smem, st>>>(a);
+    }
     ++g_kernel_launches;
     return true;
 }
@@ -249,47 +435,101 @@ void launch_time_minmax(const uint32_t* t, uint64_t n, unsigned* out_min, unsign
     ++g_kernel_launches;
 }
 
-// bucket histogram: per-block shared counts (nb <= 16384), flushed once
-__global__ void k_time_hist(const uint32_t* __restrict__ t, uint64_t n, uint32_t tmin, uint32_t tmax, int nb,
-                            unsigned* __restrict__ hist) {
-    extern __shared__ unsigned s_h[];
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) s_h[b] = 0u;
-    __syncthreads();
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        atomicAdd(s_h + time_bucket(__ldcs(t + i), tmin, tmax, nb), 1u);
-    __syncthreads();
-    for (int b = threadIdx.x; b < nb; b += blockDim.x)
-        if (s_h[b]) atomicAdd(hist + b, s_h[b]);
+// ---------------------------------------------------------------------------
+// Clustered row order: key = time bucket (major) then the Z-order of a
+// 2^cb x 2^cb cell grid over the location bounds (minor).  A counting sort
+// on the key puts the rows of one time slice and one cell next to each
+// other, as the reference backend's spatio-temporal partitions do.
+__device__ __forceinline__ uint32_t spread_bits(uint32_t v) {
+    v &= 0xFFFu;
+    v = (v | (v << 8)) & 0x00FF00FFu;
+    v = (v | (v << 4)) & 0x0F0F0F0Fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
 }
 
-void launch_time_hist(const uint32_t* t, uint64_t n, uint32_t tmin, uint32_t tmax, int nb, unsigned* hist, int sms,
-                      cudaStream_t st) {
-    const size_t smem = (size_t)nb * sizeof(unsigned);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_time_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    uint64_t blocks = std::min<uint64_t>((n + 1023) / 1024, (uint64_t)sms * 2);
+__device__ __forceinline__ uint32_t cluster_key(const ClusterKey& k, uint64_t i) {
+    const uint32_t tb = k.t ? time_bucket(k.t[i], k.tmin, k.tmax, k.nbt) : 0u;
+    if (k.cb == 0) return tb;
+    const float2 p = k.xy[i];
+    const int top = (1 << k.cb) - 1;
+    const float fx = (p.x - k.x0) * k.sx, fy = (p.y - k.y0) * k.sy;
+    const int cx = fx >= 0.f ? min((int)fx, top) : 0;   // NaN -> 0
+    const int cy = fy >= 0.f ? min((int)fy, top) : 0;
+    return (tb << (2 * k.cb)) | spread_bits((uint32_t)cx) | (spread_bits((uint32_t)cy) << 1);
+}
+
+// float <-> unsigned with the same order (for atomicMin / atomicMax)
+__device__ __forceinline__ unsigned float_order(float f) {
+    const unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__global__ void k_xy_bounds(const float2* __restrict__ xy, uint64_t n, unsigned* __restrict__ out) {
+    unsigned lx = 0xFFFFFFFFu, ly = 0xFFFFFFFFu, hx = 0u, hy = 0u;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float2 p = __ldcs(xy + i);
+        if (isfinite(p.x)) { lx = min(lx, float_order(p.x)); hx = max(hx, float_order(p.x)); }
+        if (isfinite(p.y)) { ly = min(ly, float_order(p.y)); hy = max(hy, float_order(p.y)); }
+    }
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lx = min(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+        ly = min(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+        hx = max(hx, __shfl_xor_sync(0xffffffffu, hx, o));
+        hy = max(hy, __shfl_xor_sync(0xffffffffu, hy, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(out + 0, lx);
+        atomicMin(out + 1, ly);
+        atomicMax(out + 2, hx);
+        atomicMax(out + 3, hy);
+    }
+}
+
+void launch_xy_bounds(const float2* xy, uint64_t n, unsigned* out, int sms, cudaStream_t st) {
+    uint64_t blocks = std::min<uint64_t>((n + 255) / 256, (uint64_t)sms * 8);
     if (blocks < 1) blocks = 1;
-    k_time_hist<<<(unsigned)blocks, 1024, smem, st>>>(t, n, tmin, tmax, nb, hist);
+    k_xy_bounds<<<(unsigned)blocks, 256, 0, st>>>(xy, n, out);
     ++g_kernel_launches;
 }
 
-// Scatter every column of row i to its bucket slot.  Lanes of a warp with the
-// same bucket reserve their slots with one atomic.
-__global__ void k_time_scatter(const uint32_t* __restrict__ t, uint64_t n, uint32_t tmin, uint32_t tmax, int nb,
-                               unsigned long long* __restrict__ cursor, PermuteCols pc) {
+// key histogram: lanes with the same key add once (global counters, up to 2^24 keys)
+__global__ void k_cluster_hist(ClusterKey k, uint64_t n, unsigned* __restrict__ hist) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
-    // warp-uniform trip count
-    const uint64_t first = (blockIdx.x * (uint64_t)blockDim.x) + (threadIdx.x & ~31u);
-    for (uint64_t w0 = first; w0 < n; w0 += stride) {
+    for (uint64_t w0 = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
         const uint64_t i = w0 + lane;
         const bool valid = i < n;
-        const uint32_t b = valid ? time_bucket(t[i], tmin, tmax, nb) : 0xFFFFFFFFu;
+        const uint32_t key = valid ? cluster_key(k, i) : 0u;
         const unsigned active = __ballot_sync(0xffffffffu, valid);
         if (!valid) continue;
-        const unsigned peers = __match_any_sync(active, b);
+        const unsigned peers = __match_any_sync(active, key);
+        if (lane == __ffs(peers) - 1) atomicAdd(hist + key, (unsigned)__popc(peers));
+    }
+}
+
+void launch_cluster_hist(const ClusterKey& k, uint64_t n, unsigned* hist, int sms, cudaStream_t st) {
+    uint64_t blocks = std::min<uint64_t>((n + 255) / 256, (uint64_t)sms * 8);
+    if (blocks < 1) blocks = 1;
+    k_cluster_hist<<<(unsigned)blocks, 256, 0, st>>>(k, n, hist);
+    ++g_kernel_launches;
+}
+
+__global__ void k_cluster_scatter(ClusterKey k, uint64_t n, unsigned long long* __restrict__ cursor, PermuteCols pc) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    for (uint64_t w0 = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
+        const uint64_t i = w0 + lane;
+        const bool valid = i < n;
+        const uint32_t key = valid ? cluster_key(k, i) : 0u;
+        const unsigned active = __ballot_sync(0xffffffffu, valid);
+        if (!valid) continue;
+        const unsigned peers = __match_any_sync(active, key);
         const int leader = __ffs(peers) - 1;
         unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(cursor + b, (unsigned long long)__popc(peers));
+        if (lane == leader) base = atomicAdd(cursor + key, (unsigned long long)__popc(peers));
         base = __shfl_sync(peers, base, leader);
         const uint64_t pos = base + __popc(peers & ((1u << lane) - 1u));
         for (int c = 0; c < pc.ncol; ++c) {
@@ -301,11 +541,30 @@ __global__ void k_time_scatter(const uint32_t* __restrict__ t, uint64_t n, uint3
     }
 }
 
-void launch_time_scatter(const uint32_t* t, uint64_t n, uint32_t tmin, uint32_t tmax, int nb,
-                         unsigned long long* cursor, const PermuteCols& pc, int sms, cudaStream_t st) {
+void launch_cluster_scatter(const ClusterKey& k, uint64_t n, unsigned long long* cursor, const PermuteCols& pc, int sms,
+                            cudaStream_t st) {
     uint64_t blocks = std::min<uint64_t>((n + 255) / 256, (uint64_t)sms * 8);
     if (blocks < 1) blocks = 1;
-    k_time_scatter<<<(unsigned)blocks, 256, 0, st>>>(t, n, tmin, tmax, nb, cursor, pc);
+    k_cluster_scatter<<<(unsigned)blocks, 256, 0, st>>>(k, n, cursor, pc);
+    ++g_kernel_launches;
+}
+
+// rows whose bucket is below the previous row's (0: already in bucket order)
+__global__ void k_time_unsorted(const uint32_t* __restrict__ t, uint64_t n, uint32_t tmin, uint32_t tmax, int nb,
+                                unsigned long long* __restrict__ count) {
+    unsigned long long c = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x + 1; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        c += time_bucket(__ldcs(t + i), tmin, tmax, nb) < time_bucket(t[i - 1], tmin, tmax, nb);
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+void launch_time_unsorted(const uint32_t* t, uint64_t n, uint32_t tmin, uint32_t tmax, int nb, unsigned long long* count,
+                          int sms, cudaStream_t st) {
+    uint64_t blocks = std::min<uint64_t>((n + 255) / 256, (uint64_t)sms * 8);
+    if (blocks < 1) blocks = 1;
+    k_time_unsorted<<<(unsigned)blocks, 256, 0, st>>>(t, n, tmin, tmax, nb, count);
     ++g_kernel_launches;
 }
 

@@ -113,6 +113,9 @@ struct rj_ctx {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copied[2]{}, consumed[2]{}, copy_t0{}, copy_t1{};
     rjh::DevBuf sbuf[2];
+    rjh::DevBuf zones;               // zone map of the resident table (bounds per 1024 rows)
+    bool zones_valid = false;
+    float4 qbox{};                   // locations that can reach the current query's polygons
     int passes = 1;                  // point passes of the last query
     double copy_ms = 0;              // host->device copy time of the last query
 
@@ -140,6 +143,10 @@ struct rj_polyset {
 };
 
 namespace rjh {
+
+// raster canvases of at least this many pixels use the tiered form (16 x 16
+// blocks, per-pixel data only where polygon edges pass)
+constexpr size_t kTierMinPixels = (size_t)1 << 24;
 
 int fail(rj_ctx* c, int code, const char* fmt, ...);
 

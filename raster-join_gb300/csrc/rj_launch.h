@@ -9,7 +9,26 @@
 
 namespace rj {
 
-enum { MODE_REDUCE = 0, MODE_LABEL = 1, MODE_BOUNDS = 2 };
+enum { MODE_REDUCE = 0, MODE_LABEL = 1, MODE_BOUNDS = 2, MODE_TIER_CLASSIFY = 3, MODE_TIER_LABEL = 4,
+       MODE_TIER_REDUCE = 5 };
+
+// Tiered canvas: 16 x 16-pixel blocks; per-pixel data only for mixed blocks.
+constexpr uint32_t kTierEmpty = 0xFFFFFFFFu;   // no polygon reaches the block
+constexpr uint32_t kTierMulti = 0xFFFFFFFEu;   // two or more polygons cover it whole
+constexpr uint32_t kTierMixed = 0x80000000u;   // | slot: per-pixel data in the slot
+struct TierArgs {
+    int bw, bh;                  // blocks per tile row / per tile column
+    uint32_t* full;              // [nblk] polygon covering the whole block, kTierEmpty, kTierMulti
+    uint32_t* mixed;             // [nblk] 1: per-pixel block
+    const int* slot;             // [nblk] exclusive scan of mixed
+    uint32_t* code;              // [nblk] lookup code (full polygon / empty / multi / mixed | slot)
+    uint16_t* plabel;            // [nslots * 256] pixel labels of mixed blocks
+    uint32_t* bcnt;              // [nblk] block point counts (canvas form)
+    long long* bsum;             // [nblk] block fixed-point sums or null
+    uint32_t* pcnt;              // [nslots * 256] pixel counts of mixed blocks
+    long long* psum;             // [nslots * 256] or null
+};
+
 
 // Kernels launched by this thread since the last reset (reported per call).
 extern thread_local int g_kernel_launches;
@@ -37,6 +56,11 @@ struct PolyPassArgs {
     int* nbands;                 // bands of kBand rows
     const int* band_start;       // exclusive scan of nbands, [T*P + 1]
 };
+
+size_t tier_smem_bytes();
+void launch_tier_pass(int mode, const PolyPassArgs& a, const TierArgs& tr, int sms, cudaStream_t st);
+void launch_tier_codes(const TierArgs& tr, size_t nblk, unsigned long long* multi, int sms, cudaStream_t st);
+void launch_tier_nonempty(const uint16_t* plabel, size_t n, unsigned long long* count, int sms, cudaStream_t st);
 
 struct GridArgs {
     const float2* verts;
@@ -114,7 +138,14 @@ struct PointArgs {
     double* out_nonfinite;       // fp64 sums of the non-finite aggregate values
     int* err;                    // bit0: a bounded pipeline wait ran out
     uint32_t* out_count32;       // when set, the shared histogram flushes counts here (a u32 canvas)
+    // zone map: bounds of every kZoneRows rows of the table (row0 = table row
+    // of xy[0]); iterations whose rows lie apart from qbox are skipped
+    const float4* zones;
+    uint64_t row0;
+    float4 qbox;
 };
+constexpr int kZoneShift = 10;               // zones of 1024 rows
+void launch_zone_boxes(const float2* xy, uint64_t n, float4* zones, int sms, cudaStream_t st);
 
 // Exact point-in-polygon index (CSR over a uniform grid).
 struct IndexArgs {
@@ -160,6 +191,8 @@ void launch_raster_splat(const PointArgs& pa, const CanvasXf& cx, uint32_t* canv
                          int sms, cudaStream_t st);
 void launch_raster_label(const PointArgs& pa, const CanvasXf& cx, const uint16_t* label, int sms,
                          cudaStream_t st);
+void launch_tier_label_points(const PointArgs& pa, const CanvasXf& cx, const TierArgs& tr, int sms, cudaStream_t st);
+void launch_tier_splat_points(const PointArgs& pa, const CanvasXf& cx, const TierArgs& tr, int sms, cudaStream_t st);
 void launch_index_points(const PointArgs& pa, const IndexArgs& ia, int sms, cudaStream_t st);
 void launch_exact_points(const PointArgs& pa, const ExactIndex& ix, int sms, cudaStream_t st);
 void launch_hybrid_points(const PointArgs& pa, const ExactIndex& ix, const HybridArgs& ha, int sms,
@@ -200,6 +233,7 @@ struct BatchQuery {
     unsigned long long* out_sum;          // [P] fixed-point
     double* out_nonfinite;                // [P]
     uint32_t* out_count32;                // private splat: counts flushed into the u32 canvas
+    float4 box;                           // locations that can reach the canvas (x0, y0, x1, y1)
 };
 
 struct BatchSeg {
@@ -226,7 +260,8 @@ struct BatchArgs {
 // block shape of the batched kernel (picked by the tuner)
 struct BatchShape {
     int threads;                          // 256 or 512
-    int rows;                             // rows per work item: 2048, 4096 or 8192
+    int rows;                             // rows per work item
+    int direct;                           // 0: rows staged in shared memory; 1: streamed per query (L2 reuse)
 };
 size_t batch_smem_bytes(const BatchShape& s, int nu, int hist_cap);
 int batch_blocks_per_sm(const BatchShape& s, int nu, int hist_cap);
@@ -234,15 +269,25 @@ bool launch_batch_points(const BatchArgs& a, const BatchShape& s, int sms, cudaS
 
 // time index of the resident table
 void launch_time_minmax(const uint32_t* t, uint64_t n, unsigned* out_min, unsigned* out_max, int sms, cudaStream_t st);
-void launch_time_hist(const uint32_t* t, uint64_t n, uint32_t tmin, uint32_t tmax, int nb, unsigned* hist, int sms,
-                      cudaStream_t st);
 struct PermuteCols {
     int ncol;
     const void* src[RJ_MAX_ATTRIBUTES];
     void* dst[RJ_MAX_ATTRIBUTES];
     int esz[RJ_MAX_ATTRIBUTES];           // 4 or 8 bytes
 };
-void launch_time_scatter(const uint32_t* t, uint64_t n, uint32_t tmin, uint32_t tmax, int nb,
-                         unsigned long long* cursor, const PermuteCols& pc, int sms, cudaStream_t st);
+struct ClusterKey {
+    const uint32_t* t;                    // time column, or null (spatial order only)
+    uint32_t tmin, tmax;
+    int nbt;                              // time buckets
+    const float2* xy;
+    float x0, y0, sx, sy;                 // cell = (v - v0) * s, clamped to [0, 2^cb)
+    int cb;                               // cell bits per axis (0: time order only)
+};
+void launch_xy_bounds(const float2* xy, uint64_t n, unsigned* out, int sms, cudaStream_t st);
+void launch_cluster_hist(const ClusterKey& k, uint64_t n, unsigned* hist, int sms, cudaStream_t st);
+void launch_cluster_scatter(const ClusterKey& k, uint64_t n, unsigned long long* cursor, const PermuteCols& pc, int sms,
+                            cudaStream_t st);
+void launch_time_unsorted(const uint32_t* t, uint64_t n, uint32_t tmin, uint32_t tmax, int nb, unsigned long long* count,
+                          int sms, cudaStream_t st);
 
 }  // namespace rj

@@ -407,6 +407,17 @@ k_points(PointArgs pa, M mp) {
     constexpr uint64_t per_iter = (uint64_t)BLOCK * 4 * NG;
     // block-uniform trip count: every thread of a block runs the same iterations
     for (uint64_t tb = (uint64_t)blockIdx.x * per_iter; tb < pa.n; tb += (uint64_t)gridDim.x * per_iter) {
+        if (pa.zones) {
+            // skip rows whose zones lie apart from the query's reach (uniform)
+            const uint64_t z0 = (pa.row0 + tb) >> kZoneShift;
+            const uint64_t z1 = (pa.row0 + min(tb + per_iter, pa.n) - 1) >> kZoneShift;
+            bool meets = false;
+            for (uint64_t z = z0; z <= z1; ++z) {
+                const float4 b = __ldg(pa.zones + z);
+                meets |= !(b.z < pa.qbox.x || b.x > pa.qbox.z || b.w < pa.qbox.y || b.y > pa.qbox.w);
+            }
+            if (!meets) continue;
+        }
         float x[NG][4], y[NG][4], val[NG][4];
         uint32_t mask[NG];
         if (tb + per_iter <= pa.n) {
@@ -617,6 +628,33 @@ void launch_raster_splat(const PointArgs& pa, const CanvasXf& cx, uint32_t* canv
     else launch_points_t<SplatMapper, false, false>(p2, m, sms, st);
 }
 
+// Zone map: one warp per kZoneRows rows; NaN coordinates drop out.
+__global__ void k_zone_boxes(const float2* __restrict__ xy, uint64_t n, float4* __restrict__ zones) {
+    const uint64_t nz = (n + (1ull << kZoneShift) - 1) >> kZoneShift;
+    const int lane = threadIdx.x & 31;
+    for (uint64_t z = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; z < nz;
+         z += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+        float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+        const uint64_t a = z << kZoneShift, b = (n < a + (1ull << kZoneShift)) ? n : a + (1ull << kZoneShift);
+        for (uint64_t i = a + lane; i < b; i += 32) {
+            const float2 p = __ldcs(xy + i);
+            x0 = fminf(x0, p.x); x1 = fmaxf(x1, p.x);
+            y0 = fminf(y0, p.y); y1 = fmaxf(y1, p.y);
+        }
+        x0 = warp_minf(x0); x1 = warp_maxf(x1);
+        y0 = warp_minf(y0); y1 = warp_maxf(y1);
+        if (lane == 0) zones[z] = make_float4(x0, y0, x1, y1);
+    }
+}
+
+void launch_zone_boxes(const float2* xy, uint64_t n, float4* zones, int sms, cudaStream_t st) {
+    const uint64_t nz = (n + (1ull << kZoneShift) - 1) >> kZoneShift;
+    uint64_t blocks = std::min<uint64_t>((nz * 32 + 255) / 256, (uint64_t)sms * 16);
+    if (blocks < 1) blocks = 1;
+    k_zone_boxes<<<(unsigned)blocks, 256, 0, st>>>(xy, n, zones);
+    ++g_kernel_launches;
+}
+
 __global__ void k_col_absmax(const uint32_t* __restrict__ col, int typ, uint64_t n, unsigned* __restrict__ out_bits) {
     unsigned m = 0u;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -639,6 +677,19 @@ void launch_raster_label(const PointArgs& pa, const CanvasXf& cx, const uint16_t
                          cudaStream_t st) {
     LabelMapper m{cx, label};
     launch_points(pa, m, sms, st);
+}
+
+void launch_tier_label_points(const PointArgs& pa, const CanvasXf& cx, const TierArgs& tr, int sms, cudaStream_t st) {
+    TierLabelMapper m{cx, tr};
+    launch_points(pa, m, sms, st);
+}
+
+void launch_tier_splat_points(const PointArgs& pa, const CanvasXf& cx, const TierArgs& tr, int sms, cudaStream_t st) {
+    TierSplatMapper m{cx, tr, pa.f.sum_scale};
+    PointArgs p2 = pa;
+    p2.P = 0;   // no per-polygon histogram: the canvas takes the points
+    if (pa.f.aggr) launch_points_t<TierSplatMapper, true, false>(p2, m, sms, st);
+    else launch_points_t<TierSplatMapper, false, false>(p2, m, sms, st);
 }
 
 void launch_index_points(const PointArgs& pa, const IndexArgs& ia, int sms, cudaStream_t st) {

@@ -8,25 +8,40 @@
 namespace rj {
 
 // Sum of a 64-bit value over the lanes of `peers` (a __match_any_sync group
-// inside `active`); the result is meaningful at the group's lowest lane.
+// inside `active`; every lane of `active` calls this), valid at the group's
+// lowest lane.  Small groups (random rows): the leader pulls its peers' values
+// with shuffles, as many rounds as the largest group has members.  Large
+// groups (spatially clustered rows): one warp reduction per 22/22/20-bit
+// piece of the value (each piece sums within 32 bits over at most 32 lanes;
+// the pieces recombine modulo 2^64, the two's-complement sum); groups of one
+// lane skip it.
 __device__ __forceinline__ long long group_sum(unsigned active, unsigned peers, long long q) {
     const int lane = threadIdx.x & 31;
-    const int leader = __ffs(peers) - 1;
-    long long sum = q;
-    unsigned rest = (lane == leader) ? (peers & (peers - 1u)) : 0u;
-    while (__any_sync(active, rest != 0u)) {
-        const int src = rest ? __ffs(rest) - 1 : lane;
-        const long long o = __shfl_sync(active, q, src);
-        if (rest) {
-            sum += o;
-            rest &= rest - 1u;
+    const unsigned gsize = (unsigned)__popc(peers);
+    const unsigned maxg = __reduce_max_sync(active, gsize);
+    if (maxg == 1u) return q;
+    if (maxg <= 4u) {
+        const int leader = __ffs(peers) - 1;
+        long long sum = q;
+        unsigned rest = (lane == leader) ? (peers & (peers - 1u)) : 0u;
+        while (__any_sync(active, rest != 0u)) {
+            const int src = rest ? __ffs(rest) - 1 : lane;
+            const long long o = __shfl_sync(active, q, src);
+            if (rest) {
+                sum += o;
+                rest &= rest - 1u;
+            }
         }
+        return sum;
     }
-    return sum;
+    if (gsize == 1u) return q;
+    const unsigned long long u = (unsigned long long)q;
+    const unsigned s0 = __reduce_add_sync(peers, (unsigned)(u & 0x3FFFFFull));
+    const unsigned s1 = __reduce_add_sync(peers, (unsigned)((u >> 22) & 0x3FFFFFull));
+    const unsigned s2 = __reduce_add_sync(peers, (unsigned)(u >> 44));
+    return (long long)((unsigned long long)s0 + ((unsigned long long)s1 << 22) + ((unsigned long long)s2 << 44));
 }
 
-
-// ---------------------------------------------------------------------------
 template <bool AGG, bool SMEM>
 struct Hist {
     uint32_t* s_cnt;
@@ -235,5 +250,116 @@ struct LabelMapper {
     __device__ __forceinline__ void deferred(float, float, float, const H&) const {}
 };
 
+
+// Tiered canvas, label form: block code, then the pixel label of a mixed
+// block's slot.
+__device__ __forceinline__ uint32_t tier_label_at(const TierArgs& tr, int resx, int resy, size_t blk0, int px, int py) {
+    (void)resx; (void)resy;
+    const uint32_t code = __ldg(tr.code + blk0 + (size_t)(py >> 4) * tr.bw + (px >> 4));
+    if (code == kTierEmpty) return kEmptyLabel;
+    if (code & kTierMixed) {
+        if (code == kTierMulti) return kEmptyLabel;   // never in label form (overlap takes the canvas form)
+        return __ldg(tr.plabel + (size_t)(code & ~kTierMixed) * 256 + (size_t)(py & 15) * 16 + (px & 15));
+    }
+    return code;
+}
+
+struct TierLabelMapper {
+    static constexpr bool kDefer = false;
+    static constexpr bool kTwoPhase = true;
+    CanvasXf cx;
+    TierArgs tr;
+    using Key = uint32_t;
+    static constexpr Key kNone = 0xFFFFu;
+    static constexpr Key kMulti = 0x10000u;
+    __device__ __forceinline__ Key lookup(float x, float y) const {
+        if (cx.splitx != 1 || cx.splity != 1) return kMulti;
+        float wx = win_coord(x, cx.col0.x, cx.col0.y, cx.col0.z);
+        float wy = win_coord(y, cx.row0.x, cx.row0.y, cx.row0.z);
+        if (!(wx > -1.0f && wx < (float)cx.resx + 1.0f && wy > -1.0f && wy < (float)cx.resy + 1.0f)) return kNone;
+        int px = pix_of(snap_win(wx)), py = pix_of(snap_win(wy));
+        if (px < 0 || px >= cx.resx || py < 0 || py >= cx.resy) return kNone;
+        return tier_label_at(tr, cx.resx, cx.resy, 0, px, py);
+    }
+    template <class H>
+    __device__ __forceinline__ void consume(bool valid, Key k, float x, float y, float v, const H& h,
+                                            const DeferQ& q) const {
+        h.add_warp(valid && k < kBorderLabel, (int)k, v);
+        if (valid && k == kMulti) map(x, y, v, h, q);
+    }
+    template <class H>
+    __device__ __forceinline__ void map(float x, float y, float v, const H& h, const DeferQ&) const {
+        const size_t tile_blk = (size_t)tr.bw * tr.bh;
+        canvas_visit(cx, x, y, [&](int t, int px, int py) {
+            const uint32_t lab = tier_label_at(tr, cx.resx, cx.resy, (size_t)t * tile_blk, px, py);
+            if (lab != kEmptyLabel) h.add((int)lab, v);
+        });
+    }
+    template <class H>
+    __device__ __forceinline__ void deferred(float, float, float, const H&) const {}
+};
+
+// Tiered canvas, canvas form: every point adds to its block's sums (merged
+// per warp); points of mixed blocks also to their pixel in the block's slot.
+struct TierSplatMapper {
+    static constexpr bool kDefer = false;
+    static constexpr bool kTwoPhase = true;
+    CanvasXf cx;
+    TierArgs tr;
+    float scale;
+    using Key = uint32_t;                               // pixel index in the tile
+    static constexpr Key kNone = 0xFFFFFFFFu;
+    static constexpr Key kMulti = 0xFFFFFFFEu;
+    __device__ __forceinline__ Key lookup(float x, float y) const {
+        if (cx.splitx != 1 || cx.splity != 1) return kMulti;
+        float wx = win_coord(x, cx.col0.x, cx.col0.y, cx.col0.z);
+        float wy = win_coord(y, cx.row0.x, cx.row0.y, cx.row0.z);
+        if (!(wx > -1.0f && wx < (float)cx.resx + 1.0f && wy > -1.0f && wy < (float)cx.resy + 1.0f)) return kNone;
+        int px = pix_of(snap_win(wx)), py = pix_of(snap_win(wy));
+        if (px < 0 || px >= cx.resx || py < 0 || py >= cx.resy) return kNone;
+        return (Key)py * (Key)cx.resx + (Key)px;
+    }
+    __device__ __forceinline__ void pixel_add(size_t blk0, int px, int py, long long q) const {
+        const uint32_t code = __ldg(tr.code + blk0 + (size_t)(py >> 4) * tr.bw + (px >> 4));
+        if ((code & kTierMixed) && code < kTierMulti) {
+            const size_t at = (size_t)(code & ~kTierMixed) * 256 + (size_t)(py & 15) * 16 + (px & 15);
+            atomicAdd(tr.pcnt + at, 1u);
+            if (tr.psum) atomicAdd(reinterpret_cast<unsigned long long*>(tr.psum + at), (unsigned long long)q);
+        }
+    }
+    template <class H>
+    __device__ __forceinline__ void consume(bool valid, Key k, float x, float y, float v, const H& h,
+                                            const DeferQ& dq) const {
+        const bool one = valid && k < kMulti;
+        const unsigned active = __ballot_sync(0xffffffffu, one);
+        if (one) {
+            const long long q = (tr.bsum && isfinite(v)) ? fixed_value(v, scale) : 0ll;
+            const int px = (int)(k % (Key)cx.resx), py = (int)(k / (Key)cx.resx);
+            const uint32_t b = (uint32_t)((py >> 4) * tr.bw + (px >> 4));
+            const unsigned peers = __match_any_sync(active, b);
+            const long long sum = group_sum(active, peers, q);
+            if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) {
+                atomicAdd(tr.bcnt + b, (unsigned)__popc(peers));
+                if (tr.bsum) atomicAdd(reinterpret_cast<unsigned long long*>(tr.bsum + b), (unsigned long long)sum);
+            }
+            pixel_add(0, px, py, q);
+        }
+        if (valid && k == kMulti) map(x, y, v, h, dq);
+    }
+    template <class H>
+    __device__ __forceinline__ void map(float x, float y, float v, const H&, const DeferQ&) const {
+        const size_t tile_blk = (size_t)tr.bw * tr.bh;
+        const long long q = (tr.bsum && isfinite(v)) ? fixed_value(v, scale) : 0ll;
+        canvas_visit(cx, x, y, [&](int t, int px, int py) {
+            const size_t blk0 = (size_t)t * tile_blk;
+            const size_t b = blk0 + (size_t)(py >> 4) * tr.bw + (px >> 4);
+            atomicAdd(tr.bcnt + b, 1u);
+            if (tr.bsum) atomicAdd(reinterpret_cast<unsigned long long*>(tr.bsum + b), (unsigned long long)q);
+            pixel_add(blk0, px, py, q);
+        });
+    }
+    template <class H>
+    __device__ __forceinline__ void deferred(float, float, float, const H&) const {}
+};
 
 }  // namespace rj

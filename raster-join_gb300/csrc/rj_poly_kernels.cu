@@ -200,6 +200,7 @@ __global__ void k_poly_info(PolyPassArgs a) {
             }
             r_lo = max(r_lo, 0);
             r_hi = min(r_hi, a.resy - 1);
+            if (MODE >= MODE_TIER_CLASSIFY) r_lo &= ~15;   // bands on block rows
             i_lo = max(i_lo, 0);
             i_hi = min(i_hi, a.resx - 1);
             if (r_lo <= r_hi && (MODE == MODE_BOUNDS || i_lo <= i_hi)) {
@@ -921,6 +922,7 @@ void launch_poly_info(int mode, const PolyPassArgs& a, int sms, cudaStream_t st)
     if (blocks < 1) blocks = 1;
     ++g_kernel_launches;
     if (mode == MODE_BOUNDS) k_poly_info<MODE_BOUNDS><<<blocks, 256, 0, st>>>(a);
+    else if (mode >= MODE_TIER_CLASSIFY) k_poly_info<MODE_TIER_CLASSIFY><<<blocks, 256, 0, st>>>(a);
     else k_poly_info<MODE_REDUCE><<<blocks, 256, 0, st>>>(a);
 }
 

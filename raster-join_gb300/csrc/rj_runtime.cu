@@ -25,6 +25,7 @@ using namespace rj;
 
 namespace rjh {
 
+
 int fail(rj_ctx* c, int code, const char* fmt, ...) {
     char buf[512];
     va_list ap;
@@ -553,6 +554,11 @@ PointArgs make_point_args(rj_ctx* ctx, const DevFilter& f, unsigned long long* o
     pa.out_sum = os;
     pa.out_nonfinite = (double*)ctx->scratch["out_nonfinite"].p;
     pa.err = ctx->d_err;
+    if (ctx->zones_valid && !ctx->streamed) {
+        pa.zones = (const float4*)ctx->zones.p;
+        pa.row0 = r0;
+        pa.qbox = ctx->qbox;
+    }
     return pa;
 }
 
@@ -659,7 +665,7 @@ struct ExecState {
     int passes = 1;
 };
 
-int poly_pass(rj_ctx* ctx, int mode, PolyPassArgs& a) {
+int poly_pass(rj_ctx* ctx, int mode, PolyPassArgs& a, const TierArgs* tier = nullptr) {
     unsigned int* ctr;
     int rc;
     const int TP = a.T * a.P;
@@ -681,8 +687,90 @@ int poly_pass(rj_ctx* ctx, int mode, PolyPassArgs& a) {
     launch_poly_info(mode, a, ctx->sms, ctx->stream);
     if (!launch_exclusive_scan(nbands, band_start, TP, tmp, ctx->stream))
         return fail(ctx, RJ_E_INVALID, "too many (tile, polygon) items");
-    launch_poly_pass(mode, a, ctx->sms, ctx->stream);
+    if (tier) launch_tier_pass(mode, a, *tier, ctx->sms, ctx->stream);
+    else launch_poly_pass(mode, a, ctx->sms, ctx->stream);
     RJ_CUDA(cudaGetLastError());
+    return RJ_OK;
+}
+
+// Tiered canvas of a large raster canvas: classification of 16 x 16 blocks,
+// then the label form (disjoint coverage) or the canvas form.  Results equal
+// the flat canvas's; polygon-side work follows the perimeters.
+int exec_raster_tier(rj_ctx* ctx, const rj_query* q, const RasterPlan& rp, const DevFilter& f, ExecState& es,
+                     PolyPassArgs& a, const CanvasXf& cx, uint64_t ckey) {
+    int rc;
+    TierArgs tr{};
+    tr.bw = (rp.resx + 15) / 16;
+    tr.bh = (rp.resy + 15) / 16;
+    const size_t nblk = (size_t)a.T * tr.bw * tr.bh;
+    if (nblk >= (size_t)1 << 24) return fail(ctx, RJ_E_UNSUPPORTED, "canvas too large for the tiered form");
+    int* slot;
+    int* tmp;
+    unsigned long long* cnt;   // multi blocks, covered pixel writes, labelled pixels
+    if ((rc = scratch_t(ctx, "tier_full", nblk, &tr.full))) return rc;
+    if ((rc = scratch_t(ctx, "tier_mixed", nblk, &tr.mixed))) return rc;
+    if ((rc = scratch_t(ctx, "tier_slot", nblk + 1, &slot))) return rc;
+    if ((rc = scratch_t(ctx, "tier_code", nblk, &tr.code))) return rc;
+    if ((rc = scratch_t(ctx, "tier_tmp", (size_t)scan_tmp_ints((int)nblk), &tmp))) return rc;
+    if ((rc = scratch_t(ctx, "tier_cnt", 3, &cnt))) return rc;
+    tr.slot = slot;
+    RJ_CUDA(cudaMemsetAsync(tr.full, 0xFF, nblk * 4, ctx->stream));
+    RJ_CUDA(cudaMemsetAsync(tr.mixed, 0, nblk * 4, ctx->stream));
+    RJ_CUDA(cudaMemsetAsync(cnt, 0, 3 * 8, ctx->stream));
+    if ((rc = poly_pass(ctx, MODE_TIER_CLASSIFY, a, &tr))) return rc;
+    if (!launch_exclusive_scan((const int*)tr.mixed, slot, (int)nblk, tmp, ctx->stream))
+        return fail(ctx, RJ_E_INVALID, "tier scan failed");
+    launch_tier_codes(tr, nblk, cnt, ctx->sms, ctx->stream);
+    int nslots = 0;
+    RJ_CUDA(cudaMemcpyAsync(&nslots, slot + nblk, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    const size_t spx = (size_t)std::max(nslots, 1) * 256;
+    bool label = !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->ps->overlap_on(ckey) != 1 && ctx->ps->P <= kMaxLabelPolys;
+    if (label) {
+        if ((rc = scratch_t(ctx, "tier_plabel", spx, &tr.plabel))) return rc;
+        RJ_CUDA(cudaMemsetAsync(tr.plabel, 0xFF, spx * 2, ctx->stream));
+        a.covered = cnt + 1;
+        if ((rc = poly_pass(ctx, MODE_TIER_LABEL, a, &tr))) return rc;
+        if (ctx->ps->overlap_on(ckey) == -1) {
+            launch_tier_nonempty(tr.plabel, (size_t)nslots * 256, cnt + 2, ctx->sms, ctx->stream);
+            unsigned long long hc[3] = {0, 0, 0};
+            RJ_CUDA(cudaMemcpyAsync(hc, cnt, sizeof hc, cudaMemcpyDeviceToHost, ctx->stream));
+            RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+            ctx->ps->overlap[ckey] = (hc[0] != 0 || hc[1] != hc[2]) ? 1 : 0;
+        }
+        label = ctx->ps->overlap_on(ckey) == 0;
+    }
+    es.ph->mark(2);
+    if (label) {
+        if ((rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
+                 launch_tier_label_points(pa, cx, tr, ctx->sms, ctx->stream);
+             })))
+            return rc;
+        es.ph->mark(3);
+        es.ph->mark(4);
+        return RJ_OK;
+    }
+    // canvas form: block sums + pixel canvases of the mixed blocks
+    if ((rc = scratch_t(ctx, "tier_bcnt", nblk, &tr.bcnt))) return rc;
+    if ((rc = scratch_t(ctx, "tier_pcnt", spx, &tr.pcnt))) return rc;
+    RJ_CUDA(cudaMemsetAsync(tr.bcnt, 0, nblk * 4, ctx->stream));
+    RJ_CUDA(cudaMemsetAsync(tr.pcnt, 0, spx * 4, ctx->stream));
+    if (f.aggr) {
+        if ((rc = scratch_t(ctx, "tier_bsum", nblk, &tr.bsum))) return rc;
+        if ((rc = scratch_t(ctx, "tier_psum", spx, &tr.psum))) return rc;
+        RJ_CUDA(cudaMemsetAsync(tr.bsum, 0, nblk * 8, ctx->stream));
+        RJ_CUDA(cudaMemsetAsync(tr.psum, 0, spx * 8, ctx->stream));
+    }
+    if ((rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
+             launch_tier_splat_points(pa, cx, tr, ctx->sms, ctx->stream);
+         })))
+        return rc;
+    es.ph->mark(3);
+    a.canvas_c = nullptr;
+    a.canvas_s = nullptr;
+    a.label = nullptr;
+    if ((rc = poly_pass(ctx, MODE_TIER_REDUCE, a, &tr))) return rc;
+    es.ph->mark(4);
     return RJ_OK;
 }
 
@@ -729,6 +817,12 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
     const int T = rp.splitx * rp.splity;
     const size_t tile_px = (size_t)rp.resx * rp.resy;
     const size_t npix = tile_px * T;
+    {
+        // canvas plus two pixels: locations outside reach no pixel of any tile
+        const double* bb = ctx->ps->bbox;
+        const double mx = 2.0 * (bb[2] - bb[0]) / rp.actual_x + 1e-3, my = 2.0 * (bb[3] - bb[1]) / rp.actual_y + 1e-3;
+        ctx->qbox = make_float4((float)(bb[0] - mx), (float)(bb[1] - my), (float)(bb[2] + mx), (float)(bb[3] + my));
+    }
 
     es.ph->mark(1);
     int2* wv;
@@ -753,6 +847,8 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
     a.line_filter = (q->flags & RJ_FLAG_LINE_FILTER) ? 1 : 0;
 
     const uint64_t ckey = canvas_key(rp.colxf, rp.rowxf, rp.resx, rp.resy);
+    if (!bounds && npix >= kTierMinPixels && !(q->flags & RJ_FLAG_FLAT_CANVAS))
+        return exec_raster_tier(ctx, q, rp, f, es, a, cx, ckey);
     bool use_label = !bounds && !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->ps->overlap_on(ckey) != 1 &&
                      ctx->ps->P <= kMaxLabelPolys;
     if (use_label) {
@@ -799,8 +895,17 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
 // Index join (IndexJoin::performJoin IndexJoin.cpp:156-166).  Default: the
 // classified grid; RJ_FLAG_NO_CELL_CLASSIFY / RJ_FLAG_COMPAT_INDEX_CLAMP: the
 // plain candidate lists with the full crossing test per candidate.
+// Locations that can lie inside a polygon of the set: its bounds plus a
+// margin far above the fp32 rounding of the crossing test.
+void exact_qbox(rj_ctx* ctx) {
+    const double* bb = ctx->ps->bbox;
+    const double m = 1e-4 * std::max(bb[2] - bb[0], bb[3] - bb[1]) + 1e-3;
+    ctx->qbox = make_float4((float)(bb[0] - m), (float)(bb[1] - m), (float)(bb[2] + m), (float)(bb[3] + m));
+}
+
 int exec_index(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     int rc;
+    exact_qbox(ctx);
     DevFilter f;
     if ((rc = build_filter(ctx, q, f, false))) return rc;
     if (q->grid_res <= 0 || q->grid_res > 8192) return fail(ctx, RJ_E_INVALID, "grid resolution %d out of range", q->grid_res);
@@ -835,6 +940,7 @@ int exec_index(rj_ctx* ctx, const rj_query* q, ExecState& es) {
 // test through the grid.
 int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     int rc;
+    exact_qbox(ctx);
     DevFilter f;
     if ((rc = build_filter(ctx, q, f, false))) return rc;
     if (q->grid_res <= 0 || q->grid_res > 8192) return fail(ctx, RJ_E_INVALID, "grid resolution %d out of range", q->grid_res);
@@ -1131,6 +1237,7 @@ void rj_destroy(rj_ctx* ctx) {
     free_batch_engine(ctx);
     free_points(ctx);
     for (auto& b : ctx->sbuf) dev_free(ctx, b);
+    dev_free(ctx, ctx->zones);
     if (ctx->copy_stream) {
         cudaStreamSynchronize(ctx->copy_stream);
         cudaStreamDestroy(ctx->copy_stream);
@@ -1243,6 +1350,7 @@ static int load_points_impl(rj_ctx* ctx, const rj_column* cols, int32_t ncols, u
     if (ctx->server_running) return fail(ctx, RJ_E_BUSY, "a serving loop owns the context");
     cudaSetDevice(ctx->device);
     ctx->tix.valid = false;
+    ctx->zones_valid = false;
     const bool was_streamed = ctx->streamed;
     ctx->streamed = false;
     // same layout as the resident table: copy into the existing buffers
@@ -1339,6 +1447,7 @@ int rj_free_points(rj_ctx* ctx) {
     std::lock_guard<std::recursive_mutex> lock(ctx->mu);
     if (ctx->server_running) return fail(ctx, RJ_E_BUSY, "a serving loop owns the context");
     ctx->tix.valid = false;
+    ctx->zones_valid = false;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (Column& c : ctx->cols) {
@@ -1387,6 +1496,16 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
         ctx->cache_version = ctx->ps->version;
     }
     query_rows(ctx, q, ctx->row0, ctx->row1);
+    bool owned_all = !ctx->streamed;
+    for (const Column& c : ctx->cols) owned_all = owned_all && c.owned;
+    if (!owned_all) ctx->zones_valid = false;   // caller-held columns may change between calls
+    if (!ctx->zones_valid && owned_all && ctx->npts > 0) {
+        const uint64_t nz = (ctx->npts + (1ull << kZoneShift) - 1) >> kZoneShift;
+        if ((rc = dev_alloc(ctx, ctx->zones, nz * sizeof(float4)))) return rc;
+        launch_zone_boxes((const float2*)find_col(ctx, ctx->loc_attrib)->d, ctx->npts, (float4*)ctx->zones.p, ctx->sms,
+                          ctx->stream);
+        ctx->zones_valid = true;
+    }
     if (q->flags & RJ_FLAG_NO_CACHE) {
         ctx->ps->grid.valid = false;
         ctx->ps->exact.valid = false;

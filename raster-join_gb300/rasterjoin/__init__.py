@@ -44,6 +44,7 @@ FLAG_FORCE_CANVAS = 0x8
 FLAG_PHASE_TIMING = 0x10
 FLAG_NO_CELL_CLASSIFY = 0x20
 FLAG_NO_CACHE = 0x40
+FLAG_FLAT_CANVAS = 0x80
 
 
 class RJError(RuntimeError):
@@ -98,7 +99,8 @@ class BatchStats(C.Structure):
                 ("items", C.c_uint64), ("rows_read", C.c_uint64), ("point_queries", C.c_uint64),
                 ("total_ms", C.c_double), ("setup_ms", C.c_double), ("poly_ms", C.c_double),
                 ("point_ms", C.c_double), ("reduce_ms", C.c_double), ("threads", C.c_int32),
-                ("rows_per_item", C.c_int32), ("tuned", C.c_int32), ("kernel_launches", C.c_int32)]
+                ("rows_per_item", C.c_int32), ("direct", C.c_int32), ("tuned", C.c_int32),
+                ("kernel_launches", C.c_int32)]
 
 
 class ServerConfig(C.Structure):
@@ -143,6 +145,7 @@ def load_library(path=LIB_PATH):
         "rj_polyset_destroy": (None, [C.c_void_p]),
         "rj_use_polyset": (C.c_int, [C.c_void_p, C.c_void_p]),
         "rj_build_time_index": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+        "rj_cluster_points": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
         "rj_execute_batch": (C.c_int, [C.c_void_p, C.c_int32, P(Query), P(C.c_void_p), P(Result), P(C.c_int32),
                                        C.c_uint32, P(BatchStats)]),
         "rj_server_create": (C.c_int, [C.c_void_p, P(ServerConfig), P(C.c_void_p)]),
@@ -525,6 +528,14 @@ class GLHandler:
                                                  and self._loaded_points[:1] == ("device",)):
             self.upload()
         self._check(self.lib.rj_build_time_index(self.ctx, attrib_id, nbuckets))
+
+    def clusterPoints(self, time_attrib=-1, nbuckets=0, cell_bits=8):
+        """Reorder the resident table by (time bucket, Z-order cell); with a
+        time attribute this also builds the time index."""
+        if self.dataHandler is not None and not (isinstance(self._loaded_points, tuple)
+                                                 and self._loaded_points[:1] == ("device",)):
+            self.upload()
+        self._check(self.lib.rj_cluster_points(self.ctx, time_attrib, nbuckets, cell_bits))
 
     def execute_batch(self, queries, polysets, flags=0, raise_on_error=True):
         """Run queries[i] on polysets[i] (None: the handler's polygons) in one

@@ -225,3 +225,41 @@ def test_server_rejects_context_calls_while_running(setup):
         assert e.value.code == -8
     finally:
         srv.close()
+
+
+@pytest.mark.parametrize("time_attrib,nb,bits", [(2, 512, 6), (-1, 0, 8)])
+def test_clustered_order_preserves_results(table, built, time_attrib, nb, bits):
+    """Rows ordered by (time bucket, Z-order cell) or by cell alone: every
+    join returns what it returned on the original order, and batches too."""
+    v, p = synth.voronoi_polygons(260, seed=3)
+    sv, sp = synth.star_polygons(40, seed=12, vmin=8, vmax=200, rmin=300, rmax=5000)
+    h = rj.GLHandler()
+    try:
+        h.setDataHandler(make_dh(table, v, p))
+        cases = [(fn, make_query(25.0, aggr=True, window=w, fn=fn)) for fn in
+                 (rj.RasterJoinFn, rj.IndexJoinFn, rj.HybridJoinFn, rj.RasterJoinBoundFn)
+                 for w in ((T0 + 10 * DAY, T0 + 11 * DAY), None)]
+        before = []
+        for fn, q in cases:
+            r = h.execute(fn, query=q)
+            before.append((r.count.copy(), r.sum.copy(), None if r.bounds is None else r.bounds.copy()))
+        stars = h.polyset(sv, sp)
+        mix = [make_query(12.0, aggr=True, window=(T0, T0 + 90 * DAY)), make_query(30.0),
+               make_query(60.0, aggr=True, preds=((4, rj.GT, 4),))]
+        bres, _, _ = h.execute_batch(mix, [stars] * len(mix))
+        b_before = [(r.count.copy(), r.sum.copy()) for r in bres]
+        h.clusterPoints(time_attrib, nb, bits)
+        for (fn, q), (c, s, b) in zip(cases, before):
+            r = h.execute(fn, query=q)
+            np.testing.assert_array_equal(r.count, c)
+            np.testing.assert_array_equal(r.sum, s)
+            if b is not None:
+                np.testing.assert_array_equal(r.bounds, b)
+        bres, status, _ = h.execute_batch(mix, [stars] * len(mix))
+        assert (status == 0).all()
+        for r, (c, s) in zip(bres, b_before):
+            np.testing.assert_array_equal(r.count, c)
+            np.testing.assert_array_equal(r.sum, s)
+        stars.close()
+    finally:
+        h.close()

@@ -518,3 +518,54 @@ def test_streamed_host_table_matches_resident(c1, fn, built):
     for a, b in zip(res["resident"], res["streamed"]):
         if a is not None:
             np.testing.assert_array_equal(a, b)
+
+
+def _raster(handler, cell, flags=0, max_fbo=8192):
+    handler.setCellSize(cell)
+    handler.flags = flags
+    handler.max_fbo_size = max_fbo
+    try:
+        r = handler.execute(rj.RasterJoinFn)
+        return r.count.copy(), r.sum.copy()
+    finally:
+        handler.flags = 0
+        handler.max_fbo_size = 8192
+
+
+def test_tiered_label_canvas_matches_flat_and_oracle(handler, c1):
+    """64M-pixel canvas (cell 5 m): 16 x 16 block tiers in the label form give
+    the flat canvas's and the oracle's results."""
+    pts, verts, pidx = c1
+    dh = make_dh(pts, verts, pidx)
+    c2_query(dh)
+    handler.setDataHandler(dh)
+    tier = _raster(handler, 5.0)
+    flat = _raster(handler, 5.0, rj.FLAG_FLAT_CANVAS)
+    np.testing.assert_array_equal(tier[0], flat[0])
+    np.testing.assert_array_equal(tier[1], flat[1])
+    want = oracle.raster_join(pts["xy"], verts, pidx, 5.0, f=c2_filter(pts))
+    np.testing.assert_array_equal(tier[0], want[0])
+    check_sums(tier[1], want[1])
+
+
+def test_tiered_canvas_form_overlapping_stars(handler, stars):
+    """Overlapping polygons on a 100M-pixel canvas: block sums for full blocks,
+    pixel canvases for mixed ones; identical to the flat canvas."""
+    pts, verts, pidx = stars
+    dh = make_dh(pts, verts, pidx)
+    dh.setAggregation(rj.Avg, 3)
+    handler.setDataHandler(dh)
+    tier = _raster(handler, 4.0)
+    flat = _raster(handler, 4.0, rj.FLAG_FLAT_CANVAS)
+    np.testing.assert_array_equal(tier[0], flat[0])
+    np.testing.assert_array_equal(tier[1], flat[1])
+    assert tier[0].sum() > 0
+
+
+def test_tiered_multi_tile_matches_flat(handler, c1):
+    """3 x 3 tiles of 5334^2 pixels, label form, against the flat canvas."""
+    pts, verts, pidx = c1
+    handler.setDataHandler(make_dh(pts, verts, pidx))
+    tier = _raster(handler, 2.5, max_fbo=6000)
+    flat = _raster(handler, 2.5, rj.FLAG_FLAT_CANVAS, max_fbo=6000)
+    np.testing.assert_array_equal(tier[0], flat[0])
