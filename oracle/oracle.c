@@ -817,6 +817,85 @@ int orc_raster_join(const float *xy, uint64_t n, const orc_filter *f, const floa
 }
 
 /* Canvas geometry as the raster join plans it, for tests. */
+/* Fill-rule cross-check (single-tile canvas).  For every pixel centre:
+ * poly_cover = id of the one polygon covering it by the crossing rule the
+ * library implements, -1 if none, -2 if several; tri_cover = the same from
+ * triangles (tri_poly[k] = polygon of triangle k) by GL's rule on the same
+ * snapped window coordinates: a centre is inside a counter-clockwise triangle
+ * when every edge function is positive, or zero on a left edge (going down)
+ * or a top edge (horizontal, going left).  Triangle vertices pass through
+ * float as the reference uploads them (PolyHandler::getTriangulation). */
+int orc_cover_maps(const float *verts, const int *pindex, int P, const double *tris, const int *tri_poly, int ntri,
+                   const double *bbox, double cell, int32_t *poly_cover, int32_t *tri_cover, int *dims) {
+    orc_axis ax, ay;
+    axis_plan(&ax, bbox[0], bbox[2], cell, 1 << 30);
+    axis_plan(&ay, bbox[1], bbox[3], cell, 1 << 30);
+    const int rx = ax.res, ry = ay.res;
+    dims[0] = rx;
+    dims[1] = ry;
+    for (size_t k = 0; k < (size_t)rx * ry; ++k) { poly_cover[k] = -1; tri_cover[k] = -1; }
+    const int V = pindex[P];
+    int32_t *wx = (int32_t *)malloc(sizeof(int32_t) * (size_t)V), *wy = (int32_t *)malloc(sizeof(int32_t) * (size_t)V);
+    for (int k = 0; k < V; ++k) {
+        wx[k] = snapw(win(verts[2 * k], ax.s[0], ax.t[0], ax.h));
+        wy[k] = snapw(win(verts[2 * k + 1], ay.s[0], ay.t[0], ay.h));
+    }
+    for (int p = 0; p < P; ++p) {
+        int v0 = pindex[p], nv = pindex[p + 1] - v0;
+        if (nv < 2) continue;
+        for (int j = 0; j < ry; ++j)
+            for (int i = 0; i < rx; ++i)
+                if (covers(wx + v0, wy + v0, nv, i, j)) {
+                    int32_t *c = poly_cover + (size_t)j * rx + i;
+                    *c = (*c == -1) ? p : -2;
+                }
+    }
+    for (int k = 0; k < ntri; ++k) {
+        int64_t X[3], Y[3];
+        for (int q = 0; q < 3; ++q) {
+            X[q] = snapw(win((float)tris[6 * k + 2 * q], ax.s[0], ax.t[0], ax.h));
+            Y[q] = snapw(win((float)tris[6 * k + 2 * q + 1], ay.s[0], ay.t[0], ay.h));
+        }
+        int64_t area = (X[1] - X[0]) * (Y[2] - Y[0]) - (X[2] - X[0]) * (Y[1] - Y[0]);
+        if (area == 0) continue;
+        if (area < 0) { int64_t t = X[1]; X[1] = X[2]; X[2] = t; t = Y[1]; Y[1] = Y[2]; Y[2] = t; }
+        int64_t mnx = X[0], mxx = X[0], mny = Y[0], mxy = Y[0];
+        for (int q = 1; q < 3; ++q) {
+            if (X[q] < mnx) mnx = X[q];
+            if (X[q] > mxx) mxx = X[q];
+            if (Y[q] < mny) mny = Y[q];
+            if (Y[q] > mxy) mxy = Y[q];
+        }
+        int i0 = floor256((int32_t)mnx) - 1, i1 = floor256((int32_t)mxx) + 1;
+        int j0 = floor256((int32_t)mny) - 1, j1 = floor256((int32_t)mxy) + 1;
+        if (i0 < 0) i0 = 0;
+        if (j0 < 0) j0 = 0;
+        if (i1 > rx - 1) i1 = rx - 1;
+        if (j1 > ry - 1) j1 = ry - 1;
+        for (int j = j0; j <= j1; ++j)
+            for (int i = i0; i <= i1; ++i) {
+                const int64_t cx = (int64_t)i * SUB + SUB / 2, cy = (int64_t)j * SUB + SUB / 2;
+                int in = 1;
+                for (int e = 0; e < 3 && in; ++e) {
+                    const int64_t ax0 = X[e], ay0 = Y[e], bx0 = X[(e + 1) % 3], by0 = Y[(e + 1) % 3];
+                    const int64_t f = (bx0 - ax0) * (cy - ay0) - (by0 - ay0) * (cx - ax0);
+                    const int left = (by0 < ay0), top = (by0 == ay0 && bx0 < ax0);
+                    if (f < 0 || (f == 0 && !(left || top))) in = 0;
+                }
+                if (in) {
+                    int32_t *c = tri_cover + (size_t)j * rx + i;
+                    const int p = tri_poly[k];
+                    *c = (*c == -1 || *c == p) ? p : -2;
+                }
+            }
+    }
+    free(wx);
+    free(wy);
+    axis_free(&ax);
+    axis_free(&ay);
+    return 0;
+}
+
 void orc_raster_geometry(const double *bbox, double cell, int max_res, int *out /* splitx, splity, resx, resy */) {
     orc_axis ax, ay;
     axis_plan(&ax, bbox[0], bbox[2], cell, max_res);

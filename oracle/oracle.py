@@ -57,6 +57,8 @@ def lib():
         L.orc_raster_join.restype = C.c_int
         L.orc_raster_geometry.argtypes = [dp, C.c_double, C.c_int, ip]
         L.orc_raster_geometry.restype = None
+        L.orc_cover_maps.argtypes = [fp, ip, C.c_int, dp, ip, C.c_int, dp, C.c_double, P(C.c_int32), P(C.c_int32), ip]
+        L.orc_cover_maps.restype = C.c_int
         _lib = L
     return _lib
 
@@ -199,6 +201,26 @@ def raster_join(xy, verts, pindex, cell, f=None, bbox=None, max_res=8192, bounds
     if rc != 0:
         raise MemoryError("oracle raster canvas allocation failed")
     return cnt, s, b
+
+
+def cover_maps(verts, pindex, tris, tri_poly, bbox, cell):
+    """Per-pixel coverage of a single-tile canvas by the polygon crossing rule
+    and by GL's triangle rule (fill-rule cross-check); returns two int32 maps
+    (polygon id, -1 none, -2 several)."""
+    verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 2)
+    pindex = np.ascontiguousarray(pindex, np.int32)
+    tris = np.ascontiguousarray(tris, np.float64).reshape(-1, 6)
+    tri_poly = np.ascontiguousarray(tri_poly, np.int32)
+    bbox = np.ascontiguousarray(bbox, np.float64)
+    geo = raster_geometry(bbox, cell, 1 << 30)
+    rx, ry = geo[2], geo[3]
+    a = np.empty(rx * ry, np.int32)
+    b = np.empty(rx * ry, np.int32)
+    dims = np.zeros(2, np.int32)
+    lib().orc_cover_maps(_ptr(verts, C.c_float), _ptr(pindex, C.c_int), len(pindex) - 1, _ptr(tris, C.c_double),
+                         _ptr(tri_poly, C.c_int), len(tri_poly), _ptr(bbox, C.c_double), float(cell),
+                         _ptr(a, C.c_int32), _ptr(b, C.c_int32), _ptr(dims, C.c_int))
+    return a.reshape(ry, rx), b.reshape(ry, rx)
 
 
 def raster_geometry(bbox, cell, max_res=8192):

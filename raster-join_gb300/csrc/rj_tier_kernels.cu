@@ -364,11 +364,8 @@ size_t tier_smem_bytes() { return kTierSmem; }
 void launch_tier_pass(int mode, const PolyPassArgs& a, const TierArgs& tr, int sms, cudaStream_t st) {
     ++g_kernel_launches;
     auto go = [&](auto kernel) {
-        static bool set = false;
-        if (!set) {
-            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTierSmem);
-            set = true;
-        }
+        // every instance needs the opt-in (the three kernels share one pointer type)
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTierSmem);
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTW * 32, kTierSmem);
         kernel<<<sms * std::max(per_sm, 1), kTW * 32, kTierSmem, st>>>(a, tr);
