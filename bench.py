@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--batch-queries", type=int, default=512)
     ap.add_argument("--served-requests", type=int, default=2000)
     ap.add_argument("--served-qps", type=float, default=500.0)
+    ap.add_argument("--saturate-qps", type=float, default=5000.0,
+                    help="offered rate of the saturation run of the served configuration (0: skip)")
+    ap.add_argument("--saturate-requests", type=int, default=4000)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--cluster", action="store_true",
@@ -291,9 +294,9 @@ def run_batched(rj, h, cum, n, nq):
     }
 
 
-def run_served(rj, h, cum, n, nreq, qps):
+def run_served(rj, h, cum, n, nreq, qps, seed=20261205):
     from rasterjoin import workloads as W
-    reqs = W.served_requests(nreq, qps)
+    reqs = W.served_requests(nreq, qps, seed=seed)
     rows = [window_rows(cum, *r[4]) for r in reqs]
     qs = [make_raster_query(rj, cell, win, False) for _, _, _, cell, win in reqs]
     # ---- plain: one request at a time through rj_execute, FIFO
@@ -540,6 +543,18 @@ def run_gb300(args):
             line["batched"] = run_batched(rj, h2, cum, args.table_points, args.batch_queries)
         if not args.no_served:
             line["served"] = run_served(rj, h2, cum, args.table_points, args.served_requests, args.served_qps)
+            if args.saturate_qps > 0:
+                sat = run_served(rj, h2, cum, args.table_points, args.saturate_requests, args.saturate_qps,
+                                 seed=20261207)
+                line["served_saturated"] = {
+                    "offered_qps": args.saturate_qps, "achieved_qps": sat["achieved_qps"],
+                    "plain_max_qps": sat["plain"]["max_qps"],
+                    "throughput_vs_plain": sat["achieved_qps"] / sat["plain"]["max_qps"],
+                    "p50_ms": sat["p50_ms"], "p99_ms": sat["p99_ms"], "mean_batch": sat["mean_batch"],
+                    "gpoints_s": sat["gpoints_s"],
+                    "plain_p99_ms": sat["plain"]["p99_ms"],
+                    "note": "requests offered faster than either path serves them; achieved_qps is the "
+                            "served path's throughput, plain_max_qps = 1 / mean single-request service time"}
         h2.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -121,6 +121,13 @@ struct QPlan {
     size_t npix = 0;
     bool check_overlap = false;
     uint64_t canvas = 0;         // canvas geometry (overlap status is per canvas)
+    bool tier = false;           // tiered canvas (16 x 16 blocks)
+    TierArgs tr{};
+    size_t nblk = 0;             // blocks of the tiered canvas
+    size_t est_slots = 0;        // upper bound on its mixed blocks
+    int nslots = 0;
+    int* slot_buf = nullptr;
+    int* scan_tmp = nullptr;
     size_t out_off = 0;          // first polygon of the query in the output block
     uint16_t* label = nullptr;
     uint32_t* cc = nullptr;
@@ -129,8 +136,20 @@ struct QPlan {
     float4* drow = nullptr;
 };
 
+// bytes of a tiered canvas's canvas form (block sums + slot pixels)
+size_t tier_canvas_bytes(const QPlan& p) {
+    const bool agg = p.f.aggr != 0;
+    return al256(p.nblk * 4) + (agg ? al256(p.nblk * 8) : 0) + al256(p.est_slots * 256 * 4) +
+           (agg ? al256(p.est_slots * 256 * 8) : 0);
+}
+
 size_t canvas_bytes(const QPlan& p) {
     const bool agg = p.f.aggr != 0;
+    if (p.tier) {
+        const size_t base = 4 * al256(p.nblk * 4) + al256((p.nblk + 1) * 4) +
+                            al256((size_t)scan_tmp_ints((int)std::max<size_t>(p.nblk, 1)) * 4);
+        return base + (p.mode == BQ_TLABEL ? al256(p.est_slots * 256 * 2) : tier_canvas_bytes(p));
+    }
     return p.mode == BQ_LABEL ? al256(p.npix * 2) : al256(p.npix * 4) + (agg ? al256(p.npix * 8) : 0);
 }
 
@@ -148,15 +167,27 @@ void plan_query(rj_ctx* ctx, QPlan& p, bool no_fuse) {
     if (p.f.general && !empty) return;                             // per-predicate filters: plain path
     p.T = p.rp.splitx * p.rp.splity;
     p.npix = (size_t)p.rp.resx * p.rp.resy * p.T;
-    // large canvases take the single-query path, whose tiered canvas does
-    // per-block work instead of per-pixel work
-    if (p.npix >= kTierMinPixels && !(q->flags & RJ_FLAG_FLAT_CANVAS)) return;
-    p.fused = true;
     query_rows(ctx, q, p.r0, p.r1);
     // row ranges on multiples of four rows (aligned 128-bit loads in the fused
     // pass); the rows added are outside the time window and fail its predicate
     p.r0 &= ~3ULL;
     p.r1 = std::min<uint64_t>(ctx->npts, (p.r1 + 3) & ~3ULL);
+    // large canvases: tiered form (per-block work instead of per-pixel work)
+    p.tier = use_tier(p.npix, p.r1 - p.r0) && !(q->flags & RJ_FLAG_FLAT_CANVAS);
+    if (p.tier) {
+        p.tr.bw = (p.rp.resx + 15) / 16;
+        p.tr.bh = (p.rp.resy + 15) / 16;
+        p.nblk = (size_t)p.T * p.tr.bw * p.tr.bh;
+        if (p.nblk >= (size_t)1 << 24) return;                     // single-query path
+        // mixed blocks lie on the edges (or the canvas border): blocks an edge
+        // passes are at most |dx| / 16 px + |dy| / 16 px + 3
+        const double pw = (p.ps->bbox[2] - p.ps->bbox[0]) / p.rp.splitx / p.rp.resx;
+        const double ph = (p.ps->bbox[3] - p.ps->bbox[1]) / p.rp.splity / p.rp.resy;
+        const double est = p.ps->sum_dx / (16.0 * pw) + p.ps->sum_dy / (16.0 * ph) + 3.0 * p.ps->V * p.T +
+                           2.0 * p.T * (p.tr.bw + p.tr.bh) + 64.0;
+        p.est_slots = (size_t)std::min<double>(est, (double)p.nblk);
+    }
+    p.fused = true;
     if (empty || p.r1 <= p.r0) {
         p.mode = BQ_SKIP;
         return;
@@ -164,8 +195,13 @@ void plan_query(rj_ctx* ctx, QPlan& p, bool no_fuse) {
     const bool label_ok = !(q->flags & RJ_FLAG_FORCE_CANVAS) && p.ps->P <= kMaxLabelPolys;
     p.canvas = canvas_key(p.rp.colxf, p.rp.rowxf, p.rp.resx, p.rp.resy);
     const int known = p.ps->overlap_on(p.canvas);
-    p.mode = (label_ok && known != 1) ? BQ_LABEL : BQ_SPLAT;
-    p.check_overlap = p.mode == BQ_LABEL && known != 0;
+    if (p.tier) {
+        p.mode = (label_ok && known != 1) ? BQ_TLABEL : BQ_TSPLAT;
+        p.check_overlap = p.mode == BQ_TLABEL && known != 0;
+    } else {
+        p.mode = (label_ok && known != 1) ? BQ_LABEL : BQ_SPLAT;
+        p.check_overlap = p.mode == BQ_LABEL && known != 0;
+    }
 }
 
 struct PolyScratch {
@@ -196,7 +232,7 @@ bool poly_scratch_take(Arena& ar, size_t TV, size_t TP, PolyScratch& s) {
 
 // Polygon pass of one query's canvas (label map or reduction).
 bool query_poly_pass(Engine& e, const QPlan& p, int mode, PolyScratch& s, unsigned long long* oc,
-                     unsigned long long* os, unsigned long long* covered) {
+                     unsigned long long* os, unsigned long long* covered, const TierArgs* tier = nullptr) {
     rj_ctx* ctx = e.ctx;
     const PolySet& ps = *p.ps;
     launch_transform_vertices((const float2*)ps.d_verts.p, ps.V, p.dcol, p.drow, p.rp.splitx, p.T, s.wv, nullptr,
@@ -209,8 +245,8 @@ bool query_poly_pass(Engine& e, const QPlan& p, int mode, PolyScratch& s, unsign
     a.T = p.T;
     a.resx = p.rp.resx;
     a.resy = p.rp.resy;
-    a.canvas_c = p.cc;
-    a.canvas_s = p.cs;
+    a.canvas_c = tier ? nullptr : p.cc;
+    a.canvas_s = tier ? nullptr : p.cs;
     a.label = mode == MODE_LABEL ? p.label : nullptr;
     a.covered = covered;
     a.out_count = oc;
@@ -223,7 +259,8 @@ bool query_poly_pass(Engine& e, const QPlan& p, int mode, PolyScratch& s, unsign
     cudaMemsetAsync(s.ctr, 0, sizeof(unsigned), e.st);
     launch_poly_info(mode, a, ctx->sms, e.st);
     if (!launch_exclusive_scan(s.nbands, s.band_start, a.T * a.P, s.tmp, e.st)) return false;
-    launch_poly_pass(mode, a, ctx->sms, e.st);
+    if (tier) launch_tier_pass(mode, a, *tier, ctx->sms, e.st);
+    else launch_poly_pass(mode, a, ctx->sms, e.st);
     return true;
 }
 
@@ -309,7 +346,8 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
             const size_t nouts = outs + p->ps->P, nxfs = xfs + p->rp.splitx + p->rp.splity;
             size_t cb = p->mode == BQ_SKIP ? 0 : canvas_bytes(*p);
             // a label query may need a canvas after the overlap check: reserve it
-            if (p->check_overlap) cb += al256(p->npix * 4) + (p->f.aggr ? al256(p->npix * 8) : 0);
+            if (p->check_overlap)
+                cb += p->tier ? tier_canvas_bytes(*p) : al256(p->npix * 4) + (p->f.aggr ? al256(p->npix * 8) : 0);
             const size_t fixed = poly_scratch_bytes(nmaxTV, nmaxTP) + 3 * al256(nouts * 8) + al256(nxfs * 16) +
                                  al256((wave.size() + 1) * 16) + al256((wave.size() + 1) * sizeof(BatchQuery)) +
                                  al256((wave.size() + 1) * 2 * 2 * sizeof(BatchSeg)) +
@@ -329,6 +367,7 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
         if (wave.empty()) break;
         const size_t nw = wave.size();
         const size_t total = poly_scratch_bytes(maxTV, maxTP) + 3 * al256(outs * 8) + al256(xfs * 16) + al256(nw * 16) +
+                             al256(nw * 24) +
                              al256(nw * sizeof(BatchQuery)) + al256(nw * 2 * 2 * sizeof(BatchSeg)) +
                              al256(nw * nw * 2 * 4 + 4) + need + 4096;
         if (e.ar.buf.bytes < total) {
@@ -344,9 +383,10 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
         double* onf = ar.take<double>(outs);
         float4* xf = ar.take<float4>(xfs);
         unsigned long long* lcnt = ar.take<unsigned long long>(2 * nw);
+        unsigned long long* tcnt = ar.take<unsigned long long>(3 * nw);   // tiered: multi, covered, labelled
         BatchQuery* dq = ar.take<BatchQuery>(nw);
         unsigned long long* work = ar.take<unsigned long long>(1);
-        if (!oc || !os || !onf || !xf || !lcnt || !dq || !work) return fail(ctx, RJ_E_OOM, "batch arena too small");
+        if (!oc || !os || !onf || !xf || !lcnt || !tcnt || !dq || !work) return fail(ctx, RJ_E_OOM, "batch arena too small");
         // placements + transforms
         std::vector<float4> hxf;
         hxf.reserve(xfs);
@@ -361,7 +401,31 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
             p->label = nullptr;
             p->cc = nullptr;
             p->cs = nullptr;
-            if (p->mode == BQ_LABEL) {
+            if (p->tier && p->mode != BQ_SKIP) {
+                TierArgs& tr = p->tr;
+                tr.full = ar.take<uint32_t>(p->nblk);
+                tr.mixed = ar.take<uint32_t>(p->nblk);
+                p->slot_buf = ar.take<int>(p->nblk + 1);
+                tr.slot = p->slot_buf;
+                tr.code = ar.take<uint32_t>(p->nblk);
+                p->scan_tmp = ar.take<int>((size_t)scan_tmp_ints((int)std::max<size_t>(p->nblk, 1)));
+                tr.plabel = nullptr;
+                tr.bcnt = tr.pcnt = nullptr;
+                tr.bsum = tr.psum = nullptr;
+                if (p->mode == BQ_TLABEL) {
+                    tr.plabel = ar.take<uint16_t>(p->est_slots * 256);
+                } else {
+                    tr.bcnt = ar.take<uint32_t>(p->nblk);
+                    tr.pcnt = ar.take<uint32_t>(p->est_slots * 256);
+                    if (p->f.aggr) {
+                        tr.bsum = ar.take<long long>(p->nblk);
+                        tr.psum = ar.take<long long>(p->est_slots * 256);
+                    }
+                }
+                if (!tr.full || !tr.mixed || !p->slot_buf || !tr.code || !p->scan_tmp ||
+                    (p->mode == BQ_TLABEL ? !tr.plabel : (!tr.bcnt || !tr.pcnt || (p->f.aggr && (!tr.bsum || !tr.psum)))))
+                    return fail(ctx, RJ_E_OOM, "batch arena too small for a tiered canvas");
+            } else if (p->mode == BQ_LABEL) {
                 p->label = ar.take<uint16_t>(p->npix);
             } else if (p->mode == BQ_SPLAT) {
                 p->cc = ar.take<uint32_t>(p->npix);
@@ -375,6 +439,44 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
         RJ_CUDA(cudaMemsetAsync(os, 0, outs * 8, st));
         RJ_CUDA(cudaMemsetAsync(onf, 0, outs * 8, st));
         RJ_CUDA(cudaMemsetAsync(lcnt, 0, 2 * nw * 8, st));
+        RJ_CUDA(cudaMemsetAsync(tcnt, 0, 3 * nw * 8, st));
+        // ---- tiered canvases: block classification, slots of the mixed blocks
+        bool any_tier = false;
+        for (size_t i = 0; i < nw; ++i) {
+            QPlan* p = wave[i];
+            if (!p->tier || p->mode == BQ_SKIP) continue;
+            any_tier = true;
+            RJ_CUDA(cudaMemsetAsync(p->tr.full, 0xFF, p->nblk * 4, st));
+            RJ_CUDA(cudaMemsetAsync(p->tr.mixed, 0, p->nblk * 4, st));
+            if (!query_poly_pass(e, *p, MODE_TIER_CLASSIFY, ps, nullptr, nullptr, nullptr, &p->tr))
+                return fail(ctx, RJ_E_INVALID, "too many (tile, polygon) items");
+            if (!launch_exclusive_scan((const int*)p->tr.mixed, p->slot_buf, (int)p->nblk, p->scan_tmp, st))
+                return fail(ctx, RJ_E_INVALID, "tier scan failed");
+            launch_tier_codes(p->tr, p->nblk, tcnt + 3 * i, ctx->sms, st);
+            RJ_CUDA(cudaMemcpyAsync(&p->nslots, p->slot_buf + p->nblk, sizeof(int), cudaMemcpyDeviceToHost, st));
+        }
+        if (any_tier) {
+            RJ_CUDA(cudaStreamSynchronize(st));
+            for (size_t i = 0; i < nw; ++i) {
+                QPlan* p = wave[i];
+                if (!p->tier || p->mode == BQ_SKIP) continue;
+                if ((size_t)p->nslots > p->est_slots)
+                    return fail(ctx, RJ_E_INVALID, "tiered canvas: %d mixed blocks above the bound %zu", p->nslots,
+                                p->est_slots);
+                const size_t spx = (size_t)p->nslots * 256;
+                if (p->mode == BQ_TLABEL) {
+                    RJ_CUDA(cudaMemsetAsync(p->tr.plabel, 0xFF, std::max<size_t>(spx, 1) * 2, st));
+                    if (!query_poly_pass(e, *p, MODE_TIER_LABEL, ps, nullptr, nullptr, tcnt + 3 * i + 1, &p->tr))
+                        return fail(ctx, RJ_E_INVALID, "too many (tile, polygon) items");
+                    if (p->check_overlap) launch_tier_nonempty(p->tr.plabel, spx, tcnt + 3 * i + 2, ctx->sms, st);
+                } else {
+                    RJ_CUDA(cudaMemsetAsync(p->tr.bcnt, 0, p->nblk * 4, st));
+                    RJ_CUDA(cudaMemsetAsync(p->tr.pcnt, 0, std::max<size_t>(spx, 1) * 4, st));
+                    if (p->tr.bsum) RJ_CUDA(cudaMemsetAsync(p->tr.bsum, 0, p->nblk * 8, st));
+                    if (p->tr.psum) RJ_CUDA(cudaMemsetAsync(p->tr.psum, 0, std::max<size_t>(spx, 1) * 8, st));
+                }
+            }
+        }
         // ---- polygon side: label maps / zeroed canvases
         bool any_check = false;
         for (size_t i = 0; i < nw; ++i) {
@@ -391,15 +493,41 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
             }
         }
         RJ_CUDA(cudaGetLastError());
+        for (QPlan* p : wave) any_check |= p->tier && p->check_overlap;
         if (any_check) {
             // which label maps hold every covered pixel centre exactly once
-            std::vector<unsigned long long> hl(2 * nw);
+            std::vector<unsigned long long> hl(2 * nw), ht(3 * nw);
             RJ_CUDA(cudaMemcpyAsync(hl.data(), lcnt, 2 * nw * 8, cudaMemcpyDeviceToHost, st));
+            RJ_CUDA(cudaMemcpyAsync(ht.data(), tcnt, 3 * nw * 8, cudaMemcpyDeviceToHost, st));
             RJ_CUDA(cudaStreamSynchronize(st));
             for (size_t i = 0; i < nw; ++i) {
                 QPlan* p = wave[i];
                 if (!p->check_overlap) continue;
-                const bool overlap = hl[2 * i] != hl[2 * i + 1];
+                const bool overlap = p->tier ? (ht[3 * i] != 0 || ht[3 * i + 1] != ht[3 * i + 2])
+                                             : hl[2 * i] != hl[2 * i + 1];
+                if (p->tier) {
+                    {
+                        std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+                        p->ps->overlap[p->canvas] = overlap ? 1 : 0;
+                    }
+                    if (!overlap) continue;
+                    p->mode = BQ_TSPLAT;
+                    TierArgs& tr = p->tr;
+                    const size_t spx = (size_t)std::max(p->nslots, 1) * 256;
+                    tr.bcnt = ar.take<uint32_t>(p->nblk);
+                    tr.pcnt = ar.take<uint32_t>(spx);
+                    if (p->f.aggr) {
+                        tr.bsum = ar.take<long long>(p->nblk);
+                        tr.psum = ar.take<long long>(spx);
+                    }
+                    if (!tr.bcnt || !tr.pcnt || (p->f.aggr && (!tr.bsum || !tr.psum)))
+                        return fail(ctx, RJ_E_OOM, "batch arena too small for a tiered canvas");
+                    RJ_CUDA(cudaMemsetAsync(tr.bcnt, 0, p->nblk * 4, st));
+                    RJ_CUDA(cudaMemsetAsync(tr.pcnt, 0, spx * 4, st));
+                    if (tr.bsum) RJ_CUDA(cudaMemsetAsync(tr.bsum, 0, p->nblk * 8, st));
+                    if (tr.psum) RJ_CUDA(cudaMemsetAsync(tr.psum, 0, spx * 8, st));
+                    continue;
+                }
                 {
                     std::lock_guard<std::recursive_mutex> lock(ctx->mu);
                     p->ps->overlap[p->canvas] = overlap ? 1 : 0;
@@ -470,6 +598,7 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
             d.label = p->label;
             d.canvas_c = p->cc;
             d.canvas_s = p->cs;
+            d.tr = p->tr;
             {
                 // canvas extent plus two pixels: a location outside it maps to
                 // no pixel of any tile (window range test and snapping)
@@ -478,7 +607,7 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
                 d.box = make_float4((float)(p->ps->bbox[0] - mx), (float)(p->ps->bbox[1] - my),
                                     (float)(p->ps->bbox[2] + mx), (float)(p->ps->bbox[3] + my));
             }
-            if (p->mode == BQ_LABEL && d.P <= kBatchHistCap) max_hist = std::max(max_hist, d.P);
+            if ((p->mode == BQ_LABEL || p->mode == BQ_TLABEL) && d.P <= kBatchHistCap) max_hist = std::max(max_hist, d.P);
             if (p->mode == BQ_SPLAT && p->T == 1 && p->npix <= (size_t)kBatchHistCap) {
                 // small canvas: splat into the block's shared histogram (indexed by
                 // pixel) and flush into the canvas
@@ -492,7 +621,8 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
         }
         const int hist_cap = (max_hist + 1) & ~1;
         for (size_t i = 0; i < nw; ++i)
-            hq[i].hist_smem = (hq[i].mode == BQ_LABEL || hq[i].out_count32) && hq[i].P <= hist_cap ? 1 : 0;
+            hq[i].hist_smem = (hq[i].mode == BQ_LABEL || hq[i].mode == BQ_TLABEL || hq[i].out_count32) &&
+                                      hq[i].P <= hist_cap ? 1 : 0;
         ba.nu = (int)ucols.size();
         for (int u = 0; u < ba.nu; ++u) {
             ba.ucol[u] = ucols[u];
@@ -537,11 +667,18 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
             cudaMemsetAsync(oc, 0, outs * 8, st);
             cudaMemsetAsync(os, 0, outs * 8, st);
             cudaMemsetAsync(onf, 0, outs * 8, st);
-            for (QPlan* p : act)
+            for (QPlan* p : act) {
                 if (p->mode == BQ_SPLAT) {
                     cudaMemsetAsync(p->cc, 0, p->npix * 4, st);
                     if (p->cs) cudaMemsetAsync(p->cs, 0, p->npix * 8, st);
+                } else if (p->mode == BQ_TSPLAT) {
+                    const size_t spx = (size_t)std::max(p->nslots, 1) * 256;
+                    cudaMemsetAsync(p->tr.bcnt, 0, p->nblk * 4, st);
+                    cudaMemsetAsync(p->tr.pcnt, 0, spx * 4, st);
+                    if (p->tr.bsum) cudaMemsetAsync(p->tr.bsum, 0, p->nblk * 8, st);
+                    if (p->tr.psum) cudaMemsetAsync(p->tr.psum, 0, spx * 8, st);
                 }
+            }
         };
         if ((flags & RJ_BATCH_AUTOTUNE) && !e.tuned && nitems > 0) {
             static const BatchShape cands[] = {{256, 2048, 0},  {256, 4096, 0},  {256, 8192, 0},  {512, 4096, 0},
@@ -577,9 +714,13 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
         cudaEventRecord(e.ev[2], st);
         // ---- canvas-path queries: polygon pass over their canvases
         for (QPlan* p : act) {
-            if (p->mode != BQ_SPLAT) continue;
-            if (!query_poly_pass(e, *p, MODE_REDUCE, ps, oc + p->out_off, os + p->out_off, nullptr))
-                return fail(ctx, RJ_E_INVALID, "too many (tile, polygon) items");
+            if (p->mode == BQ_SPLAT) {
+                if (!query_poly_pass(e, *p, MODE_REDUCE, ps, oc + p->out_off, os + p->out_off, nullptr))
+                    return fail(ctx, RJ_E_INVALID, "too many (tile, polygon) items");
+            } else if (p->mode == BQ_TSPLAT) {
+                if (!query_poly_pass(e, *p, MODE_TIER_REDUCE, ps, oc + p->out_off, os + p->out_off, nullptr, &p->tr))
+                    return fail(ctx, RJ_E_INVALID, "too many (tile, polygon) items");
+            }
         }
         RJ_CUDA(cudaGetLastError());
         cudaEventRecord(e.ev[3], st);
@@ -810,8 +951,8 @@ int rj_polyset_create(rj_ctx* ctx, const float* xy, const int32_t* pindex, int32
                       rj_polyset** out) {
     if (!ctx || !out) return RJ_E_INVALID;
     *out = nullptr;
-    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
-    ctx->err.clear();
+    // no context lock: the new set is private until returned, and its upload
+    // does not wait for joins in flight
     rj_polyset* ps = new rj_polyset();
     ps->ctx = ctx;
     int rc = load_polyset(ctx, ps->s, xy, pindex, npolys, bbox);

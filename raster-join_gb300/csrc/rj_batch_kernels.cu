@@ -56,7 +56,37 @@ __device__ __forceinline__ void batch_query(const BatchArgs& a, const BatchQuery
     Hist<AGG, SMEM> h{s_cnt, s_sum, Q->out_count, Q->out_sum, Q->out_nonfinite, Q->sum_scale};
     const DeferQ dq{nullptr, nullptr, nullptr, nullptr};
     const CanvasXf cx = Q->cx;
-    if (mode == BQ_LABEL) {
+    if (mode == BQ_TLABEL || mode == BQ_TSPLAT) {
+        const TierLabelMapper ml{cx, Q->tr};
+        const TierSplatMapper ms{cx, Q->tr, Q->sum_scale};
+        for (int base = 0; base < nrows; base += 4 * BLOCK) {
+            float x[4], y[4], v[4];
+            bool ok[4];
+            uint32_t key[4];
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int r = base + k * BLOCK + tid;
+                ok[k] = r < nrows;
+                x[k] = y[k] = v[k] = 0.f;
+                key[k] = 0xFFFFFFFFu;
+                if (ok[k]) {
+                    const float2 p = s_xy[r];
+                    x[k] = p.x;
+                    y[k] = p.y;
+                    #pragma unroll
+                    for (int u = 0; u < kBatchMaxCols; ++u)
+                        if (u < a.nu) ok[k] = ok[k] && (order_key(a.utyp[u], s_col[u * a.rows + r]) - lo[u] <= span[u]);
+                    if (AGG && ok[k]) v[k] = agg_value(aggr_typ, s_col[aggr_u * a.rows + r]);
+                    if (ok[k]) key[k] = mode == BQ_TLABEL ? ml.lookup(x[k], y[k]) : ms.lookup(x[k], y[k]);
+                }
+            }
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (mode == BQ_TLABEL) ml.consume(ok[k], key[k], x[k], y[k], v[k], h, dq);
+                else ms.consume(ok[k], key[k], x[k], y[k], v[k], h, dq);
+            }
+        }
+    } else if (mode == BQ_LABEL) {
         const LabelMapper m{cx, Q->label};
         for (int base = 0; base < nrows; base += 4 * BLOCK) {
             float x[4], y[4], v[4];
@@ -290,7 +320,21 @@ __device__ __forceinline__ void direct_query(const BatchArgs& a, const BatchQuer
                 if (ok) mask |= 1u << k;
             }
         }
-        if (mode == BQ_LABEL) {
+        if (mode == BQ_TLABEL) {
+            const TierLabelMapper tm{cx, Q->tr};
+            uint32_t key[4];
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) key[k] = ((mask >> k) & 1u) ? tm.lookup(x[k], y[k]) : TierLabelMapper::kNone;
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) tm.consume(((mask >> k) & 1u) != 0u, key[k], x[k], y[k], v[k], h, dq);
+        } else if (mode == BQ_TSPLAT) {
+            const TierSplatMapper tm{cx, Q->tr, Q->sum_scale};
+            uint32_t key[4];
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) key[k] = ((mask >> k) & 1u) ? tm.lookup(x[k], y[k]) : TierSplatMapper::kNone;
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) tm.consume(((mask >> k) & 1u) != 0u, key[k], x[k], y[k], v[k], h, dq);
+        } else if (mode == BQ_LABEL) {
             LabelMapper::Key key[4];
             #pragma unroll
             for (int k = 0; k < 4; ++k) key[k] = ((mask >> k) & 1u) ? lm.lookup(x[k], y[k]) : LabelMapper::kNone;

@@ -214,7 +214,7 @@ void launch_cls_codes(const int* cell_start, const int4* entries, uint32_t* code
 // the same set of queries covers); a block of rows is staged in shared memory
 // once and every query of its segment runs over it.
 constexpr int kBatchMaxCols = 6;          // distinct scalar columns one batch may read
-enum { BQ_LABEL = 0, BQ_SPLAT = 1, BQ_SKIP = 2 };
+enum { BQ_LABEL = 0, BQ_SPLAT = 1, BQ_SKIP = 2, BQ_TLABEL = 3, BQ_TSPLAT = 4 };   // T: tiered canvas
 
 struct BatchQuery {
     uint32_t lo[kBatchMaxCols];           // interval predicate per batch column:
@@ -234,6 +234,7 @@ struct BatchQuery {
     double* out_nonfinite;                // [P]
     uint32_t* out_count32;                // private splat: counts flushed into the u32 canvas
     float4 box;                           // locations that can reach the canvas (x0, y0, x1, y1)
+    TierArgs tr;                          // BQ_TLABEL / BQ_TSPLAT
 };
 
 struct BatchSeg {

@@ -537,17 +537,18 @@ static void launch_plain_t(const PointArgs& pa, const M& mp, int sms, cudaStream
     ++g_kernel_launches;
 }
 
-// Point-kernel variant: 0 = plain, 4 points x 256 threads (default);
-// 1 = plain, 8 points x 256 threads; 2 = bulk-copy pipeline; 3 = plain,
-// 4 points x 512 threads; 4 = plain, 4 points x 128 threads.
-// RJ_POINT_VARIANT overrides the default (a tuning knob; every variant
-// computes the same result).
+// Point-kernel variant: 3 = plain, 4 points x 512 threads (default; the
+// fastest on GB300 for the config-2 hybrid pass: 0.833 ms vs 0.910 ms for
+// 4 x 256, 1.077 ms for 8 x 256, 0.949 ms for 4 x 128); 0 = plain, 4 points x
+// 256 threads; 1 = plain, 8 points x 256 threads; 2 = bulk-copy pipeline;
+// 4 = plain, 4 points x 128 threads.  RJ_POINT_VARIANT overrides the default
+// (a tuning knob; every variant computes the same result).
 static int point_variant() {
     static int v = -1;
     if (v < 0) {
         const char* e = getenv("RJ_POINT_VARIANT");
-        v = e ? atoi(e) : 0;
-        if (v < 0 || v > 4) v = 0;
+        v = e ? atoi(e) : 3;
+        if (v < 0 || v > 4) v = 3;
     }
     return v;
 }
@@ -556,9 +557,9 @@ template <class M, bool AGG, bool SMEM>
 static void launch_points_t(const PointArgs& pa, const M& mp, int sms, cudaStream_t st) {
     switch (point_variant()) {
         case 1: launch_plain_t<M, AGG, SMEM, 2, 256>(pa, mp, sms, st); break;
-        case 3: launch_plain_t<M, AGG, SMEM, 1, 512>(pa, mp, sms, st); break;
         case 4: launch_plain_t<M, AGG, SMEM, 1, 128>(pa, mp, sms, st); break;
-        default: launch_plain_t<M, AGG, SMEM, 1, 256>(pa, mp, sms, st); break;
+        case 0: launch_plain_t<M, AGG, SMEM, 1, 256>(pa, mp, sms, st); break;
+        default: launch_plain_t<M, AGG, SMEM, 1, 512>(pa, mp, sms, st); break;
     }
 }
 

@@ -18,8 +18,8 @@ namespace rj {
 __device__ __forceinline__ long long group_sum(unsigned active, unsigned peers, long long q) {
     const int lane = threadIdx.x & 31;
     const unsigned gsize = (unsigned)__popc(peers);
+    if (__all_sync(active, gsize == 1u)) return q;          // no two lanes share a key (a vote)
     const unsigned maxg = __reduce_max_sync(active, gsize);
-    if (maxg == 1u) return q;
     if (maxg <= 4u) {
         const int leader = __ffs(peers) - 1;
         long long sum = q;

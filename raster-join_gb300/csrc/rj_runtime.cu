@@ -25,6 +25,14 @@ using namespace rj;
 
 namespace rjh {
 
+// refinement of the query grid for the hybrid join's exact tests (override
+// with RJ_HYBRID_EXACT_SCALE: 1, 2, 4)
+static const int kHybridExactScale = [] {
+    const char* e = getenv("RJ_HYBRID_EXACT_SCALE");
+    const int v = e ? atoi(e) : 1;
+    return (v == 1 || v == 2 || v == 4) ? v : 1;
+}();
+
 
 int fail(rj_ctx* c, int code, const char* fmt, ...) {
     char buf[512];
@@ -378,11 +386,11 @@ int build_grid(rj_ctx* ctx, int res, int clamp, IndexArgs& ia, bool with_pair_ce
 
 // Resolution of the classified grid: the query grid times 2^k, about 1024
 // cells across, with cells much larger than the fp32 error of the test.
-int exact_res(const rj_ctx* ctx, int res) {
+int exact_res(const rj_ctx* ctx, int res, int max_scale) {
     const double ext = std::max(ctx->ps->bbox[2] - ctx->ps->bbox[0], ctx->ps->bbox[3] - ctx->ps->bbox[1]);
     const double err = std::ldexp(1.0, -21) * (ctx->ps->max_abs_coord + 6.0 * std::max(ctx->ps->max_edge_dx, ctx->ps->max_edge_dy) + 1.0);
     int g = res;
-    while (g * 2 <= 1024 && ext / (g * 2) > 64.0 * err) g *= 2;
+    while (g * 2 <= 1024 && g * 2 <= res * max_scale && ext / (g * 2) > 64.0 * err) g *= 2;
     return g;
 }
 
@@ -391,9 +399,11 @@ int exact_res(const rj_ctx* ctx, int res) {
 // range on the query grid (index-size.glsl:50-68, upper bound clamped to the
 // grid) contains the query-grid cell holding it; every query-grid cell is a
 // block of 2^k x 2^k classified cells.
-int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix) {
+// max_scale: finest refinement of the query grid (the hybrid join tests only
+// the points near an outline, so a coarser classified grid is cheaper overall).
+int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix, int max_scale = 1024) {
     int rc;
-    const int G = exact_res(ctx, user_res);
+    const int G = exact_res(ctx, user_res, max_scale);
     const int scale = G / user_res;
     ExactCache& xc = ctx->ps->exact;
     const size_t ncells = (size_t)G * G;
@@ -847,7 +857,8 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
     a.line_filter = (q->flags & RJ_FLAG_LINE_FILTER) ? 1 : 0;
 
     const uint64_t ckey = canvas_key(rp.colxf, rp.rowxf, rp.resx, rp.resy);
-    if (!bounds && npix >= kTierMinPixels && !(q->flags & RJ_FLAG_FLAT_CANVAS))
+    const uint64_t rows = std::min(ctx->row1, ctx->npts) - std::min(ctx->row0, ctx->npts);
+    if (!bounds && use_tier(npix, rows) && !(q->flags & RJ_FLAG_FLAT_CANVAS))
         return exec_raster_tier(ctx, q, rp, f, es, a, cx, ckey);
     bool use_label = !bounds && !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->ps->overlap_on(ckey) != 1 &&
                      ctx->ps->P <= kMaxLabelPolys;
@@ -946,7 +957,7 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     if (q->grid_res <= 0 || q->grid_res > 8192) return fail(ctx, RJ_E_INVALID, "grid resolution %d out of range", q->grid_res);
     es.ph->mark(1);
     ExactIndex ix{};
-    if ((rc = build_exact(ctx, q->grid_res, ix))) return rc;
+    if ((rc = build_exact(ctx, q->grid_res, ix, kHybridExactScale))) return rc;
 
     // canvas: getResolution(bbox, fboSize) (HybridJoin.cpp:62-66, Utils.h:29-34)
     const double dx = ctx->ps->bbox[2] - ctx->ps->bbox[0], dy = ctx->ps->bbox[3] - ctx->ps->bbox[1];
@@ -1110,10 +1121,22 @@ int load_polyset(rj_ctx* ctx, PolySet& s, const float* xy, const int32_t* pindex
         }
         s.h_mbr[i] = make_float4(a, b, c, d);
     }
-    RJ_CUDA(cudaMemcpyAsync(s.d_verts.p, xy, (size_t)V * 8, cudaMemcpyHostToDevice, ctx->stream));
-    RJ_CUDA(cudaMemcpyAsync(s.d_pindex.p, pindex, (size_t)(npolys + 1) * 4, cudaMemcpyHostToDevice, ctx->stream));
-    RJ_CUDA(cudaMemcpyAsync(s.d_edge_poly.p, edge_poly.data(), (size_t)V * 4, cudaMemcpyHostToDevice, ctx->stream));
-    RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    // synchronous copies on the default stream: they do not wait for the
+    // context's (non-blocking) streams, so a set can be uploaded while joins run
+    RJ_CUDA(cudaMemcpy(s.d_verts.p, xy, (size_t)V * 8, cudaMemcpyHostToDevice));
+    RJ_CUDA(cudaMemcpy(s.d_pindex.p, pindex, (size_t)(npolys + 1) * 4, cudaMemcpyHostToDevice));
+    RJ_CUDA(cudaMemcpy(s.d_edge_poly.p, edge_poly.data(), (size_t)V * 4, cudaMemcpyHostToDevice));
+    double sdx = 0, sdy = 0;   // total edge extents: bound on the canvas blocks edges cross
+    for (int i = 0; i < npolys; ++i) {
+        const int v0 = pindex[i], n = pindex[i + 1] - v0;
+        for (int k = 0; k < n; ++k) {
+            const int kn = (k + 1 == n) ? 0 : k + 1;
+            sdx += std::fabs((double)xy[2 * (v0 + kn)] - xy[2 * (v0 + k)]);
+            sdy += std::fabs((double)xy[2 * (v0 + kn) + 1] - xy[2 * (v0 + k) + 1]);
+        }
+    }
+    s.sum_dx = sdx;
+    s.sum_dy = sdy;
     s.P = npolys;
     s.V = V;
     for (int i = 0; i < 4; ++i) s.bbox[i] = bb[i];

@@ -5,6 +5,8 @@ Every query of a batch must give exactly the result it gives alone through
 rj_execute (counts and fixed-point sums are order-independent integers, so
 the comparison is bit-exact), and alone it matches the CPU oracle.  The time
 index reorders the table: results before and after must be identical."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -263,3 +265,24 @@ def test_clustered_order_preserves_results(table, built, time_attrib, nb, bits):
         stars.close()
     finally:
         h.close()
+
+
+def test_batch_tiered_canvases(setup):
+    """Large canvases (>= 2^24 pixels) take the tiered form inside the fused
+    batch: label form, canvas form after an overlap check, several tiles;
+    each equals the flat single-query result."""
+    h, sets, _ = setup
+    qs = [make_query(5.0, aggr=True), make_query(4.0, aggr=True, window=(T0, T0 + 200 * DAY)),
+          make_query(2.5, max_fbo=6000), make_query(6.0, preds=((4, rj.GT, 3),))]
+    ss = [sets[0], sets[1], sets[0], sets[4]]
+    flat = []
+    for s, q in zip(ss, qs):
+        q2 = rj.Query()
+        C.pointer(q2)[0] = q
+        q2.flags = rj.FLAG_FLAT_CANVAS
+        flat.append(single(h, s, q2))
+    res, status, stats = h.execute_batch(qs, ss)
+    assert (status == 0).all() and stats["fused"] == len(qs) and stats["fallback"] == 0
+    for (c, sm), r in zip(flat, res):
+        np.testing.assert_array_equal(r.count, c)
+        np.testing.assert_array_equal(r.sum, sm)
