@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--saturate-requests", type=int, default=4000)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--config3", action="store_true",
+                    help="run configuration 3 instead (2B resident points, raster and error-bounds joins at eps 10 m "
+                         "and 1 m, 260 Voronoi cells and 2000 stars) and print its own line")
     ap.add_argument("--cluster", action="store_true",
                     help="config 2: reorder the table by 156 m cells before timing (default: generated order)")
     return ap.parse_args()
@@ -563,10 +566,58 @@ def run_gb300(args):
     return 0
 
 
+def run_config3(args):
+    """Configuration 3: 2B points resident (x, y generated on the device),
+    two polygon sets, raster and error-bounds joins at eps 10 m and 1 m."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import rasterjoin as rj
+    from rasterjoin import synth, workloads as W
+    n = args.points if args.points != 100_000_000 else 2_000_000_000
+    tab = W.device_table(n, 7)
+    torch.cuda.synchronize()
+    h = rj.GLHandler()
+    h.attachDevice([(1, rj.Location, tab["xy"].data_ptr())], n, 1)
+    sets = {"voronoi260": synth.voronoi_polygons(260, seed=20261203),
+            "stars2000": synth.star_polygons(2000, seed=20261203, vmin=20, vmax=500, rmin=200, rmax=2000)}
+    out = []
+    for name, (v, p) in sets.items():
+        ps = h.polyset(v, p)
+        h.usePolySet(ps)
+        for eps in (10.0, 1.0):
+            for fn in (rj.RasterJoinFn, rj.RasterJoinBoundFn):
+                q = rj.default_query()
+                q.function_type = fn
+                q.cell_size = eps
+                h.execute(fn, query=q)                 # warm-up (builds the polygon structures once)
+                ms = []
+                for _ in range(max(1, args.steps)):
+                    t0 = time.perf_counter()
+                    r = h.execute(fn, query=q)
+                    ms.append((time.perf_counter() - t0) * 1e3)
+                P = len(p) - 1
+                rec = {"polygons": name, "eps_m": eps, "join": "raster" if fn == rj.RasterJoinFn else "error-bounds",
+                       "ms": float(np.median(ms)), "gpoints_s": n / float(np.median(ms)) / 1e6,
+                       "total_count": int(r.count.sum())}
+                if fn == rj.RasterJoinBoundFn:
+                    b = r.bounds.astype(np.int64)
+                    rec["mean_hard_range"] = float(np.mean(b[2 * P:3 * P] + b[3 * P:]))
+                out.append(rec)
+        h.usePolySet(None)
+        ps.close()
+    h.close()
+    print(json.dumps({"metric": "config 3: Gpoints/s joined over %d resident points" % n, "unit": "Gpoints/s",
+                      "n_gpus": 1, "data": "synthetic, generated on the device", "results": out}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config3:
+        return run_config3(args)
     return run_gb300(args)
 
 

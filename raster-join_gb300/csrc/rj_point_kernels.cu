@@ -537,29 +537,33 @@ static void launch_plain_t(const PointArgs& pa, const M& mp, int sms, cudaStream
     ++g_kernel_launches;
 }
 
-// Point-kernel variant: 3 = plain, 4 points x 512 threads (default; the
-// fastest on GB300 for the config-2 hybrid pass: 0.833 ms vs 0.910 ms for
-// 4 x 256, 1.077 ms for 8 x 256, 0.949 ms for 4 x 128); 0 = plain, 4 points x
-// 256 threads; 1 = plain, 8 points x 256 threads; 2 = bulk-copy pipeline;
-// 4 = plain, 4 points x 128 threads.  RJ_POINT_VARIANT overrides the default
-// (a tuning knob; every variant computes the same result).
+// Point-kernel variant: 0 = plain, 4 points x 256 threads; 1 = plain, 8
+// points x 256 threads; 2 = bulk-copy pipeline; 3 = plain, 4 points x 512
+// threads; 4 = plain, 4 points x 128 threads.  Defaults measured on GB300
+// (config-2 query, 100M points): the hybrid pass is fastest with 3 (0.833 ms
+// vs 0.910 ms for 0, 1.077 ms for 1, 0.949 ms for 4), the raster-label and
+// index passes with 0 (0.65 ms vs 0.79 ms; 2.07 ms vs 2.36 ms).
+// RJ_POINT_VARIANT overrides the default for every mapper (a tuning knob;
+// every variant computes the same result).
+template <class M>
 static int point_variant() {
-    static int v = -1;
-    if (v < 0) {
+    static int v = -2;
+    if (v == -2) {
         const char* e = getenv("RJ_POINT_VARIANT");
-        v = e ? atoi(e) : 3;
-        if (v < 0 || v > 4) v = 3;
+        v = e ? atoi(e) : -1;
+        if (v < -1 || v > 4) v = -1;
     }
-    return v;
+    if (v >= 0) return v;
+    return M::kDefer ? 3 : 0;   // the hybrid mapper defers border points to a block queue
 }
 
 template <class M, bool AGG, bool SMEM>
 static void launch_points_t(const PointArgs& pa, const M& mp, int sms, cudaStream_t st) {
-    switch (point_variant()) {
+    switch (point_variant<M>()) {
         case 1: launch_plain_t<M, AGG, SMEM, 2, 256>(pa, mp, sms, st); break;
+        case 3: launch_plain_t<M, AGG, SMEM, 1, 512>(pa, mp, sms, st); break;
         case 4: launch_plain_t<M, AGG, SMEM, 1, 128>(pa, mp, sms, st); break;
-        case 0: launch_plain_t<M, AGG, SMEM, 1, 256>(pa, mp, sms, st); break;
-        default: launch_plain_t<M, AGG, SMEM, 1, 512>(pa, mp, sms, st); break;
+        default: launch_plain_t<M, AGG, SMEM, 1, 256>(pa, mp, sms, st); break;
     }
 }
 
@@ -594,7 +598,7 @@ static void launch_points(const PointArgs& pa, const M& mp, int sms, cudaStream_
     const bool agg = pa.f.aggr != 0;
     const bool smem_ok = hist_bytes(pa.P, agg) + queue_bytes(M::kDefer) <= (size_t)std::max(g_max_smem_optin - 1024, 0);
     // bulk-copy pipeline for tables of at least one tile per SM (columns are 16-byte aligned)
-    if (point_variant() == 2 && pa.err && pa.n >= (uint64_t)kPipeTile * sms && smem_ok) {
+    if (point_variant<M>() == 2 && pa.err && pa.n >= (uint64_t)kPipeTile * sms && smem_ok) {
         bool launched = agg ? launch_pipe_t<M, true, true>(pa, mp, sms, st) : launch_pipe_t<M, false, true>(pa, mp, sms, st);
         if (launched) return;
     }
