@@ -28,13 +28,47 @@
 namespace rj {
 
 size_t batch_smem_bytes(const BatchShape& s, int nu, int hist_cap) {
-    return (size_t)hist_cap * 12 + (s.direct ? 0 : (size_t)s.rows * (8 + 4 * (size_t)nu));
+    return (size_t)hist_cap * 16 + (s.direct ? 0 : (size_t)s.rows * (8 + 4 * (size_t)nu));
+}
+
+// The shared histogram stays zero between (item, query) visits: a flush
+// visits only the keys whose count left zero (the touched list) and zeroes
+// them again, so a visit costs its hits, not the query's polygon count.
+template <bool AGG, int BLOCK>
+__device__ __forceinline__ void flush_touched(const BatchQuery* __restrict__ Q, uint32_t* s_cnt,
+                                              unsigned long long* s_sum, int* s_touch, int* s_ntouch) {
+    __syncthreads();
+    const int nt = *s_ntouch;
+    for (int k = threadIdx.x; k < nt; k += BLOCK) {
+        const int b = s_touch[k];
+        const uint32_t c = s_cnt[b];
+        if (Q->out_count32) atomicAdd(Q->out_count32 + b, c);   // private splat canvas
+        else atomicAdd(Q->out_count + b, (unsigned long long)c);
+        s_cnt[b] = 0u;
+        if (AGG) {
+            atomicAdd(Q->out_sum + b, s_sum[b]);
+            s_sum[b] = 0ull;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *s_ntouch = 0;
+    __syncthreads();
+}
+
+__device__ __forceinline__ void hist_init(uint32_t* s_cnt, unsigned long long* s_sum, int cap, int* s_ntouch) {
+    for (int b = threadIdx.x; b < cap; b += blockDim.x) {
+        s_cnt[b] = 0u;
+        s_sum[b] = 0ull;
+    }
+    if (threadIdx.x == 0) *s_ntouch = 0;
+    __syncthreads();
 }
 
 template <bool AGG, bool SMEM, int BLOCK>
 __device__ __forceinline__ void batch_query(const BatchArgs& a, const BatchQuery* __restrict__ Q,
                                             const float2* s_xy, const uint32_t* s_col, int nrows,
-                                            uint32_t* s_cnt, unsigned long long* s_sum) {
+                                            uint32_t* s_cnt, unsigned long long* s_sum, int* s_touch,
+                                            int* s_ntouch) {
     const int tid = threadIdx.x;
     const int mode = Q->mode;
     const int P = Q->P;
@@ -46,14 +80,10 @@ __device__ __forceinline__ void batch_query(const BatchArgs& a, const BatchQuery
     }
     const int aggr_u = Q->aggr_u;
     const int aggr_typ = Q->aggr_typ;
-    if (SMEM) {
-        for (int b = tid; b < P; b += BLOCK) {
-            s_cnt[b] = 0u;
-            if (AGG) s_sum[b] = 0ull;
-        }
-        __syncthreads();
-    }
+    (void)P;
     Hist<AGG, SMEM> h{s_cnt, s_sum, Q->out_count, Q->out_sum, Q->out_nonfinite, Q->sum_scale};
+    h.s_touched = s_touch;
+    h.s_ntouched = s_ntouch;
     const DeferQ dq{nullptr, nullptr, nullptr, nullptr};
     const CanvasXf cx = Q->cx;
     if (mode == BQ_TLABEL || mode == BQ_TSPLAT) {
@@ -139,17 +169,7 @@ __device__ __forceinline__ void batch_query(const BatchArgs& a, const BatchQuery
             for (int k = 0; k < 4; ++k) m.consume(ok[k], key[k], x[k], y[k], v[k], h, dq);
         }
     }
-    if (SMEM) {
-        __syncthreads();
-        for (int b = tid; b < P; b += BLOCK) {
-            const uint32_t c = s_cnt[b];
-            if (c) {
-                if (Q->out_count32) atomicAdd(Q->out_count32 + b, c);   // private splat canvas
-                else atomicAdd(Q->out_count + b, (unsigned long long)c);
-                if (AGG) atomicAdd(Q->out_sum + b, s_sum[b]);
-            }
-        }
-    }
+    if (SMEM) flush_touched<AGG, BLOCK>(Q, s_cnt, s_sum, s_touch, s_ntouch);
 }
 
 template <int BLOCK>
@@ -157,12 +177,15 @@ __global__ void __launch_bounds__(BLOCK) k_batch_points(BatchArgs a) {
     extern __shared__ unsigned long long smem_b[];
     unsigned long long* s_sum = smem_b;
     uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_sum + a.hist_cap);
-    float2* s_xy = reinterpret_cast<float2*>(s_cnt + a.hist_cap);   // hist_cap is even: 8-byte aligned
+    int* s_touch = reinterpret_cast<int*>(s_cnt + a.hist_cap);
+    float2* s_xy = reinterpret_cast<float2*>(s_touch + a.hist_cap);   // hist_cap is even: 8-byte aligned
     uint32_t* s_col = reinterpret_cast<uint32_t*>(s_xy + a.rows);
     __shared__ unsigned long long s_item;
     __shared__ int s_seg;
+    __shared__ int s_ntouch;
     __shared__ float4 s_box[BLOCK / 32 + 1];
     const int tid = threadIdx.x;
+    hist_init(s_cnt, s_sum, a.hist_cap, &s_ntouch);
     for (;;) {
         if (tid == 0) {
             const unsigned long long it = atomicAdd(a.work, 1ull);
@@ -229,11 +252,11 @@ __global__ void __launch_bounds__(BLOCK) k_batch_points(BatchArgs a) {
             const bool agg = Q->aggr_u >= 0;
             const bool smem = Q->hist_smem != 0;
             if (agg) {
-                if (smem) batch_query<true, true, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum);
-                else batch_query<true, false, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum);
+                if (smem) batch_query<true, true, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum, s_touch, &s_ntouch);
+                else batch_query<true, false, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum, s_touch, &s_ntouch);
             } else {
-                if (smem) batch_query<false, true, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum);
-                else batch_query<false, false, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum);
+                if (smem) batch_query<false, true, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum, s_touch, &s_ntouch);
+                else batch_query<false, false, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum, s_touch, &s_ntouch);
             }
         }
         __syncthreads();   // the staged rows are overwritten by the next item
@@ -248,7 +271,8 @@ __global__ void __launch_bounds__(BLOCK) k_batch_points(BatchArgs a) {
 // boundaries are multiples of four rows, so the vector loads stay aligned.
 template <bool AGG, bool SMEM, int BLOCK>
 __device__ __forceinline__ void direct_query(const BatchArgs& a, const BatchQuery* __restrict__ Q, uint64_t r0,
-                                             uint64_t r1, bool last, uint32_t* s_cnt, unsigned long long* s_sum) {
+                                             uint64_t r1, bool last, uint32_t* s_cnt, unsigned long long* s_sum,
+                                             int* s_touch, int* s_ntouch) {
     const int tid = threadIdx.x;
     const int mode = Q->mode;
     const int P = Q->P;
@@ -262,14 +286,10 @@ __device__ __forceinline__ void direct_query(const BatchArgs& a, const BatchQuer
         used[u] = u < a.nu && (lo[u] != 0u || span[u] != 0xFFFFFFFFu || u == aggr_u);
     }
     const int aggr_typ = Q->aggr_typ;
-    if (SMEM) {
-        for (int b = tid; b < P; b += BLOCK) {
-            s_cnt[b] = 0u;
-            if (AGG) s_sum[b] = 0ull;
-        }
-        __syncthreads();
-    }
+    (void)P;
     Hist<AGG, SMEM> h{s_cnt, s_sum, Q->out_count, Q->out_sum, Q->out_nonfinite, Q->sum_scale};
+    h.s_touched = s_touch;
+    h.s_ntouched = s_ntouch;
     const DeferQ dq{nullptr, nullptr, nullptr, nullptr};
     const CanvasXf cx = Q->cx;
     const LabelMapper lm{cx, Q->label};
@@ -348,18 +368,7 @@ __device__ __forceinline__ void direct_query(const BatchArgs& a, const BatchQuer
             for (int k = 0; k < 4; ++k) sm.consume(((mask >> k) & 1u) != 0u, key[k], x[k], y[k], v[k], h, dq);
         }
     }
-    if (SMEM) {
-        __syncthreads();
-        for (int b = tid; b < P; b += BLOCK) {
-            const uint32_t c = s_cnt[b];
-            if (c) {
-                if (Q->out_count32) atomicAdd(Q->out_count32 + b, c);
-                else atomicAdd(Q->out_count + b, (unsigned long long)c);
-                if (AGG) atomicAdd(Q->out_sum + b, s_sum[b]);
-            }
-        }
-        __syncthreads();
-    }
+    if (SMEM) flush_touched<AGG, BLOCK>(Q, s_cnt, s_sum, s_touch, s_ntouch);
 }
 
 template <int BLOCK>
@@ -367,9 +376,12 @@ __global__ void __launch_bounds__(BLOCK) k_batch_direct(BatchArgs a) {
     extern __shared__ unsigned long long smem_b[];
     unsigned long long* s_sum = smem_b;
     uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_sum + a.hist_cap);
+    int* s_touch = reinterpret_cast<int*>(s_cnt + a.hist_cap);
     __shared__ unsigned long long s_item;
     __shared__ int s_seg;
+    __shared__ int s_ntouch;
     const int tid = threadIdx.x;
+    hist_init(s_cnt, s_sum, a.hist_cap, &s_ntouch);
     for (;;) {
         if (tid == 0) {
             const unsigned long long it = atomicAdd(a.work, 1ull);
@@ -399,11 +411,11 @@ __global__ void __launch_bounds__(BLOCK) k_batch_direct(BatchArgs a) {
             const bool agg = Q->aggr_u >= 0;
             const bool smem = Q->hist_smem != 0;
             if (agg) {
-                if (smem) direct_query<true, true, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum);
-                else direct_query<true, false, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum);
+                if (smem) direct_query<true, true, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum, s_touch, &s_ntouch);
+                else direct_query<true, false, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum, s_touch, &s_ntouch);
             } else {
-                if (smem) direct_query<false, true, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum);
-                else direct_query<false, false, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum);
+                if (smem) direct_query<false, true, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum, s_touch, &s_ntouch);
+                else direct_query<false, false, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum, s_touch, &s_ntouch);
             }
         }
         __syncthreads();   // s_item is rewritten for the next item

@@ -50,6 +50,13 @@ struct Hist {
     unsigned long long* g_sum;
     double* g_nonfinite;
     float scale;
+    // optional: keys whose shared count left zero, so a flush visits only them
+    int* s_touched = nullptr;
+    int* s_ntouched = nullptr;
+    __device__ __forceinline__ void count(int p, unsigned c) const {
+        const unsigned old = atomicAdd(s_cnt + p, c);
+        if (s_touched && old == 0u) s_touched[atomicAdd(s_ntouched, 1)] = p;
+    }
     __device__ __forceinline__ long long fixq(int p, float v) const {
         if (!isfinite(v)) {
             atomicAdd(g_nonfinite + p, (double)v);
@@ -59,7 +66,7 @@ struct Hist {
     }
     __device__ __forceinline__ void add(int p, float v) const {
         if (SMEM) {
-            atomicAdd(s_cnt + p, 1u);
+            count(p, 1u);
             if (AGG) atomicAdd(s_sum + p, (unsigned long long)fixq(p, v));
         } else {
             atomicAdd(g_cnt + p, 1ull);
@@ -80,7 +87,7 @@ struct Hist {
         if (lane == leader) {
             const unsigned c = (unsigned)__popc(peers);
             if (SMEM) {
-                atomicAdd(s_cnt + p, c);
+                count(p, c);
                 if (AGG) atomicAdd(s_sum + p, (unsigned long long)sum);
             } else {
                 atomicAdd(g_cnt + p, (unsigned long long)c);
@@ -190,7 +197,7 @@ struct SplatMapper {
             if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) {
                 const unsigned c = (unsigned)__popc(peers);
                 if (priv) {
-                    atomicAdd(h.s_cnt + k, c);
+                    h.count((int)k, c);
                     if (canvas_s) atomicAdd(h.s_sum + k, (unsigned long long)sum);
                 } else {
                     atomicAdd(canvas_c + k, c);

@@ -10,9 +10,10 @@
 //     touched by another) keep per-pixel data, in a compact slot of 256
 //     pixels.
 // Coverage is the same pixel-centre rule as the flat canvas (exact integer
-// crossings of the row centre lines, spans between sorted crossings), so
-// every result is identical; the work becomes proportional to polygon
-// perimeters and mixed blocks instead of polygon areas.
+// crossings of the row centre lines; a pixel is inside when an odd number of
+// crossings lie at or left of it), so every result is identical; the work
+// becomes proportional to polygon perimeters and mixed blocks instead of
+// polygon areas.
 //
 // One warp per (tile, polygon, band of 16 rows); bands are aligned to block
 // rows.  Per band the warp builds two pixel bitmaps over the polygon's
@@ -30,84 +31,62 @@ namespace {
 constexpr int kTW = 8;            // warps per block
 constexpr int kTBand = 16;        // rows per work item (one block row)
 constexpr int kTEdgeCap = 256;    // staged edges per warp
-constexpr int kTCrossCap = 512;   // crossings per row per warp
 constexpr int kTWords = 256;      // bitmap words per warp: 8192 pixel columns
-constexpr size_t kTierSmem =
-    (size_t)kTW * (kTEdgeCap * sizeof(int4) + kTCrossCap * sizeof(int) + 2 * kTWords * sizeof(uint32_t));
+constexpr size_t kTierSmem = (size_t)kTW * (kTEdgeCap * sizeof(int4) + 3 * kTWords * sizeof(uint32_t));
 
-__device__ __forceinline__ int x1_of(int x0) { return x0 + 32; }
 // bits [a, b) of a word, 0 <= a < b <= 32
 __device__ __forceinline__ uint32_t bitrange(int a, int b) {
     return (b >= 32 ? 0xFFFFFFFFu : ((1u << b) - 1u)) & ~((1u << a) - 1u);
 }
 
-__device__ __forceinline__ void tsort(int* buf, int m, int lane) {
-    int mp = 2;
-    while (mp < m) mp <<= 1;
-    for (int i = m + lane; i < mp; i += 32) buf[i] = INT_MAX;
+// Coverage of row j's pixel centres in [i_lo, i_hi] as a bitmap R[0, nw)
+// (bit b of word w = pixel (w_lo + w) * 32 + b).  A pixel is covered when an
+// odd number of the row's crossings lie at or left of it (crossing pixel
+// L = first pixel right of the crossing, exact integer arithmetic), so each
+// crossing toggles one bit and a prefix XOR over the row gives the coverage:
+// no sorting, O(crossings + words) per row.  Crossings left of i_lo act from
+// i_lo; those right of i_hi do not matter.
+__device__ __forceinline__ void row_cover(int j, const int4* edge, int nb, bool overflow, const int2* pv, int n,
+                                          int i_lo, int i_hi, int w_lo, int nw, uint32_t* R, int lane) {
+    for (int w = lane; w < nw; w += 32) R[w] = 0u;
     __syncwarp();
-    for (int k = 2; k <= mp; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = lane; i < mp; i += 32) {
-                const int ixj = i ^ j;
-                if (ixj > i) {
-                    const int x = buf[i], y = buf[ixj];
-                    const bool up = (i & k) == 0;
-                    if ((x > y) == up) {
-                        buf[i] = y;
-                        buf[ixj] = x;
-                    }
-                }
-            }
-            __syncwarp();
-        }
-    }
-}
-
-// Sorted crossings of row j's centre line into cross[0, m); returns m, or -1
-// when the row has more crossings than the buffer holds.
-__device__ __forceinline__ int row_crossings(int j, const int4* edge, int nb, bool overflow, const int2* pv, int n,
-                                             int* cross, int lane) {
     const int32_t cy = j * kSub + kSub / 2;
-    int m = 0;
     const int ne = overflow ? n : nb;
-    for (int e0 = 0; e0 < ne; e0 += 32) {
-        const int e = e0 + lane;
-        bool c = false;
-        int L = 0;
-        if (e < ne) {
-            int4 q;
-            if (!overflow) {
-                q = edge[e];
-            } else {
-                const int2 A = pv[e];
-                const int2 B = pv[(e + 1 == n) ? 0 : e + 1];
-                q = make_int4(A.x, A.y, B.x, B.y);
-            }
-            if (cross_row(q.y, q.w, cy)) { c = true; L = cross_L(q.x, q.y, q.z, q.w, cy); }
+    for (int e = lane; e < ne; e += 32) {
+        int4 q;
+        if (!overflow) {
+            q = edge[e];
+        } else {
+            const int2 A = pv[e];
+            const int2 B = pv[(e + 1 == n) ? 0 : e + 1];
+            q = make_int4(A.x, A.y, B.x, B.y);
         }
-        const unsigned bm = __ballot_sync(0xffffffffu, c);
-        const int pos = m + __popc(bm & ((1u << lane) - 1u));
-        if (c && pos < kTCrossCap) cross[pos] = L;
-        m += __popc(bm);
+        if (cross_row(q.y, q.w, cy)) {
+            const int L = max(cross_L(q.x, q.y, q.z, q.w, cy), i_lo);
+            if (L <= i_hi) atomicXor(R + ((L >> 5) - w_lo), 1u << (L & 31));
+        }
     }
     __syncwarp();
-    if (m > kTCrossCap) return -1;
-    if (m > 1) tsort(cross, m, lane);
-    return m;
-}
-
-// Row crossings by all edges of the polygon, one pixel at a time (a row with
-// more crossings than the buffer: pathological polygons only).
-__device__ __forceinline__ bool pixel_inside(const int2* pv, int n, int i, int j) {
-    const int32_t cy = j * kSub + kSub / 2;
-    bool inside = false;
-    for (int k = 0; k < n; ++k) {
-        const int2 A = pv[k];
-        const int2 B = pv[(k + 1 == n) ? 0 : k + 1];
-        if (cross_row(A.y, B.y, cy)) inside ^= (i < cross_L(A.x, A.y, B.x, B.y, cy));
+    uint32_t carry = 0u;   // parity of the toggles in the words before this chunk
+    for (int w0 = 0; w0 < nw; w0 += 32) {
+        const int w = w0 + lane;
+        const uint32_t t = w < nw ? R[w] : 0u;
+        const unsigned odd = __ballot_sync(0xffffffffu, (__popc(t) & 1) != 0);
+        uint32_t x = t;   // inclusive prefix parity inside the word
+        x ^= x << 1;
+        x ^= x << 2;
+        x ^= x << 4;
+        x ^= x << 8;
+        x ^= x << 16;
+        if (((unsigned)__popc(odd & ((1u << lane) - 1u)) & 1u) ^ carry) x = ~x;
+        if (w < nw) {
+            const int x0 = (w_lo + w) * 32;
+            const int a0 = max(i_lo - x0, 0), b0 = min(i_hi + 1 - x0, 32);
+            R[w] = a0 < b0 ? (x & bitrange(a0, b0)) : 0u;
+        }
+        carry ^= (unsigned)__popc(odd) & 1u;
     }
-    return inside;
+    __syncwarp();
 }
 
 template <int MODE>
@@ -118,10 +97,9 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
     const int TP = a.T * a.P;
     const int total = a.band_start[TP];
     int4* my_edge = s_tier + (size_t)warp * kTEdgeCap;
-    int* my_cross = reinterpret_cast<int*>(s_tier + (size_t)kTW * kTEdgeCap) + (size_t)warp * kTCrossCap;
-    uint32_t* my_I = reinterpret_cast<uint32_t*>(reinterpret_cast<int*>(s_tier + (size_t)kTW * kTEdgeCap) +
-                                                 (size_t)kTW * kTCrossCap) + (size_t)warp * 2 * kTWords;
+    uint32_t* my_I = reinterpret_cast<uint32_t*>(s_tier + (size_t)kTW * kTEdgeCap) + (size_t)warp * 3 * kTWords;
     uint32_t* my_U = my_I + kTWords;
+    uint32_t* my_R = my_U + kTWords;
     for (;;) {
         int item = 0, tp = 0;
         if (lane == 0) {
@@ -176,71 +154,25 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
         __syncwarp();
 
         // I: pixels covered on every row of the block row; U: on some row
+        const int nw = w_hi - w_lo + 1;
         const bool rows_ok = jb + kTBand - 1 <= a.resy - 1;
-        for (int w = w_lo + lane; w <= w_hi; w += 32) {
-            const int x0 = w * 32;
+        for (int w = lane; w < nw; w += 32) {
+            const int x0 = (w_lo + w) * 32;
             const int a0 = max(i_lo - x0, 0), b0 = min(i_hi + 1 - x0, 32);
-            my_I[w - w_lo] = (rows_ok && a0 < b0) ? ((b0 >= 32 ? 0xFFFFFFFFu : ((1u << b0) - 1u)) & ~((1u << a0) - 1u)) : 0u;
-            if (MODE == MODE_TIER_CLASSIFY) my_U[w - w_lo] = 0u;
+            my_I[w] = (rows_ok && a0 < b0) ? bitrange(a0, b0) : 0u;
+            my_U[w] = 0u;
         }
         __syncwarp();
-        bool slow = false;
-        for (int r = 0; r < kTBand && MODE != MODE_TIER_LABEL; ++r) {
-            const int j = jb + r;
-            const bool live = j <= a.resy - 1 && j >= j_lo && j <= j_hi;
-            int m = live ? row_crossings(j, my_edge, nb, overflow, pv, n, my_cross, lane) : 0;
-            if (m < 0) {
-                slow = true;
-                m = 0;
-            }
-            if (MODE == MODE_TIER_CLASSIFY) {
-                for (int w = w_lo + lane; w <= w_hi; w += 32) {
-                    const int x0 = w * 32;
-                    uint32_t v = 0u;
-                    for (int s = 0; s + 1 < m; s += 2) {
-                        const int L = max(max(my_cross[s], i_lo), x0), R = min(min(my_cross[s + 1], i_hi + 1), x1_of(x0));
-                        if (L < R) v |= bitrange(L - x0, R - x0);
-                    }
-                    if (slow && live) {
-                        // pathological row: every pixel of the word by the full test
-                        v = 0u;
-                        for (int b = 0; b < 32; ++b) {
-                            const int i = x0 + b;
-                            if (i >= i_lo && i <= i_hi && pixel_inside(pv, n, i, j)) v |= 1u << b;
-                        }
-                    }
-                    my_I[w - w_lo] &= v;
-                    my_U[w - w_lo] |= v;
+        if (MODE != MODE_TIER_LABEL) {
+            for (int r = 0; r < kTBand; ++r) {
+                const int j = jb + r;
+                const bool live = j <= a.resy - 1 && j >= j_lo && j <= j_hi;
+                if (live) row_cover(j, my_edge, nb, overflow, pv, n, i_lo, i_hi, w_lo, nw, my_R, lane);
+                for (int w = lane; w < nw; w += 32) {
+                    const uint32_t v = live ? my_R[w] : 0u;
+                    my_I[w] &= v;
+                    if (MODE == MODE_TIER_CLASSIFY) my_U[w] |= v;
                 }
-                slow = false;
-                __syncwarp();
-            } else if (MODE == MODE_TIER_REDUCE) {
-                // full blocks are counted once below; pixels of the others
-                // (mixed blocks) are visited along the row's spans
-                if (!live) {
-                    for (int w = w_lo + lane; w <= w_hi; w += 32) my_I[w - w_lo] = 0u;
-                    __syncwarp();
-                    continue;
-                }
-                // I over the band must be complete before the pixel visits, so the
-                // canvas modes make two sweeps: this one narrows I ...
-                for (int w = w_lo + lane; w <= w_hi; w += 32) {
-                    const int x0 = w * 32;
-                    uint32_t v = 0u;
-                    if (!slow) {
-                        for (int s = 0; s + 1 < m; s += 2) {
-                            const int L = max(max(my_cross[s], i_lo), x0), R = min(min(my_cross[s + 1], i_hi + 1), x1_of(x0));
-                            if (L < R) v |= bitrange(L - x0, R - x0);
-                        }
-                    } else {
-                        for (int b = 0; b < 32; ++b) {
-                            const int i = x0 + b;
-                            if (i >= i_lo && i <= i_hi && pixel_inside(pv, n, i, j)) v |= 1u << b;
-                        }
-                    }
-                    my_I[w - w_lo] &= v;
-                }
-                slow = false;
                 __syncwarp();
             }
         }
@@ -261,7 +193,7 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
             continue;
         }
 
-        // ---- canvas modes: second sweep over the rows
+        // ---- canvas modes
         unsigned long long acc_c = 0;
         long long acc_s = 0;
         if (MODE == MODE_TIER_REDUCE) {
@@ -275,47 +207,37 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
                 }
             }
         }
+        // covered pixels of the blocks that are not full for p (reduce) or of
+        // the mixed blocks (labels): the pixel slots
         for (int r = 0; r < kTBand; ++r) {
             const int j = jb + r;
             if (!(j <= a.resy - 1 && j >= j_lo && j <= j_hi)) continue;
-            const int m = row_crossings(j, my_edge, nb, overflow, pv, n, my_cross, lane);
-            // block columns of the row's spans that are not full for p
-            auto visit_block = [&](int bc, int L, int R) {
-                // pixels [L, R) of block column bc on row j (mixed block)
-                const size_t b = blk0 + bc;
-                const int sl = __ldg(tr.slot + b);
-                const size_t base = (size_t)sl * 256 + (size_t)(j & 15) * 16;
-                for (int i = L; i < R; ++i) {
-                    const size_t q = base + (i & 15);
-                    if (MODE == MODE_TIER_LABEL) {
-                        tr.plabel[q] = (uint16_t)p;
-                        ++acc_c;
-                    } else {
-                        acc_c += __ldg(tr.pcnt + q);
-                        if (tr.psum) acc_s += __ldg(tr.psum + q);
+            row_cover(j, my_edge, nb, overflow, pv, n, i_lo, i_hi, w_lo, nw, my_R, lane);
+            for (int w = lane; w < nw; w += 32) {
+                const uint32_t bits = my_R[w];
+                if (!bits) continue;
+                const int x0 = (w_lo + w) * 32;
+                #pragma unroll
+                for (int half = 0; half < 2; ++half) {
+                    uint32_t hb = (bits >> (half * 16)) & 0xFFFFu;
+                    if (!hb) continue;
+                    if (MODE == MODE_TIER_REDUCE && ((my_I[w] >> (half * 16)) & 0xFFFFu) == 0xFFFFu) continue;
+                    const int bc = (x0 >> 4) + half;
+                    const size_t b = blk0 + bc;
+                    if (MODE == MODE_TIER_LABEL && !__ldg(tr.mixed + b)) continue;
+                    const size_t base = (size_t)__ldg(tr.slot + b) * 256 + (size_t)(j & 15) * 16;
+                    while (hb) {
+                        const int bit = __ffs(hb) - 1;
+                        hb &= hb - 1u;
+                        const size_t q = base + bit;   // (x0 + 16 * half + bit) & 15 == bit
+                        if (MODE == MODE_TIER_LABEL) {
+                            tr.plabel[q] = (uint16_t)p;
+                            ++acc_c;
+                        } else {
+                            acc_c += __ldg(tr.pcnt + q);
+                            if (tr.psum) acc_s += __ldg(tr.psum + q);
+                        }
                     }
-                }
-            };
-            if (m >= 0) {
-                for (int s = 0; s + 1 < m; s += 2) {
-                    const int L = max(my_cross[s], i_lo), R = min(my_cross[s + 1], i_hi + 1);
-                    if (L >= R) continue;
-                    for (int bc = (L >> 4) + lane; bc <= ((R - 1) >> 4); bc += 32) {
-                        const int w = (bc >> 1) - w_lo;
-                        const bool full = ((my_I[w] >> ((bc & 1) * 16)) & 0xFFFFu) == 0xFFFFu;
-                        if (full && MODE == MODE_TIER_REDUCE) continue;
-                        if (MODE == MODE_TIER_LABEL && !__ldg(tr.mixed + blk0 + bc)) continue;
-                        visit_block(bc, max(L, bc * 16), min(R, bc * 16 + 16));
-                    }
-                }
-            } else {
-                for (int bc = (i_lo >> 4) + lane; bc <= (i_hi >> 4); bc += 32) {
-                    const int w = (bc >> 1) - w_lo;
-                    const bool full = ((my_I[w] >> ((bc & 1) * 16)) & 0xFFFFu) == 0xFFFFu;
-                    if (full && MODE == MODE_TIER_REDUCE) continue;
-                    if (MODE == MODE_TIER_LABEL && !__ldg(tr.mixed + blk0 + bc)) continue;
-                    for (int i = max(bc * 16, i_lo); i < min(bc * 16 + 16, i_hi + 1); ++i)
-                        if (pixel_inside(pv, n, i, j)) visit_block(bc, i, i + 1);
                 }
             }
             __syncwarp();
