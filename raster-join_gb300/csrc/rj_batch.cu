@@ -545,6 +545,7 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
         // ---- batch columns, query descriptors, segments
         BatchArgs ba{};
         ba.xy = (const float2*)find_col(ctx, ctx->loc_attrib)->d;
+        ba.zones = ctx->zones_valid ? (const float4*)ctx->zones.p : nullptr;
         std::vector<const uint32_t*> ucols;
         std::vector<int> utyps;
         auto slot_of = [&](const uint32_t* col, int typ) {
@@ -781,6 +782,8 @@ int execute_batch(Engine& e, int nq, const rj_query* qs, const rj_query* const* 
             }
             plan_query(ctx, p, (flags & RJ_BATCH_NO_FUSE) != 0);
         }
+        const int zrc = ensure_zones(ctx, true);   // lets the point pass skip rows far from a query
+        if (zrc) return zrc;
     }
     const double t_setup = now_ms();
     BatchOut bo;

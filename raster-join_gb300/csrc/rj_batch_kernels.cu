@@ -64,116 +64,132 @@ __device__ __forceinline__ void hist_init(uint32_t* s_cnt, unsigned long long* s
     __syncthreads();
 }
 
+// The columns one query reads, in shared memory (read as broadcasts inside
+// the row loops instead of being held in registers): device pointers for the
+// direct pass, staged column slots for the staged one.
+struct QueryCols {
+    const uint32_t* col[kBatchMaxCols];
+    int slot[kBatchMaxCols];
+    uint32_t lo[kBatchMaxCols], span[kBatchMaxCols];
+    int typ[kBatchMaxCols];
+    int n;       // columns with a predicate or the aggregate
+    int aggr;    // index of the aggregate column in the list, or -1
+};
+
+// Fills `qc` for query Q (thread 0) and publishes it to the block.
+__device__ __forceinline__ void load_query_cols(const BatchArgs& a, const BatchQuery* __restrict__ Q, QueryCols* qc) {
+    if (threadIdx.x == 0) {
+        // a predicate narrower than the full range, or the aggregate
+        int n = 0;
+        qc->aggr = -1;
+        for (int u = 0; u < a.nu; ++u) {
+            const uint32_t lo = Q->lo[u], sp = Q->span[u];
+            if (lo == 0u && sp == 0xFFFFFFFFu && u != Q->aggr_u) continue;
+            if (u == Q->aggr_u) qc->aggr = n;
+            qc->col[n] = a.ucol[u];
+            qc->slot[n] = u;
+            qc->typ[n] = a.utyp[u];
+            qc->lo[n] = lo;
+            qc->span[n] = sp;
+            ++n;
+        }
+        qc->n = n;
+    }
+    __syncthreads();
+}
+
+// The four points x/y/v/mask of one thread through the mapper of MODE.
+template <int MODE, bool AGG, bool SMEM>
+__device__ __forceinline__ void map_points4(const BatchQuery* __restrict__ Q, const CanvasXf& cx, const float* x,
+                                            const float* y, const float* v, uint32_t mask, const Hist<AGG, SMEM>& h) {
+    const DeferQ dq{nullptr, nullptr, nullptr, nullptr};
+    if constexpr (MODE == BQ_TLABEL) {
+        const TierLabelMapper tm{cx, Q->tr};
+        uint32_t key[4];
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) key[k] = ((mask >> k) & 1u) ? tm.lookup(x[k], y[k]) : TierLabelMapper::kNone;
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) tm.consume(((mask >> k) & 1u) != 0u, key[k], x[k], y[k], v[k], h, dq);
+    } else if constexpr (MODE == BQ_TSPLAT) {
+        const TierSplatMapper tm{cx, Q->tr, Q->sum_scale};
+        uint32_t key[4];
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) key[k] = ((mask >> k) & 1u) ? tm.lookup(x[k], y[k]) : TierSplatMapper::kNone;
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) tm.consume(((mask >> k) & 1u) != 0u, key[k], x[k], y[k], v[k], h, dq);
+    } else if constexpr (MODE == BQ_LABEL) {
+        const LabelMapper lm{cx, Q->label};
+        LabelMapper::Key key[4];
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) key[k] = ((mask >> k) & 1u) ? lm.lookup(x[k], y[k]) : LabelMapper::kNone;
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) lm.consume(((mask >> k) & 1u) != 0u, key[k], x[k], y[k], v[k], h, dq);
+    } else {
+        const SplatMapper sm{cx, Q->canvas_c, Q->canvas_s, Q->sum_scale, Q->out_nonfinite, SMEM ? 1 : 0};
+        SplatMapper::Key key[4];
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) key[k] = ((mask >> k) & 1u) ? sm.lookup(x[k], y[k]) : SplatMapper::kNone;
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) sm.consume(((mask >> k) & 1u) != 0u, key[k], x[k], y[k], v[k], h, dq);
+    }
+}
+
+// Staged rows [0, nrows) of one query with the mapper of MODE (one loop per
+// mode, so only that mapper's state is live in it).
+template <int MODE, bool AGG, bool SMEM, int BLOCK>
+__device__ __forceinline__ void staged_rows(const BatchArgs& a, const BatchQuery* __restrict__ Q, const float2* s_xy,
+                                            const uint32_t* s_col, int nrows, const Hist<AGG, SMEM>& h,
+                                            const QueryCols* qc) {
+    const int tid = threadIdx.x;
+    const int ncu = qc->n, aggc = qc->aggr;
+    const int aggr_typ = Q->aggr_typ;
+    const CanvasXf cx = Q->cx;
+    for (int base = 0; base < nrows; base += 4 * BLOCK) {
+        float x[4], y[4], v[4];
+        uint32_t mask = 0u;
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int r = base + k * BLOCK + tid;
+            x[k] = y[k] = v[k] = 0.f;
+            if (r >= nrows) continue;
+            const float2 p = s_xy[r];
+            x[k] = p.x;
+            y[k] = p.y;
+            bool ok = true;
+            #pragma unroll 1
+            for (int u = 0; u < ncu; ++u) {
+                const uint32_t c = s_col[qc->slot[u] * a.rows + r];
+                ok = ok && (order_key(qc->typ[u], c) - qc->lo[u] <= qc->span[u]);
+                if (AGG && u == aggc) v[k] = agg_value(aggr_typ, c);
+            }
+            if (ok) mask |= 1u << k;
+        }
+        map_points4<MODE, AGG, SMEM>(Q, cx, x, y, v, mask, h);
+    }
+}
+
 template <bool AGG, bool SMEM, int BLOCK>
 __device__ __forceinline__ void batch_query(const BatchArgs& a, const BatchQuery* __restrict__ Q,
                                             const float2* s_xy, const uint32_t* s_col, int nrows,
                                             uint32_t* s_cnt, unsigned long long* s_sum, int* s_touch,
-                                            int* s_ntouch) {
-    const int tid = threadIdx.x;
-    const int mode = Q->mode;
-    const int P = Q->P;
-    uint32_t lo[kBatchMaxCols], span[kBatchMaxCols];
-    #pragma unroll
-    for (int u = 0; u < kBatchMaxCols; ++u) {
-        lo[u] = Q->lo[u];
-        span[u] = Q->span[u];
-    }
-    const int aggr_u = Q->aggr_u;
-    const int aggr_typ = Q->aggr_typ;
-    (void)P;
+                                            int* s_ntouch, QueryCols* qc) {
+    load_query_cols(a, Q, qc);
     Hist<AGG, SMEM> h{s_cnt, s_sum, Q->out_count, Q->out_sum, Q->out_nonfinite, Q->sum_scale};
     h.s_touched = s_touch;
     h.s_ntouched = s_ntouch;
-    const DeferQ dq{nullptr, nullptr, nullptr, nullptr};
-    const CanvasXf cx = Q->cx;
-    if (mode == BQ_TLABEL || mode == BQ_TSPLAT) {
-        const TierLabelMapper ml{cx, Q->tr};
-        const TierSplatMapper ms{cx, Q->tr, Q->sum_scale};
-        for (int base = 0; base < nrows; base += 4 * BLOCK) {
-            float x[4], y[4], v[4];
-            bool ok[4];
-            uint32_t key[4];
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int r = base + k * BLOCK + tid;
-                ok[k] = r < nrows;
-                x[k] = y[k] = v[k] = 0.f;
-                key[k] = 0xFFFFFFFFu;
-                if (ok[k]) {
-                    const float2 p = s_xy[r];
-                    x[k] = p.x;
-                    y[k] = p.y;
-                    #pragma unroll
-                    for (int u = 0; u < kBatchMaxCols; ++u)
-                        if (u < a.nu) ok[k] = ok[k] && (order_key(a.utyp[u], s_col[u * a.rows + r]) - lo[u] <= span[u]);
-                    if (AGG && ok[k]) v[k] = agg_value(aggr_typ, s_col[aggr_u * a.rows + r]);
-                    if (ok[k]) key[k] = mode == BQ_TLABEL ? ml.lookup(x[k], y[k]) : ms.lookup(x[k], y[k]);
-                }
-            }
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (mode == BQ_TLABEL) ml.consume(ok[k], key[k], x[k], y[k], v[k], h, dq);
-                else ms.consume(ok[k], key[k], x[k], y[k], v[k], h, dq);
-            }
-        }
-    } else if (mode == BQ_LABEL) {
-        const LabelMapper m{cx, Q->label};
-        for (int base = 0; base < nrows; base += 4 * BLOCK) {
-            float x[4], y[4], v[4];
-            bool ok[4];
-            LabelMapper::Key key[4];
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int r = base + k * BLOCK + tid;
-                ok[k] = r < nrows;
-                x[k] = y[k] = v[k] = 0.f;
-                key[k] = LabelMapper::kNone;
-                if (ok[k]) {
-                    const float2 p = s_xy[r];
-                    x[k] = p.x;
-                    y[k] = p.y;
-                    #pragma unroll
-                    for (int u = 0; u < kBatchMaxCols; ++u)
-                        if (u < a.nu) ok[k] = ok[k] && (order_key(a.utyp[u], s_col[u * a.rows + r]) - lo[u] <= span[u]);
-                    if (AGG && ok[k]) v[k] = agg_value(aggr_typ, s_col[aggr_u * a.rows + r]);
-                    if (ok[k]) key[k] = m.lookup(x[k], y[k]);
-                }
-            }
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) m.consume(ok[k], key[k], x[k], y[k], v[k], h, dq);
-        }
-    } else {
-        const SplatMapper m{cx, Q->canvas_c, Q->canvas_s, Q->sum_scale, Q->out_nonfinite, SMEM ? 1 : 0};
-        for (int base = 0; base < nrows; base += 4 * BLOCK) {
-            float x[4], y[4], v[4];
-            bool ok[4];
-            SplatMapper::Key key[4];
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int r = base + k * BLOCK + tid;
-                ok[k] = r < nrows;
-                x[k] = y[k] = v[k] = 0.f;
-                key[k] = SplatMapper::kNone;
-                if (ok[k]) {
-                    const float2 p = s_xy[r];
-                    x[k] = p.x;
-                    y[k] = p.y;
-                    #pragma unroll
-                    for (int u = 0; u < kBatchMaxCols; ++u)
-                        if (u < a.nu) ok[k] = ok[k] && (order_key(a.utyp[u], s_col[u * a.rows + r]) - lo[u] <= span[u]);
-                    if (AGG && ok[k]) v[k] = agg_value(aggr_typ, s_col[aggr_u * a.rows + r]);
-                    if (ok[k]) key[k] = m.lookup(x[k], y[k]);
-                }
-            }
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) m.consume(ok[k], key[k], x[k], y[k], v[k], h, dq);
-        }
+    switch (Q->mode) {
+        case BQ_TLABEL: staged_rows<BQ_TLABEL, AGG, SMEM, BLOCK>(a, Q, s_xy, s_col, nrows, h, qc); break;
+        case BQ_TSPLAT: staged_rows<BQ_TSPLAT, AGG, SMEM, BLOCK>(a, Q, s_xy, s_col, nrows, h, qc); break;
+        case BQ_LABEL: staged_rows<BQ_LABEL, AGG, SMEM, BLOCK>(a, Q, s_xy, s_col, nrows, h, qc); break;
+        default: staged_rows<BQ_SPLAT, AGG, SMEM, BLOCK>(a, Q, s_xy, s_col, nrows, h, qc); break;
     }
+    // the flush's barriers also keep qc until every thread is done with it
     if (SMEM) flush_touched<AGG, BLOCK>(Q, s_cnt, s_sum, s_touch, s_ntouch);
+    else __syncthreads();
 }
 
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_batch_points(BatchArgs a) {
+__global__ void __launch_bounds__(BLOCK, 768 / BLOCK) k_batch_points(BatchArgs a) {
     extern __shared__ unsigned long long smem_b[];
     unsigned long long* s_sum = smem_b;
     uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_sum + a.hist_cap);
@@ -184,6 +200,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch_points(BatchArgs a) {
     __shared__ int s_seg;
     __shared__ int s_ntouch;
     __shared__ float4 s_box[BLOCK / 32 + 1];
+    __shared__ QueryCols s_qc;
     const int tid = threadIdx.x;
     hist_init(s_cnt, s_sum, a.hist_cap, &s_ntouch);
     for (;;) {
@@ -252,11 +269,11 @@ __global__ void __launch_bounds__(BLOCK) k_batch_points(BatchArgs a) {
             const bool agg = Q->aggr_u >= 0;
             const bool smem = Q->hist_smem != 0;
             if (agg) {
-                if (smem) batch_query<true, true, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum, s_touch, &s_ntouch);
-                else batch_query<true, false, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum, s_touch, &s_ntouch);
+                if (smem) batch_query<true, true, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum, s_touch, &s_ntouch, &s_qc);
+                else batch_query<true, false, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum, s_touch, &s_ntouch, &s_qc);
             } else {
-                if (smem) batch_query<false, true, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum, s_touch, &s_ntouch);
-                else batch_query<false, false, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum, s_touch, &s_ntouch);
+                if (smem) batch_query<false, true, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum, s_touch, &s_ntouch, &s_qc);
+                else batch_query<false, false, BLOCK>(a, Q, s_xy, s_col, nrows, s_cnt, s_sum, s_touch, &s_ntouch, &s_qc);
             }
         }
         __syncthreads();   // the staged rows are overwritten by the next item
@@ -269,32 +286,29 @@ __global__ void __launch_bounds__(BLOCK) k_batch_points(BatchArgs a) {
 // L2 and the others of the segment hit it there (the last one reads with
 // evict-first).  Items are longer (more rows per histogram flush); segment
 // boundaries are multiples of four rows, so the vector loads stay aligned.
-template <bool AGG, bool SMEM, int BLOCK>
-__device__ __forceinline__ void direct_query(const BatchArgs& a, const BatchQuery* __restrict__ Q, uint64_t r0,
-                                             uint64_t r1, bool last, uint32_t* s_cnt, unsigned long long* s_sum,
-                                             int* s_touch, int* s_ntouch) {
+//
+// direct_rows: rows [r0, r1) of one query with the mapper of MODE (one loop
+// per mode, so only that mapper's state is live in it).
+template <int MODE, bool AGG, bool SMEM, int BLOCK>
+__device__ __forceinline__ void direct_rows(const BatchArgs& a, const BatchQuery* __restrict__ Q, uint64_t r0,
+                                            uint64_t r1, bool last, const Hist<AGG, SMEM>& h, const QueryCols* dc) {
     const int tid = threadIdx.x;
-    const int mode = Q->mode;
-    const int P = Q->P;
-    uint32_t lo[kBatchMaxCols], span[kBatchMaxCols];
-    bool used[kBatchMaxCols];
-    const int aggr_u = Q->aggr_u;
-    #pragma unroll
-    for (int u = 0; u < kBatchMaxCols; ++u) {
-        lo[u] = Q->lo[u];
-        span[u] = Q->span[u];
-        used[u] = u < a.nu && (lo[u] != 0u || span[u] != 0xFFFFFFFFu || u == aggr_u);
-    }
+    const int ncu = dc->n, aggc = dc->aggr;
     const int aggr_typ = Q->aggr_typ;
-    (void)P;
-    Hist<AGG, SMEM> h{s_cnt, s_sum, Q->out_count, Q->out_sum, Q->out_nonfinite, Q->sum_scale};
-    h.s_touched = s_touch;
-    h.s_ntouched = s_ntouch;
-    const DeferQ dq{nullptr, nullptr, nullptr, nullptr};
+    const float4 qb = Q->box;
     const CanvasXf cx = Q->cx;
-    const LabelMapper lm{cx, Q->label};
-    const SplatMapper sm{cx, Q->canvas_c, Q->canvas_s, Q->sum_scale, Q->out_nonfinite, SMEM ? 1 : 0};
     for (uint64_t tb = r0; tb < r1; tb += (uint64_t)BLOCK * 4) {
+        if (a.zones) {
+            // skip rows whose zones lie apart from the query's polygons (uniform)
+            const uint64_t z0 = tb >> kZoneShift;
+            const uint64_t z1 = (min(tb + (uint64_t)BLOCK * 4, r1) - 1) >> kZoneShift;
+            bool meets = false;
+            for (uint64_t z = z0; z <= z1; ++z) {
+                const float4 b = __ldg(a.zones + z);
+                meets |= !(b.z < qb.x || b.x > qb.z || b.w < qb.y || b.y > qb.w);
+            }
+            if (!meets) continue;
+        }
         const uint64_t base = tb + (uint64_t)tid * 4;
         float x[4], y[4], v[4];
         uint32_t mask = 0u;
@@ -307,15 +321,15 @@ __device__ __forceinline__ void direct_query(const BatchArgs& a, const BatchQuer
             x[2] = p1.x; y[2] = p1.y; x[3] = p1.z; y[3] = p1.w;
             v[0] = v[1] = v[2] = v[3] = 0.f;
             mask = 0xFu;
-            #pragma unroll
-            for (int u = 0; u < kBatchMaxCols; ++u) {
-                if (!used[u]) continue;
-                const uint4 c = last ? __ldcs(reinterpret_cast<const uint4*>(a.ucol[u] + base))
-                                     : __ldcg(reinterpret_cast<const uint4*>(a.ucol[u] + base));
-                const int t = a.utyp[u];
-                mask &= ((order_key(t, c.x) - lo[u] <= span[u]) ? 1u : 0u) | ((order_key(t, c.y) - lo[u] <= span[u]) ? 2u : 0u) |
-                        ((order_key(t, c.z) - lo[u] <= span[u]) ? 4u : 0u) | ((order_key(t, c.w) - lo[u] <= span[u]) ? 8u : 0u);
-                if (AGG && u == aggr_u) {
+            #pragma unroll 1
+            for (int u = 0; u < ncu; ++u) {
+                const uint4* cp = reinterpret_cast<const uint4*>(dc->col[u] + base);
+                const uint4 c = last ? __ldcs(cp) : __ldcg(cp);
+                const int t = dc->typ[u];
+                const uint32_t lo = dc->lo[u], sp = dc->span[u];
+                mask &= ((order_key(t, c.x) - lo <= sp) ? 1u : 0u) | ((order_key(t, c.y) - lo <= sp) ? 2u : 0u) |
+                        ((order_key(t, c.z) - lo <= sp) ? 4u : 0u) | ((order_key(t, c.w) - lo <= sp) ? 8u : 0u);
+                if (AGG && u == aggc) {
                     v[0] = agg_value(aggr_typ, c.x); v[1] = agg_value(aggr_typ, c.y);
                     v[2] = agg_value(aggr_typ, c.z); v[3] = agg_value(aggr_typ, c.w);
                 }
@@ -330,49 +344,40 @@ __device__ __forceinline__ void direct_query(const BatchArgs& a, const BatchQuer
                 x[k] = p.x;
                 y[k] = p.y;
                 bool ok = true;
-                #pragma unroll
-                for (int u = 0; u < kBatchMaxCols; ++u) {
-                    if (!used[u]) continue;
-                    const uint32_t c = a.ucol[u][i];
-                    ok = ok && (order_key(a.utyp[u], c) - lo[u] <= span[u]);
-                    if (AGG && u == aggr_u) v[k] = agg_value(aggr_typ, c);
+                #pragma unroll 1
+                for (int u = 0; u < ncu; ++u) {
+                    const uint32_t c = dc->col[u][i];
+                    ok = ok && (order_key(dc->typ[u], c) - dc->lo[u] <= dc->span[u]);
+                    if (AGG && u == aggc) v[k] = agg_value(aggr_typ, c);
                 }
                 if (ok) mask |= 1u << k;
             }
         }
-        if (mode == BQ_TLABEL) {
-            const TierLabelMapper tm{cx, Q->tr};
-            uint32_t key[4];
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) key[k] = ((mask >> k) & 1u) ? tm.lookup(x[k], y[k]) : TierLabelMapper::kNone;
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) tm.consume(((mask >> k) & 1u) != 0u, key[k], x[k], y[k], v[k], h, dq);
-        } else if (mode == BQ_TSPLAT) {
-            const TierSplatMapper tm{cx, Q->tr, Q->sum_scale};
-            uint32_t key[4];
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) key[k] = ((mask >> k) & 1u) ? tm.lookup(x[k], y[k]) : TierSplatMapper::kNone;
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) tm.consume(((mask >> k) & 1u) != 0u, key[k], x[k], y[k], v[k], h, dq);
-        } else if (mode == BQ_LABEL) {
-            LabelMapper::Key key[4];
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) key[k] = ((mask >> k) & 1u) ? lm.lookup(x[k], y[k]) : LabelMapper::kNone;
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) lm.consume(((mask >> k) & 1u) != 0u, key[k], x[k], y[k], v[k], h, dq);
-        } else {
-            SplatMapper::Key key[4];
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) key[k] = ((mask >> k) & 1u) ? sm.lookup(x[k], y[k]) : SplatMapper::kNone;
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) sm.consume(((mask >> k) & 1u) != 0u, key[k], x[k], y[k], v[k], h, dq);
-        }
+        map_points4<MODE, AGG, SMEM>(Q, cx, x, y, v, mask, h);
     }
+}
+
+template <bool AGG, bool SMEM, int BLOCK>
+__device__ __forceinline__ void direct_query(const BatchArgs& a, const BatchQuery* __restrict__ Q, uint64_t r0,
+                                             uint64_t r1, bool last, uint32_t* s_cnt, unsigned long long* s_sum,
+                                             int* s_touch, int* s_ntouch, QueryCols* dc) {
+    load_query_cols(a, Q, dc);
+    Hist<AGG, SMEM> h{s_cnt, s_sum, Q->out_count, Q->out_sum, Q->out_nonfinite, Q->sum_scale};
+    h.s_touched = s_touch;
+    h.s_ntouched = s_ntouch;
+    switch (Q->mode) {
+        case BQ_TLABEL: direct_rows<BQ_TLABEL, AGG, SMEM, BLOCK>(a, Q, r0, r1, last, h, dc); break;
+        case BQ_TSPLAT: direct_rows<BQ_TSPLAT, AGG, SMEM, BLOCK>(a, Q, r0, r1, last, h, dc); break;
+        case BQ_LABEL: direct_rows<BQ_LABEL, AGG, SMEM, BLOCK>(a, Q, r0, r1, last, h, dc); break;
+        default: direct_rows<BQ_SPLAT, AGG, SMEM, BLOCK>(a, Q, r0, r1, last, h, dc); break;
+    }
+    // the flush's barriers also keep dc until every thread is done with it
     if (SMEM) flush_touched<AGG, BLOCK>(Q, s_cnt, s_sum, s_touch, s_ntouch);
+    else __syncthreads();
 }
 
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_batch_direct(BatchArgs a) {
+__global__ void __launch_bounds__(BLOCK, 768 / BLOCK) k_batch_direct(BatchArgs a) {
     extern __shared__ unsigned long long smem_b[];
     unsigned long long* s_sum = smem_b;
     uint32_t* s_cnt = reinterpret_cast<uint32_t*>(s_sum + a.hist_cap);
@@ -380,6 +385,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch_direct(BatchArgs a) {
     __shared__ unsigned long long s_item;
     __shared__ int s_seg;
     __shared__ int s_ntouch;
+    __shared__ QueryCols s_dc;
     const int tid = threadIdx.x;
     hist_init(s_cnt, s_sum, a.hist_cap, &s_ntouch);
     for (;;) {
@@ -411,11 +417,11 @@ __global__ void __launch_bounds__(BLOCK) k_batch_direct(BatchArgs a) {
             const bool agg = Q->aggr_u >= 0;
             const bool smem = Q->hist_smem != 0;
             if (agg) {
-                if (smem) direct_query<true, true, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum, s_touch, &s_ntouch);
-                else direct_query<true, false, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum, s_touch, &s_ntouch);
+                if (smem) direct_query<true, true, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum, s_touch, &s_ntouch, &s_dc);
+                else direct_query<true, false, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum, s_touch, &s_ntouch, &s_dc);
             } else {
-                if (smem) direct_query<false, true, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum, s_touch, &s_ntouch);
-                else direct_query<false, false, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum, s_touch, &s_ntouch);
+                if (smem) direct_query<false, true, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum, s_touch, &s_ntouch, &s_dc);
+                else direct_query<false, false, BLOCK>(a, Q, r0, r1, last, s_cnt, s_sum, s_touch, &s_ntouch, &s_dc);
             }
         }
         __syncthreads();   // s_item is rewritten for the next item

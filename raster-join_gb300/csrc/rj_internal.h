@@ -191,5 +191,6 @@ void decode_result(int P, const unsigned long long* hc, const unsigned long long
                    const long long* hb, rj_result* res);
 void free_batch_engine(rj_ctx* ctx);
 void query_rows(const rj_ctx* ctx, const rj_query* q, uint64_t& r0, uint64_t& r1);
+int ensure_zones(rj_ctx* ctx, bool sync);
 
 }  // namespace rjh

@@ -256,6 +256,7 @@ struct BatchArgs {
     unsigned long long* work;             // work-item counter (zeroed before the launch)
     int rows;                             // rows per work item
     int hist_cap;                         // shared-memory histogram entries
+    const float4* zones;                  // bounds of every 2^kZoneShift table rows, or null
 };
 
 // block shape of the batched kernel (picked by the tuner)

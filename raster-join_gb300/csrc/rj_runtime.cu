@@ -1158,6 +1158,24 @@ void free_polyset(rj_ctx* ctx, PolySet& s) {
     s.P = s.V = 0;
 }
 
+// Zone map of an owned resident table (built once per table order; caller
+// held columns may change between calls, so they get none).  With `sync` the
+// map is complete on return, for kernels on other streams.
+int ensure_zones(rj_ctx* ctx, bool sync) {
+    bool owned_all = !ctx->streamed;
+    for (const Column& c : ctx->cols) owned_all = owned_all && c.owned;
+    if (!owned_all) ctx->zones_valid = false;
+    if (ctx->zones_valid || !owned_all || ctx->npts == 0) return RJ_OK;
+    const uint64_t nz = (ctx->npts + (1ull << kZoneShift) - 1) >> kZoneShift;
+    int rc;
+    if ((rc = dev_alloc(ctx, ctx->zones, nz * sizeof(float4)))) return rc;
+    launch_zone_boxes((const float2*)find_col(ctx, ctx->loc_attrib)->d, ctx->npts, (float4*)ctx->zones.p, ctx->sms,
+                      ctx->stream);
+    if (sync && cudaStreamSynchronize(ctx->stream) != cudaSuccess) return fail(ctx, RJ_E_CUDA, "zone map build failed");
+    ctx->zones_valid = true;
+    return RJ_OK;
+}
+
 void query_rows(const rj_ctx* ctx, const rj_query* q, uint64_t& r0, uint64_t& r1) {
     r0 = 0;
     r1 = ctx->npts;
@@ -1519,16 +1537,7 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
         ctx->cache_version = ctx->ps->version;
     }
     query_rows(ctx, q, ctx->row0, ctx->row1);
-    bool owned_all = !ctx->streamed;
-    for (const Column& c : ctx->cols) owned_all = owned_all && c.owned;
-    if (!owned_all) ctx->zones_valid = false;   // caller-held columns may change between calls
-    if (!ctx->zones_valid && owned_all && ctx->npts > 0) {
-        const uint64_t nz = (ctx->npts + (1ull << kZoneShift) - 1) >> kZoneShift;
-        if ((rc = dev_alloc(ctx, ctx->zones, nz * sizeof(float4)))) return rc;
-        launch_zone_boxes((const float2*)find_col(ctx, ctx->loc_attrib)->d, ctx->npts, (float4*)ctx->zones.p, ctx->sms,
-                          ctx->stream);
-        ctx->zones_valid = true;
-    }
+    if ((rc = ensure_zones(ctx, false))) return rc;
     if (q->flags & RJ_FLAG_NO_CACHE) {
         ctx->ps->grid.valid = false;
         ctx->ps->exact.valid = false;
