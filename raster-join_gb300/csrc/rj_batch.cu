@@ -545,7 +545,6 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
         // ---- batch columns, query descriptors, segments
         BatchArgs ba{};
         ba.xy = (const float2*)find_col(ctx, ctx->loc_attrib)->d;
-        ba.zones = ctx->zones_valid ? (const float4*)ctx->zones.p : nullptr;
         std::vector<const uint32_t*> ucols;
         std::vector<int> utyps;
         auto slot_of = [&](const uint32_t* col, int typ) {
@@ -607,6 +606,10 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
                 const double my = 2.0 * (p->ps->bbox[3] - p->ps->bbox[1]) / p->rp.actual_y + 1e-3;
                 d.box = make_float4((float)(p->ps->bbox[0] - mx), (float)(p->ps->bbox[1] - my),
                                     (float)(p->ps->bbox[2] + mx), (float)(p->ps->bbox[3] + my));
+                // zone checks only when the query's reach misses part of the table
+                const float4 tb = ctx->table_box;
+                const bool covers = d.box.x <= tb.x && d.box.y <= tb.y && d.box.z >= tb.z && d.box.w >= tb.w;
+                d.zones = (ctx->zones_valid && !covers) ? (const float4*)ctx->zones.p : nullptr;
             }
             if ((p->mode == BQ_LABEL || p->mode == BQ_TLABEL) && d.P <= kBatchHistCap) max_hist = std::max(max_hist, d.P);
             if (p->mode == BQ_SPLAT && p->T == 1 && p->npix <= (size_t)kBatchHistCap) {
@@ -782,7 +785,7 @@ int execute_batch(Engine& e, int nq, const rj_query* qs, const rj_query* const* 
             }
             plan_query(ctx, p, (flags & RJ_BATCH_NO_FUSE) != 0);
         }
-        const int zrc = ensure_zones(ctx, true);   // lets the point pass skip rows far from a query
+        const int zrc = ensure_zones(ctx);   // lets the point pass skip rows far from a query
         if (zrc) return zrc;
     }
     const double t_setup = now_ms();

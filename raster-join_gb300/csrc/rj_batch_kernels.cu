@@ -296,15 +296,16 @@ __device__ __forceinline__ void direct_rows(const BatchArgs& a, const BatchQuery
     const int ncu = dc->n, aggc = dc->aggr;
     const int aggr_typ = Q->aggr_typ;
     const float4 qb = Q->box;
+    const float4* zones = Q->zones;
     const CanvasXf cx = Q->cx;
     for (uint64_t tb = r0; tb < r1; tb += (uint64_t)BLOCK * 4) {
-        if (a.zones) {
+        if (zones) {
             // skip rows whose zones lie apart from the query's polygons (uniform)
             const uint64_t z0 = tb >> kZoneShift;
             const uint64_t z1 = (min(tb + (uint64_t)BLOCK * 4, r1) - 1) >> kZoneShift;
             bool meets = false;
             for (uint64_t z = z0; z <= z1; ++z) {
-                const float4 b = __ldg(a.zones + z);
+                const float4 b = __ldg(zones + z);
                 meets |= !(b.z < qb.x || b.x > qb.z || b.w < qb.y || b.y > qb.w);
             }
             if (!meets) continue;

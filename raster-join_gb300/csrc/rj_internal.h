@@ -116,6 +116,7 @@ struct rj_ctx {
     rjh::DevBuf sbuf[2];
     rjh::DevBuf zones;               // zone map of the resident table (bounds per 1024 rows)
     bool zones_valid = false;
+    float4 table_box{};              // bounds of the table's finite locations (with the zone map)
     float4 qbox{};                   // locations that can reach the current query's polygons
     int passes = 1;                  // point passes of the last query
     double copy_ms = 0;              // host->device copy time of the last query
@@ -191,6 +192,6 @@ void decode_result(int P, const unsigned long long* hc, const unsigned long long
                    const long long* hb, rj_result* res);
 void free_batch_engine(rj_ctx* ctx);
 void query_rows(const rj_ctx* ctx, const rj_query* q, uint64_t& r0, uint64_t& r1);
-int ensure_zones(rj_ctx* ctx, bool sync);
+int ensure_zones(rj_ctx* ctx);
 
 }  // namespace rjh

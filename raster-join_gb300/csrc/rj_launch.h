@@ -234,6 +234,7 @@ struct BatchQuery {
     double* out_nonfinite;                // [P]
     uint32_t* out_count32;                // private splat: counts flushed into the u32 canvas
     float4 box;                           // locations that can reach the canvas (x0, y0, x1, y1)
+    const float4* zones;                  // zone map (bounds per 2^kZoneShift rows), or null: no skip
     TierArgs tr;                          // BQ_TLABEL / BQ_TSPLAT
 };
 
@@ -256,7 +257,6 @@ struct BatchArgs {
     unsigned long long* work;             // work-item counter (zeroed before the launch)
     int rows;                             // rows per work item
     int hist_cap;                         // shared-memory histogram entries
-    const float4* zones;                  // bounds of every 2^kZoneShift table rows, or null
 };
 
 // block shape of the batched kernel (picked by the tuner)

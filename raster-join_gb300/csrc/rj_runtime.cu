@@ -564,7 +564,11 @@ PointArgs make_point_args(rj_ctx* ctx, const DevFilter& f, unsigned long long* o
     pa.out_sum = os;
     pa.out_nonfinite = (double*)ctx->scratch["out_nonfinite"].p;
     pa.err = ctx->d_err;
-    if (ctx->zones_valid && !ctx->streamed) {
+    // the zone check costs a dependent load per iteration: skip it when the
+    // query's reach holds every finite location of the table (nothing to skip)
+    const float4 tb = ctx->table_box, qb = ctx->qbox;
+    const bool covers = qb.x <= tb.x && qb.y <= tb.y && qb.z >= tb.z && qb.w >= tb.w;
+    if (ctx->zones_valid && !ctx->streamed && !covers) {
         pa.zones = (const float4*)ctx->zones.p;
         pa.row0 = r0;
         pa.qbox = ctx->qbox;
@@ -1158,20 +1162,35 @@ void free_polyset(rj_ctx* ctx, PolySet& s) {
     s.P = s.V = 0;
 }
 
-// Zone map of an owned resident table (built once per table order; caller
-// held columns may change between calls, so they get none).  With `sync` the
-// map is complete on return, for kernels on other streams.
-int ensure_zones(rj_ctx* ctx, bool sync) {
+// Zone map of an owned resident table and the bounds of its finite locations
+// (built once per table order; caller-held columns may change between calls,
+// so they get none).  Complete on return, for kernels on any stream.
+int ensure_zones(rj_ctx* ctx) {
     bool owned_all = !ctx->streamed;
     for (const Column& c : ctx->cols) owned_all = owned_all && c.owned;
     if (!owned_all) ctx->zones_valid = false;
     if (ctx->zones_valid || !owned_all || ctx->npts == 0) return RJ_OK;
     const uint64_t nz = (ctx->npts + (1ull << kZoneShift) - 1) >> kZoneShift;
     int rc;
-    if ((rc = dev_alloc(ctx, ctx->zones, nz * sizeof(float4)))) return rc;
-    launch_zone_boxes((const float2*)find_col(ctx, ctx->loc_attrib)->d, ctx->npts, (float4*)ctx->zones.p, ctx->sms,
-                      ctx->stream);
-    if (sync && cudaStreamSynchronize(ctx->stream) != cudaSuccess) return fail(ctx, RJ_E_CUDA, "zone map build failed");
+    // zones, then the bounds of the whole table's finite locations after them
+    if ((rc = dev_alloc(ctx, ctx->zones, nz * sizeof(float4) + 16))) return rc;
+    const float2* xy = (const float2*)find_col(ctx, ctx->loc_attrib)->d;
+    launch_zone_boxes(xy, ctx->npts, (float4*)ctx->zones.p, ctx->sms, ctx->stream);
+    unsigned* dbox = (unsigned*)((char*)ctx->zones.p + nz * sizeof(float4));
+    unsigned hb[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u};
+    RJ_CUDA(cudaMemcpyAsync(dbox, hb, sizeof hb, cudaMemcpyHostToDevice, ctx->stream));
+    launch_xy_bounds(xy, ctx->npts, dbox, ctx->sms, ctx->stream);
+    RJ_CUDA(cudaMemcpyAsync(hb, dbox, sizeof hb, cudaMemcpyDeviceToHost, ctx->stream));
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return fail(ctx, RJ_E_CUDA, "zone map build failed");
+    auto unorder = [](unsigned u) {   // inverse of the kernel's order-preserving map
+        const unsigned b = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+        float f;
+        std::memcpy(&f, &b, 4);
+        return f;
+    };
+    // no finite location: an empty box (lo > hi) that every query box contains
+    ctx->table_box = hb[0] > hb[2] ? make_float4(INFINITY, INFINITY, -INFINITY, -INFINITY)
+                                   : make_float4(unorder(hb[0]), unorder(hb[1]), unorder(hb[2]), unorder(hb[3]));
     ctx->zones_valid = true;
     return RJ_OK;
 }
@@ -1537,7 +1556,7 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
         ctx->cache_version = ctx->ps->version;
     }
     query_rows(ctx, q, ctx->row0, ctx->row1);
-    if ((rc = ensure_zones(ctx, false))) return rc;
+    if ((rc = ensure_zones(ctx))) return rc;
     if (q->flags & RJ_FLAG_NO_CACHE) {
         ctx->ps->grid.valid = false;
         ctx->ps->exact.valid = false;
