@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the library links or calls this file;
  * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline arm use it,
- * as the checker and the timed CPU baseline.
+ * as the parity reference of the GPU results and the timed CPU baseline.
  *
  * Every function restates one reference algorithm (paths relative to the
  * VIDA-NYU/raster-join tree) in plain C with fp32 arithmetic evaluated one
