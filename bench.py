@@ -187,6 +187,11 @@ def cpu_baseline(pts, verts, pidx, join, sample_points):
     return n, wall, tj, tb, threads
 
 
+def metric_name(join):
+    """The metric both arms report (same string, so their lines compare)."""
+    return "Gpoints/s joined (config 2: %s join; exact, so within any epsilon incl. 10 m)" % join
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -203,11 +208,11 @@ def run_reference(args):
     value = sample / step / 1e9
     line = {
         "impl": "reference",
-        "metric": "Gpoints/s joined (exact join, config 2 query)",
+        "metric": metric_name(args.join),
         "value": value, "unit": "Gpoints/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_points": sample, "parallelism": "cpu-threads"},
+        "config": {"workload": WORKLOAD, "join": args.join, "sample_points": sample, "parallelism": "cpu-threads"},
         "cpu_baseline": {"value": value, "unit": "Gpoints/s", "cores": threads, "kind": "port",
                          "sample": "CPUJoin restatement (grid 1024 built each step + join) over the first %d points "
                                    "of the config-2 table, with the config-2 filters and avg as a labelled "
@@ -513,7 +518,7 @@ def run_gb300(args):
     traffic = profiled_traffic(args.join, n)
 
     line = {
-        "metric": "Gpoints/s joined (config 2: %s join; exact, so within any epsilon incl. 10 m)" % args.join,
+        "metric": metric_name(args.join),
         "value": value, "unit": "Gpoints/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded; stands in for the NYC-taxi table)",
