@@ -19,9 +19,10 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "librj.so")
-SOURCES = ["rj_runtime.cu", "rj_point_kernels.cu", "rj_poly_kernels.cu", "rj_noalloc.cu",
-           "rj_batch.cu", "rj_batch_kernels.cu", "rj_tier_kernels.cu"]
-HEADERS = ["rj_device.cuh", "rj_launch.h", "rj_internal.h", "rj_point_map.cuh",
+SOURCES = ["rj_runtime.cu", "rj_point_kernels.cu", "rj_point_exact.cu", "rj_poly_kernels.cu", "rj_noalloc.cu",
+           "rj_batch.cu", "rj_batch_kernels.cu", "rj_batch_direct.cu", "rj_tier_kernels.cu"]
+HEADERS = ["rj_device.cuh", "rj_launch.h", "rj_internal.h", "rj_point_map.cuh", "rj_point_core.cuh",
+           "rj_batch_common.cuh",
            os.path.join("..", "..", "include", "rj.h")]
 
 NVCC_FLAGS = [
