@@ -517,6 +517,8 @@ k_points(PointArgs pa, M mp) {
 }
 
 // ---------------------------------------------------------------------------
+// The launch helpers below are static: each translation unit that includes
+// this header launches its own kernel instances and keeps its own copy.
 static int g_max_smem_optin = -1;
 
 static size_t hist_bytes(int P, bool agg) { return (size_t)P * (agg ? 12 : 4); }
