@@ -132,3 +132,36 @@ def test_compat_float_equality_semantics():
     typed = oracle.bruteforce(xy, verts, pidx, f=cols2.filt([(7, oracle.GTE, 0)]))[0]
     compat = oracle.bruteforce(xy, verts, pidx, f=cols2.filt([(7, oracle.GTE, 0)], compat_float_eq=True))[0]
     assert typed.sum() == 3 and compat.sum() == 4
+
+
+def _near_edges(verts, pidx, seed):
+    """Points on the vertices, on the edges and 1e-4..0.5 m to either side."""
+    rng = np.random.default_rng(seed)
+    out = [verts.astype(np.float32)]
+    for p in range(len(pidx) - 1):
+        v = verts[pidx[p]:pidx[p + 1]].astype(np.float64)
+        w = np.roll(v, -1, axis=0)
+        d = w - v
+        nrm = np.c_[-d[:, 1], d[:, 0]] / np.maximum(np.hypot(d[:, 0], d[:, 1]), 1e-9)[:, None]
+        for t in rng.random(2):
+            q = v + d * t
+            for off in (0.0, 1e-4, -1e-4, 0.5, -0.5):
+                out.append((q + off * nrm).astype(np.float32))
+    return np.concatenate(out)
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_exact_joins_agree_on_overlapping_stars_near_edges(seed):
+    """Concave, overlapping star polygons (each polygon counts on its own) and
+    points placed on and next to every edge: the index, hybrid and CPUJoin
+    restatements give the brute-force fp32 crossing-number counts exactly."""
+    from rasterjoin import workloads
+    rng = np.random.default_rng(seed)
+    verts, pidx = workloads.star_set(rng, 40, 6, 60, 300.0, 4000.0)
+    xy = np.concatenate([_near_edges(verts, pidx, seed),
+                         rng.uniform(0, synth.BOX, (20_000, 2)).astype(np.float32)])
+    brute, _ = oracle.bruteforce(xy, verts, pidx)
+    assert brute.sum() > 0
+    np.testing.assert_array_equal(oracle.index_join(xy, verts, pidx, 256)[0], brute)
+    np.testing.assert_array_equal(oracle.hybrid_join(xy, verts, pidx, 256)[0], brute)
+    np.testing.assert_array_equal(oracle.cpujoin(xy, verts, pidx, 1024)[0], brute)
