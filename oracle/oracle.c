@@ -27,6 +27,14 @@
  * The polygon pass decides coverage per pixel centre with an exact integer
  * edge test on 1/256-pixel snapped window coordinates (the GL rasteriser's
  * rule); the reference's triangulation is not needed for that decision.
+ *
+ * Pinning.  The exact joins (index, hybrid, CPUJoin, brute force) are pinned
+ * by the reference's own known-answer fixture (RasterJoin/test/baseline.hpp:
+ * 139-217) and agree with each other exactly on seeded and edge-adversarial
+ * inputs.  Raster pixel assignment is parity unpinned against the reference:
+ * it is the GL driver's rasteriser, which cannot run here; the pixel-centre
+ * rule is cross-checked against GL's triangle rule on the reference's own
+ * triangulation (compiled from its sources into oracle/_ref).
  */
 #include <math.h>
 #include <stdint.h>
