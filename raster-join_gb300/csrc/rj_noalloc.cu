@@ -21,6 +21,10 @@
 // it and produce wrong counts.  The first call on a device looks the array's
 // address up for that device (cudaGetSymbolAddress); make that first call
 // before capturing the stream into anything that records work.
+// Errors: argument and size checks fail before any work is queued.  A CUDA
+// error already pending on the calling thread when the call starts is
+// reported (RJ_E_CUDA) and left pending, and nothing is queued; otherwise a
+// CUDA error returned by the call comes from this call's own launches.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -110,6 +114,21 @@ extern "C" RJ_API int rj_raster_count_noalloc(const float* d_xy, uint64_t npoint
         return na_fail(err, errlen, RJ_E_INVALID,
                        "canvas larger than 2048 x 2048 pixels: use rj_execute, or a larger cell size");
     const int resx = std::max(1, (int)ax), resy = std::max(1, (int)ay);
+    // the polygon work-list scan's tile sums must fit their slice of the
+    // array; checked before anything is queued on the caller's stream
+    if (scan_tmp_ints(npolys) > (int)kScanInts)
+        return na_fail(err, errlen, RJ_E_INVALID, "polygon work list exceeds the scratch array");
+    // An error left pending by earlier work on this thread is not this call's:
+    // report it and leave it pending for its owner, queueing nothing.
+    {
+        const cudaError_t prior = cudaPeekAtLastError();
+        if (prior != cudaSuccess) {
+            char msg[192];
+            std::snprintf(msg, sizeof msg, "an earlier CUDA error is pending on this thread: %s",
+                          cudaGetErrorString(prior));
+            return na_fail(err, errlen, RJ_E_CUDA, msg);
+        }
+    }
 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) {
@@ -195,9 +214,7 @@ extern "C" RJ_API int rj_raster_count_noalloc(const float* d_xy, uint64_t npoint
     a.nbands = (int*)(base + kOffBands);
     a.band_start = (int*)(base + kOffBandStart);
     launch_poly_info(MODE_REDUCE, a, nd.sms, st);
-    if (scan_tmp_ints(npolys) > (int)kScanInts ||
-        !launch_exclusive_scan(a.nbands, (int*)(base + kOffBandStart), npolys, (int*)(base + kOffScan), st))
-        return na_fail(err, errlen, RJ_E_INVALID, "polygon work list exceeds the scratch array");
+    launch_exclusive_scan(a.nbands, (int*)(base + kOffBandStart), npolys, (int*)(base + kOffScan), st);
     launch_poly_pass(MODE_REDUCE, a, nd.sms, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return na_fail(err, errlen, RJ_E_CUDA, cudaGetErrorString(e));
