@@ -1,21 +1,32 @@
 #!/usr/bin/env python
 """Raster Join benchmark on GB300.
 
-Default workload (benchmark configuration 2, the one the headline metric is
-quoted for that fits one GPU): 100M points resident in HBM with columns
-x, y (float32), t (uint32, one year), a (float32 lognormal), f1, f2 (int32
-0..9); 260 Voronoi neighbourhoods over a 40 x 40 km box; the hybrid join
-(exact) with the time range = first 6 months, f1 > 2, f2 < 8, a < 50 and
-avg(a), polygon grid index 256 x 256.
+Headline (the metric "Gpoints/s joined at eps = 10 m", benchmark
+configuration 3 at its eps = 10 m point): 2,000,000,000 points resident in
+HBM (x, y float32: 16 GB), drawn from the configurations' generator (80 %
+from 8 Gaussians with sigma 2 km, 20 % uniform, 40 x 40 km box); 260 Voronoi
+neighbourhoods; the bounded raster join, count(), at eps = 10 m (the pixel
+side, as the configurations quote it: a 4000 x 4000 canvas).  The reference's
+own published point for this axis is the raster join at eps = 10 m over
+335M taxi points (experiments/results-paper/scalability/taxi-in-memory.txt:1).
 
-A step is one query answered from scratch: grid index, outline mask and
-polygon labels rebuilt (RJ_FLAG_NO_CACHE), one streaming pass over the
-points, results read back.  `value` is points joined per second with the
-table resident; `e2e` adds, every step, the host->device copy of all six
-columns from pinned memory and the result read-back.
+A step is one query answered from scratch: the polygon label map and its
+block codes rebuilt (RJ_FLAG_NO_CACHE), one streaming pass over the points,
+the per-polygon counts read back.  `value` is points joined per second with
+the table resident; `e2e` adds, every step, the host->device copy of the
+location column from pinned memory (rj_load_points) and the read-back.
+
+In the same run:
+  * the full 2B-point result is checked against an independent path of the
+    library (the point canvas plus the polygon pass, RJ_FLAG_FORCE_CANVAS);
+  * a 20M-point sample of the host generator is joined alone on the GPU and
+    checked bit for bit against the oracle's raster join; the reference arm
+    (--impl reference) times CPUJoin on the same sample;
+  * extra keys: configuration 2 (hybrid / index joins with filters and avg,
+    100M points), batched (configuration 4) and served (configuration 5).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--join hybrid|index|raster] [--points N]
+                  [--points N] [--no-config2] [--no-batched] [--no-served]
 """
 import argparse
 import json
@@ -32,8 +43,21 @@ for p in (os.path.join(ROOT, "raster-join_gb300"), os.path.join(ROOT, "oracle"),
     if p not in sys.path:
         sys.path.insert(0, p)
 
-BYTES_PER_POINT = 24          # x, y, t, a, f1, f2: 4 bytes each, all read by the query
-WORKLOAD = "config2: 100M pts (x,y,t,a,f1,f2), 260 Voronoi polys, 40x40 km, t in first 6 months & f1>2 & f2<8 & a<50, avg(a), grid 256"
+HEADLINE_POINTS = 2_000_000_000
+HEADLINE_CELL = 10.0
+HEADLINE_BYTES_PER_POINT = 8      # x, y float32: the only column a plain count reads
+SAMPLE_POINTS = 20_000_000        # host-generated sample: oracle check and the CPU arms
+POLY_SEED = 20261203
+TABLE_SEED = 7
+SAMPLE_SEED = 20261203
+METRIC = "Gpoints/s joined at eps=10 m (raster count)"
+WORKLOAD = ("config3 at eps 10 m: 2,000,000,000 points resident (x, y float32, 16 GB), 260 Voronoi "
+            "neighbourhoods over a 40 x 40 km box, bounded raster join count(), cell 10 m (4000 x 4000 canvas)")
+
+# configuration 2 (extra key)
+C2_BYTES_PER_POINT = 24          # x, y, t, a, f1, f2: 4 bytes each, all read by the query
+C2_WORKLOAD = ("config2: 100M pts (x,y,t,a,f1,f2), 260 Voronoi polys, 40x40 km, t in first 6 months & f1>2 & "
+               "f2<8 & a<50, avg(a), grid 256")
 
 
 def parse():
@@ -42,11 +66,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--join", default="hybrid", choices=["hybrid", "index", "raster"])
-    ap.add_argument("--points", type=int, default=100_000_000)
+    ap.add_argument("--points", type=int, default=HEADLINE_POINTS, help="headline table size")
+    ap.add_argument("--sample-points", type=int, default=SAMPLE_POINTS)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--count-only", action="store_true", help="count instead of avg(a) (diagnostic)")
+    ap.add_argument("--no-config2", action="store_true")
+    ap.add_argument("--c2-points", type=int, default=100_000_000)
+    ap.add_argument("--c2-steps", type=int, default=50)
     ap.add_argument("--table-points", type=int, default=1_000_000_000,
                     help="resident table of the batched and served runs")
     ap.add_argument("--batch-queries", type=int, default=512)
@@ -58,10 +84,8 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--config3", action="store_true",
-                    help="run configuration 3 instead (2B resident points, raster and error-bounds joins at eps 10 m "
-                         "and 1 m, 260 Voronoi cells and 2000 stars) and print its own line")
-    ap.add_argument("--cluster", action="store_true",
-                    help="config 2: reorder the table by 156 m cells before timing (default: generated order)")
+                    help="run all of configuration 3 instead (raster and error-bounds joins at eps 10 m and 1 m, "
+                         "260 Voronoi cells and 2000 stars) and print its own line")
     return ap.parse_args()
 
 
@@ -69,10 +93,27 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def headline_config(n, sample):
+    """The workload both arms report (identical dicts, so their lines compare)."""
+    return {"workload": WORKLOAD, "points": n, "polygons": 260, "cell_m": HEADLINE_CELL, "canvas": "4000x4000",
+            "aggregation": "count", "sample_points": sample,
+            "l2": "inputs (16 GB per step) larger than L2"}
+
+
+def voronoi():
+    from rasterjoin import synth
+    return synth.voronoi_polygons(260, seed=POLY_SEED)
+
+
+def host_sample(n):
+    from rasterjoin import synth
+    return synth.points(n, seed=SAMPLE_SEED)["xy"]
+
+
 def make_workload(n, seed):
     from rasterjoin import synth
     pts = synth.points(n, seed=seed, columns=True)
-    verts, pidx = synth.voronoi_polygons(260, seed=20261203)
+    verts, pidx = synth.voronoi_polygons(260, seed=POLY_SEED)
     return pts, verts, pidx
 
 
@@ -160,68 +201,81 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(join, n):
-    """DRAM bytes per launch of the point kernel from the committed ncu summary, scaled to n points."""
+def profiled_traffic(key, n):
+    """DRAM bytes per launch of a point kernel from the committed ncu summary
+    (bytes per point of a smaller capture), scaled to n points."""
     try:
         with open(os.path.join(ROOT, "profiles", "point_pass_traffic.json")) as fh:
             d = json.load(fh)
-        e = d[join]
-        return float(e["dram_bytes_per_point"]) * n
+        return float(d[key]["dram_bytes_per_point"]) * n
     except Exception:
         return None
 
 
 # ---------------------------------------------------------------------------
-def cpu_baseline(pts, verts, pidx, join, sample_points):
-    """CPUJoin restatement (oracle port, all host threads) on a bounded sample."""
+# CPU arms: the reference's own CPU join (CPUJoin, restated without Qt in the
+# oracle: CPUJoin.cpp:62-122, GridIndexF.cpp:60-175,383-549), count, grid 1024
+# as the reference's scripts run it (cpu-scalability.ps1:28).
+def cpujoin_count(xy, verts, pidx, threads):
+    """One CPUJoin run (grid built + join); returns (counts, wall s, join s, build s)."""
     import oracle
-    cons, trange = query_constraints()
-    n = min(sample_points, len(pts["xy"]))
-    cols = oracle.Columns({2: (oracle.Uint, pts["t"][:n]), 3: (oracle.Float, pts["a"][:n]),
-                           4: (oracle.Int, pts["f1"][:n]), 5: (oracle.Int, pts["f2"][:n])})
-    f = cols.filt([(a, o, v) for a, o, v in cons], aggr_attrib=3, time_range=trange)
-    threads = os.cpu_count() or 1
     t0 = time.perf_counter()
-    _, _, tj, tb = oracle.cpujoin(pts["xy"][:n], verts, pidx, 1024, f=f, nthreads=threads)
-    wall = time.perf_counter() - t0
-    return n, wall, tj, tb, threads
+    c, _, tj, tb = oracle.cpujoin(xy, verts, pidx, 1024, nthreads=threads)
+    return c, time.perf_counter() - t0, tj, tb
 
 
-def metric_name(join):
+def cpu_baseline_headline(sample_xy, verts, pidx):
+    threads = os.cpu_count() or 1
+    _, wall, tj, tb = cpujoin_count(sample_xy, verts, pidx, threads)
+    n1 = min(len(sample_xy), 2_000_000)
+    _, wall1, tj1, tb1 = cpujoin_count(sample_xy[:n1], verts, pidx, 1)
+    return {"value": len(sample_xy) / wall / 1e9, "unit": "Gpoints/s", "cores": threads, "kind": "port",
+            "sample": "CPUJoin restatement (count, grid 1024 built %.2f s + join %.2f s) with %d threads over a "
+                      "%d-point sample of the same generator (the sample the GPU also joins alone)"
+                      % (tb, tj, threads, len(sample_xy)),
+            "single_core": {"value": n1 / wall1 / 1e9, "unit": "Gpoints/s", "cores": 1,
+                            "sample": "the first %d points of that sample, one thread (grid %.2f s + join %.2f s)"
+                                      % (n1, tb1, tj1)}}
+
+
+def metric_name(join=None):
     """The metric both arms report (same string, so their lines compare)."""
-    return "Gpoints/s joined (config 2: %s join; exact, so within any epsilon incl. 10 m)" % join
+    return METRIC
 
 
 def run_reference(args):
+    """CPUJoin (the reference's CPU join, oracle restatement, all host threads)
+    over the headline's sample; per step: grid build + join."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    sample = min(args.points, 20_000_000)
-    pts, verts, pidx = make_workload(sample, seed=20261203)
-    times = []
+    sample = min(args.sample_points, args.points)
+    xy = host_sample(sample)
+    verts, pidx = voronoi()
     threads = os.cpu_count() or 1
+    times = []
     for i in range(args.warmup + args.steps):
-        n, wall, tj, tb, threads = cpu_baseline(pts, verts, pidx, args.join, sample)
+        _, wall, _, _ = cpujoin_count(xy, verts, pidx, threads)
         if i >= args.warmup:
             times.append(wall)
     step = float(np.mean(times))
     value = sample / step / 1e9
     line = {
         "impl": "reference",
-        "metric": metric_name(args.join),
+        "metric": METRIC,
         "value": value, "unit": "Gpoints/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "join": args.join, "sample_points": sample, "parallelism": "cpu-threads"},
+        "dtype": "f32", "data": "synthetic (seeded; stands in for the NYC-taxi table)",
+        "config": headline_config(args.points, sample),
+        "parallelism": "cpu-threads",
         "cpu_baseline": {"value": value, "unit": "Gpoints/s", "cores": threads, "kind": "port",
-                         "sample": "CPUJoin restatement (grid 1024 built each step + join) over the first %d points "
-                                   "of the config-2 table, with the config-2 filters and avg as a labelled "
-                                   "extension (CPUJoin itself counts only)" % sample},
+                         "sample": "CPUJoin restatement (count, grid 1024 built each step + join) with %d threads "
+                                   "over the %d-point sample of the headline's generator that the GPU arm also "
+                                   "joins alone; a per-point rate of the same workload" % (threads, sample)},
         "e2e": {"value": value, "unit": "Gpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
-
 
 
 # ---------------------------------------------------------------------------
@@ -376,57 +430,46 @@ def run_served(rj, h, cum, n, nreq, qps, seed=20261205):
 
 
 # ---------------------------------------------------------------------------
-def run_gb300(args):
-    import torch
-    rank, world, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
-    import __graft_entry__
-    __graft_entry__.build()
-    import rasterjoin as rj
+def clocks_around(sampler, t0, t1):
+    timed = sampler.summary(t0, t1)
+    c = dict(sampler.summary())
+    c["samples_in_timed_region"] = timed["samples"]
+    if timed["samples"]:
+        c["sm_mhz_timed_region"] = timed["sm_mhz"]
+    return c
 
+
+def run_headline(args, rj, torch, local, world):
+    """The headline line: eps = 10 m raster count over the resident 2B table."""
+    from rasterjoin import workloads as W
     n = args.points
-    pts, verts, pidx = make_workload(n, seed=20261203 + rank)
+    verts, pidx = voronoi()
     P = len(pidx) - 1
+    tab = W.device_table(n, TABLE_SEED + dist_env()[0])
+    del tab["t"], tab["a"]
+    xy_dev = tab["xy"]
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
     stream = torch.cuda.Stream()
     h = rj.GLHandler(device=local, stream=stream.cuda_stream)
-    dh = rj.DataHandler()
-    dh.add_column(1, rj.Location, pts["xy"])
-    dh.add_column(2, rj.Uint, pts["t"])
-    dh.add_column(3, rj.Float, pts["a"])
-    dh.add_column(4, rj.Int, pts["f1"])
-    dh.add_column(5, rj.Int, pts["f2"])
-    dh.setPolygons(verts, pidx)
-    cons, trange = query_constraints()
-    dh.setQueryConstraints(cons)
-    dh.setTimeRange(*trange)
-    dh.setAggregation(rj.Count if args.count_only else rj.Avg, -1 if args.count_only else 3)
-    h.setDataHandler(dh)
-    h.setAccuracyDistance(10.0 if args.join == "raster" else 100.0)
-    h.setPolyIndexResolution(256)
-    h.flags = rj.FLAG_NO_CACHE | rj.FLAG_PHASE_TIMING
-    fn = fn_of(args.join)
-    h.upload()
-    if args.cluster:
-        # resident layout: rows grouped by 156 m cells (Z-order), as the
-        # reference backend groups them in spatial partitions; no time pruning
-        h.clusterPoints(-1, 0, 8)
-    q = h.make_query(fn)
+    h.attachDevice([(1, rj.Location, xy_dev.data_ptr())], n, 1)
+    ps = h.polyset(verts, pidx)
+    h.usePolySet(ps)
+    q = rj.default_query()
+    q.function_type = rj.RasterJoinFn
+    q.cell_size = HEADLINE_CELL
+    q.flags = rj.FLAG_NO_CACHE | rj.FLAG_PHASE_TIMING
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
-    for _ in range(max(3, args.warmup)):
-        h.execute(fn, query=q)
+    for _ in range(max(3, args.warmup)):          # the first also autotunes the count kernel
+        h.execute(rj.RasterJoinFn, query=q)
     torch.cuda.synchronize()
-
-    dev_uuid = None
+    shape = (h.getTuning(rj.TUNE_COUNT_SHAPE), h.getTuning(rj.TUNE_COUNT_BLOCK_SHIFT))
     try:
-        dev_uuid = torch.cuda.get_device_properties(local).uuid
-        dev_uuid = "GPU-" + str(dev_uuid)
+        dev_uuid = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
     except Exception:
         dev_uuid = local
     sampler = ClockSampler(dev_uuid)
@@ -440,7 +483,7 @@ def run_gb300(args):
     t_wall0 = time.time()
     for i in range(args.steps):
         starts[i].record(stream)
-        h.execute(fn, query=q)
+        h.execute(rj.RasterJoinFn, query=q)
         ends[i].record(stream)
         t = h.timings()
         pt_ms.append(t["pt_render_ms"])
@@ -448,56 +491,51 @@ def run_gb300(args):
     torch.cuda.synchronize()
     barrier()
     t_wall1 = time.time()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = sum(step_ms)
+    total_ms = sum(s_.elapsed_time(e_) for s_, e_ in zip(starts, ends))
     if world > 1:
         tt = torch.tensor([total_ms], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(tt.item())
-    # keep sampling a little under the same load if the timed loop was short
     probe_end = time.time() + max(0.0, 1.5 - (t_wall1 - t_wall0))
     while time.time() < probe_end:
-        h.execute(fn, query=q)
+        h.execute(rj.RasterJoinFn, query=q)
     torch.cuda.synchronize()
     sampler.stop()
-    clocks_timed = sampler.summary(t_wall0, t_wall1)
-    clocks_all = sampler.summary()
-    clocks = dict(clocks_all)
-    clocks["samples_in_timed_region"] = clocks_timed["samples"]
-
+    clocks = clocks_around(sampler, t_wall0, t_wall1)
     res = h.last
     ms_per_step = total_ms / args.steps
-    value = world * n / (total_ms / args.steps / 1e3) / 1e9
+    value = world * n / (ms_per_step / 1e3) / 1e9
 
-    # ---- end to end through the public API with host buffers (pinned) ----
-    pinned = {}
-    for k in ("xy", "t", "a", "f1", "f2"):
-        arr = pts[k]
-        tns = torch.empty(arr.shape, dtype={np.float32: torch.float32, np.uint32: torch.int32,
-                                            np.int32: torch.int32}[arr.dtype.type], pin_memory=True)
-        tns.numpy().view(arr.dtype)[...] = arr
-        pinned[k] = tns.numpy().view(arr.dtype)
-    dh2 = rj.DataHandler()
-    dh2.add_column(1, rj.Location, pinned["xy"])
-    dh2.add_column(2, rj.Uint, pinned["t"])
-    dh2.add_column(3, rj.Float, pinned["a"])
-    dh2.add_column(4, rj.Int, pinned["f1"])
-    dh2.add_column(5, rj.Int, pinned["f2"])
-    dh2.setPolygons(verts, pidx)
-    dh2.setQueryConstraints(cons)
-    dh2.setTimeRange(*trange)
-    dh2.setAggregation(rj.Avg, 3)
-    h.setDataHandler(dh2)
-    h.upload(force=True)
+    # ---- the full result against an independent path: point canvas + polygon pass ----
+    qc = rj.default_query()
+    qc.function_type = rj.RasterJoinFn
+    qc.cell_size = HEADLINE_CELL
+    qc.flags = rj.FLAG_FORCE_CANVAS
+    canvas_equal = bool(np.array_equal(h.execute(rj.RasterJoinFn, query=qc).count, res.count))
+
+    # ---- end to end: the location column from pinned host memory every step ----
+    pinned = torch.empty((n, 2), dtype=torch.float32, pin_memory=True)
+    pinned.copy_(xy_dev)
+    host_xy = pinned.numpy()
+    del tab, xy_dev
+    h.usePolySet(None)
+    ps.close()
+    h.close()
+    torch.cuda.empty_cache()
+    he = rj.GLHandler(device=local, stream=stream.cuda_stream)
+    dh = rj.DataHandler()
+    dh.add_column(1, rj.Location, host_xy)
+    dh.setPolygons(verts, pidx)
+    he.setDataHandler(dh)
+    he.setCellSize(HEADLINE_CELL)
+    he.flags = rj.FLAG_NO_CACHE
     e2e_times = []
     for i in range(args.e2e_steps + 2):
         barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        h.upload(force=True)                 # H2D of all columns (rj_load_points)
-        if args.cluster:
-            h.clusterPoints(-1, 0, 8)        # same resident layout as the timed loop
-        r = h.execute(fn, query=q)           # join + D2H of the results
+        he.upload(force=True)                 # H2D of the location column (rj_load_points)
+        r = he.execute(rj.RasterJoinFn)       # join + D2H of the counts
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         if i >= 2:
@@ -507,43 +545,153 @@ def run_gb300(args):
         tt = torch.tensor([e2e_s], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(tt.item())
-    same = bool(np.array_equal(r.count, res.count))
-    h2d = n * BYTES_PER_POINT
-    d2h = P * (8 + 8 + 12 + 16)
+    e2e_same = bool(np.array_equal(r.count, res.count))
+    he.close()
+    del pinned, host_xy, dh
+    torch.cuda.empty_cache()
 
-    # ---- roofline of the point pass ----
+    # ---- the sample: joined alone on the GPU and checked against the oracle ----
+    import oracle
+    sample = min(args.sample_points, n)
+    sxy = host_sample(sample)
+    hs = rj.GLHandler(device=local, stream=stream.cuda_stream)
+    dh = rj.DataHandler()
+    dh.add_column(1, rj.Location, sxy)
+    dh.setPolygons(verts, pidx)
+    hs.setDataHandler(dh)
+    hs.setCellSize(HEADLINE_CELL)
+    hs.flags = rj.FLAG_NO_CACHE
+    for _ in range(3):
+        rs = hs.execute(rj.RasterJoinFn)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(10):
+        rs = hs.execute(rj.RasterJoinFn)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sample_ms = e0.elapsed_time(e1) / 10
+    hs.close()
+    want = oracle.raster_join(sxy, verts, pidx, HEADLINE_CELL)[0]
+    oracle_equal = bool(np.array_equal(rs.count, want))
+
     peak, peak_kind = measured_peaks()
     mean_pt = float(np.mean(pt_ms))
-    achieved = (n * BYTES_PER_POINT / 1e9) / (mean_pt / 1e3) if mean_pt > 0 else None
-    traffic = profiled_traffic(args.join, n)
-
+    achieved = (n * HEADLINE_BYTES_PER_POINT / 1e9) / (mean_pt / 1e3) if mean_pt > 0 else None
     line = {
-        "metric": metric_name(args.join),
+        "metric": METRIC,
         "value": value, "unit": "Gpoints/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded; stands in for the NYC-taxi table)",
-        "config": {"workload": WORKLOAD, "join": args.join, "points_per_gpu": n, "polygons": P,
-                   "layout": "rows clustered by 156 m cells (rj_cluster_points, no time pruning)" if args.cluster
-                   else "generated order",
-                   "grid_res": 256, "l2": "inputs (2.4 GB per step) larger than L2", "parallelism":
-                   "replicas" if world > 1 else "single-gpu"},
-        "e2e": {"value": world * n / e2e_s / 1e9, "unit": "Gpoints/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "same_result": same},
+        "config": headline_config(n, sample),
+        "parallelism": "replicas" if world > 1 else "single-gpu",
+        "e2e": {"value": world * n / e2e_s / 1e9, "unit": "Gpoints/s",
+                "h2d_bytes_per_step": n * HEADLINE_BYTES_PER_POINT, "d2h_bytes_per_step": P * (8 + 8 + 12),
+                "same_result": e2e_same,
+                "method": "rj_load_points from pinned host memory + rj_execute + counts read back, every step"},
         "gpu_launches": int(sum(launches)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "kernel": "k_points (point pass)", "kernel_ms": mean_pt,
-                     "algorithmic_bytes_per_launch": n * BYTES_PER_POINT, "peak_kind": peak_kind},
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": profiled_traffic("raster_count", n),
+                     "kernel": "k_label_count (shape %d, block codes 2^%d px)" % shape, "kernel_ms": mean_pt,
+                     "algorithmic_bytes_per_launch": n * HEADLINE_BYTES_PER_POINT, "peak_kind": peak_kind},
         "clocks": clocks,
+        "checks": {"full_table_vs_canvas_path": canvas_equal,
+                   "sample_vs_oracle": oracle_equal,
+                   "sample": "%d points of the host generator, joined alone on the GPU, against the oracle's "
+                             "raster join (bit-exact counts)" % sample},
+        "sample": {"points": sample, "gpu_gpoints_s": sample / sample_ms / 1e6, "gpu_ms": sample_ms},
     }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        sample = min(n, 20_000_000)
-        s_n, wall, tj, tb, threads = cpu_baseline(pts, verts, pidx, args.join, sample)
-        line["cpu_baseline"] = {"value": s_n / wall / 1e9, "unit": "Gpoints/s", "cores": threads, "kind": "port",
-                                "sample": "CPUJoin restatement (grid 1024 build %.2fs + join %.2fs) over the first "
-                                          "%d points of the same table, config-2 filters and avg as a labelled "
-                                          "extension" % (tb, tj, s_n)}
+    return line, (sxy, verts, pidx)
+
+
+def run_config2(args, rj, torch, local, join, pts, verts, pidx):
+    """Configuration 2 (hybrid or index join, filters, time range, avg(a)) on
+    100M host-generated points; returns an extra-key dict and the result."""
+    n = len(pts["xy"])
+    stream = torch.cuda.Stream()
+    h = rj.GLHandler(device=local, stream=stream.cuda_stream)
+    dh = rj.DataHandler()
+    dh.add_column(1, rj.Location, pts["xy"])
+    dh.add_column(2, rj.Uint, pts["t"])
+    dh.add_column(3, rj.Float, pts["a"])
+    dh.add_column(4, rj.Int, pts["f1"])
+    dh.add_column(5, rj.Int, pts["f2"])
+    dh.setPolygons(verts, pidx)
+    cons, trange = query_constraints()
+    dh.setQueryConstraints(cons)
+    dh.setTimeRange(*trange)
+    dh.setAggregation(rj.Avg, 3)
+    h.setDataHandler(dh)
+    h.setAccuracyDistance(100.0)
+    h.setPolyIndexResolution(256)
+    h.flags = rj.FLAG_NO_CACHE | rj.FLAG_PHASE_TIMING
+    fn = fn_of(join)
+    h.upload()
+    q = h.make_query(fn)
+    out = {}
+    for _ in range(3):
+        h.execute(fn, query=q)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pt = []
+    e0.record(stream)
+    for _ in range(args.c2_steps):
+        h.execute(fn, query=q)
+        pt.append(h.timings()["pt_render_ms"])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.c2_steps
+    res = h.last
     h.close()
+    peak, _ = measured_peaks()
+    mean_pt = float(np.mean(pt))
+    achieved = (n * C2_BYTES_PER_POINT / 1e9) / (mean_pt / 1e3)
+    out = {"workload": C2_WORKLOAD, "join": join, "gpoints_s": n / ms / 1e6, "ms_per_step": ms,
+           "point_pass_ms": mean_pt,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "traffic": profiled_traffic(join, n)}}
+    return out, res
+
+
+def run_gb300(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import __graft_entry__
+    __graft_entry__.build()
+    import rasterjoin as rj
+
+    line, (sxy, verts, pidx) = run_headline(args, rj, torch, local, world)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_headline(sxy, verts, pidx)
+    del sxy
+    if rank == 0 and world == 1 and not args.no_config2:
+        import oracle
+        extra = {}
+        pts, verts2, pidx2 = make_workload(args.c2_points, seed=20261203)
+        results = {}
+        for join in ("hybrid", "index"):
+            extra[join], results[join] = run_config2(args, rj, torch, local, join, pts, verts2, pidx2)
+        # the hybrid and index counts against CPUJoin's exact counts on the same 100M points
+        cols = oracle.Columns({2: (oracle.Uint, pts["t"]), 3: (oracle.Float, pts["a"]),
+                               4: (oracle.Int, pts["f1"]), 5: (oracle.Int, pts["f2"])})
+        cons, trange = query_constraints()
+        f = cols.filt(cons, aggr_attrib=3, time_range=trange)
+        t0 = time.perf_counter()
+        c, s_, _, _ = oracle.cpujoin(pts["xy"], verts2, pidx2, 256, f=f)
+        rel = lambda r: float(np.max(np.abs(r.sum - s_) / np.maximum(np.abs(s_), 1e-30)))
+        extra["check"] = {"hybrid_counts_vs_cpujoin": bool(np.array_equal(results["hybrid"].count, c)),
+                          "index_counts_vs_cpujoin": bool(np.array_equal(results["index"].count, c)),
+                          "hybrid_sums_max_rel_err": rel(results["hybrid"]),
+                          "index_sums_max_rel_err": rel(results["index"]),
+                          "cpujoin_s": time.perf_counter() - t0,
+                          "oracle": "CPUJoin restatement (grid 256) with the config-2 filters and avg, fp64 sums"}
+        line["config2"] = extra
+        del pts
     if rank == 0 and world == 1 and not (args.no_batched and args.no_served):
         stream2 = torch.cuda.Stream()
         h2, cum = resident_table(rj, torch, args.table_points, 20261206, stream2)

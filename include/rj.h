@@ -85,7 +85,7 @@ typedef struct {
                                            points.vert:98-107 */
 #define RJ_FLAG_LINE_FILTER        0x4u /* error bounds keep only pixels whose
                                            centre is within 0.5 px of the edge:
-                                           line-bound.frag:245 */
+                                           line-bound.frag:221 */
 #define RJ_FLAG_FORCE_CANVAS       0x8u /* raster/hybrid: always accumulate a
                                            point canvas (no polygon label map) */
 #define RJ_FLAG_PHASE_TIMING       0x10u /* record CUDA events per phase       */
@@ -233,6 +233,57 @@ RJ_API void rj_query_init(rj_query *q);
 RJ_API int rj_get_timings(const rj_ctx *ctx, rj_timings *out);
 /* the reference's tab-separated timing line for the last call */
 RJ_API int rj_format_time_stats(const rj_ctx *ctx, char *buf, size_t buflen);
+
+/* ---- exact partial sums (replicas over row shards) ------------------------
+ * Sums are exact int64 sums of round(v * 2^shift) per polygon; the double
+ * sum of rj_result is fixed * 2^-shift + nonfinite (the fp64 sum of the
+ * non-finite values).  Replicas that join row shards of one table add their
+ * int64 partials (two's complement, wrapping) and decode once, which gives
+ * the bits of the single-GPU join, provided every shard uses the shift the
+ * whole table would: rj_sum_shift_for(largest |value| over all shards, total
+ * rows).  The reference has no counterpart (one process, one GPU).
+ *   rj_get_sum_partials: the last rj_execute's fixed and non-finite partials
+ *     (npolys entries each; either pointer may be NULL) and its shift.
+ *   rj_set_sum_shift: use this shift for subsequent sums (RJ_SUM_SHIFT_AUTO:
+ *     chosen per query from the aggregate column and the table size).  A
+ *     query whose values could overflow at the forced shift on this table
+ *     fails with RJ_E_INVALID.
+ *   rj_sum_shift_for: the shift chosen for values of magnitude <= max_abs
+ *     over `rows` rows.
+ *   rj_column_absmax: largest finite |aggregate value| of a loaded column. */
+#define RJ_SUM_SHIFT_AUTO (-2147483647 - 1)
+RJ_API int rj_get_sum_partials(const rj_ctx *ctx, int64_t *fixed, double *nonfinite, int32_t *shift);
+RJ_API int rj_set_sum_shift(rj_ctx *ctx, int32_t shift);
+RJ_API int32_t rj_sum_shift_for(double max_abs, uint64_t rows);
+RJ_API int rj_column_absmax(const rj_ctx *ctx, int32_t attrib_id, double *out);
+
+/* ---- kernel tuning ---------------------------------------------------------
+ * Kernel shapes of this context.  Every shape computes the same result; the
+ * knobs only choose how the work is laid out on the GPU.  The reference has
+ * no counterpart (its point pass is one glDrawArrays, RasterJoin.cpp:135).
+ *   RJ_TUNE_POINT_SHAPE      generic point pass: -1 = default per join,
+ *                            0 = 4 points x 256 threads, 2 = bulk-copy
+ *                            pipeline, 3 = 4 points x 512 threads
+ *   RJ_TUNE_COUNT_SHAPE      lean raster count pass (one canvas tile, label
+ *                            map, no filter, count): -1 = autotuned (each
+ *                            shape is timed once per context and query
+ *                            class on the table itself, the fastest is
+ *                            kept), else a shape index
+ *                            0..rj_get_tuning(RJ_TUNE_COUNT_SHAPES)-1
+ *   RJ_TUNE_COUNT_BLOCK_SHIFT block-code map of that pass: -1 = autotuned,
+ *                            else log2 of the block side (4..8)
+ *   RJ_TUNE_HYBRID_EXACT_SCALE classified grid of the hybrid join's exact
+ *                            tests: the query grid refined 1, 2 or 4 times
+ *   RJ_TUNE_COUNT_SHAPES     (read only) number of count-pass shapes
+ * rj_get_tuning on RJ_TUNE_COUNT_SHAPE / _BLOCK_SHIFT reports the values the
+ * last count pass ran with (-1 when the last query did not take it). */
+#define RJ_TUNE_POINT_SHAPE        0
+#define RJ_TUNE_COUNT_SHAPE        1
+#define RJ_TUNE_COUNT_BLOCK_SHIFT  2
+#define RJ_TUNE_HYBRID_EXACT_SCALE 3
+#define RJ_TUNE_COUNT_SHAPES       4
+RJ_API int rj_set_tuning(rj_ctx *ctx, int32_t knob, int32_t value);
+RJ_API int rj_get_tuning(const rj_ctx *ctx, int32_t knob, int32_t *value);
 
 /* ---- polygon sets --------------------------------------------------------
  * A polygon collection held on the device independently of the context's own

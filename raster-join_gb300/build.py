@@ -20,7 +20,8 @@ OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "librj.so")
 SOURCES = ["rj_runtime.cu", "rj_point_kernels.cu", "rj_point_exact.cu", "rj_poly_kernels.cu", "rj_noalloc.cu",
-           "rj_batch.cu", "rj_batch_kernels.cu", "rj_batch_direct.cu", "rj_tier_kernels.cu"]
+           "rj_batch.cu", "rj_batch_kernels.cu", "rj_batch_direct.cu", "rj_tier_kernels.cu",
+           "rj_count_kernels.cu"]
 HEADERS = ["rj_device.cuh", "rj_launch.h", "rj_internal.h", "rj_point_map.cuh", "rj_point_core.cuh",
            "rj_batch_common.cuh",
            os.path.join("..", "..", "include", "rj.h")]
@@ -86,12 +87,26 @@ def build(force=False, verbose=False):
 
     def compile_one(src):
         obj = os.path.join(OBJ, src.replace(".cu", ".o"))
+        # per-object stamp: the source, every shared header, the flags, the machine
+        h = hashlib.sha256()
+        for f in [src] + HEADERS:
+            with open(os.path.join(CSRC, f), "rb") as fh:
+                h.update(fh.read())
+        h.update(" ".join(NVCC_FLAGS).encode())
+        h.update(os.uname().machine.encode())
+        ostamp = obj + ".stamp"
+        if not force and os.path.exists(obj) and os.path.exists(ostamp):
+            with open(ostamp) as fh:
+                if fh.read().strip() == h.hexdigest():
+                    return obj
         cmd = [nvcc] + NVCC_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))
         if verbose and (r.stdout or r.stderr):
             print(r.stdout + r.stderr)
+        with open(ostamp, "w") as fh:
+            fh.write(h.hexdigest())
         return obj
 
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:

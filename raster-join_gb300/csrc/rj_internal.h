@@ -136,6 +136,17 @@ struct rj_ctx {
     int sum_shift = 0;        // fixed-point scale 2^s of the current query's sums
     uint64_t row0 = 0, row1 = ~0ULL;   // rows of the current query (time index window)
     int server_running = 0;   // a serving loop owns the context
+    // kernel tuning (rj_set_tuning): forced shapes, -1 = default / autotuned
+    int point_shape = -1;
+    int count_shape = -1, count_bshift = -1;
+    int hybrid_exact_scale = 1;
+    int last_count_shape = -1, last_count_bshift = -1;
+    std::map<std::string, int> tuned;   // autotuned choice per query class
+    // exact partial sums of the last query (rj_get_sum_partials)
+    int forced_shift = RJ_SUM_SHIFT_AUTO;
+    std::vector<long long> last_fixed;
+    std::vector<double> last_nonfinite;
+    int last_shift = 0;
     void* batch_engine = nullptr;   // executor of rj_execute_batch
 };
 

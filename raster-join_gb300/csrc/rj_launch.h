@@ -143,6 +143,7 @@ struct PointArgs {
     const float4* zones;
     uint64_t row0;
     float4 qbox;
+    int shape = -1;              // kernel shape (-1: the default for the mapper)
 };
 constexpr int kZoneShift = 10;               // zones of 1024 rows
 void launch_zone_boxes(const float2* xy, uint64_t n, float4* zones, int sms, cudaStream_t st);
@@ -184,6 +185,31 @@ void launch_outline_mask(const float2* verts, const int* pindex, int P, const in
                          const HybXf& h, float margin, uint32_t* mask, int words, int sms, cudaStream_t st);
 void launch_dilate_mask(const uint32_t* in, uint32_t* out, int resx, int resy, int words, int radius,
                         int sms, cudaStream_t st);
+
+// Lean raster count over one canvas tile with a polygon label map
+// (rj_count_kernels.cu): no filter, count only.
+struct LabelCountArgs {
+    const float4* xy;            // location column as point pairs, 16-byte aligned
+    uint64_t n;                  // points
+    float4 col0, row0;           // the tile transform (s, t, h) per axis
+    int resx, resy;
+    const uint16_t* label;       // [resy][resx] polygon label, kEmptyLabel outside every polygon
+    const uint16_t* codes;       // [nby][nbx] block codes (label shared by the block, or mixed)
+    int bs;                      // log2 of the block side
+    int nbx;                     // blocks per canvas row
+    int code_words;              // 32-bit words of the code map (its u16 count rounded up)
+    int P;
+    unsigned long long* out_count;
+    // zone map (bounds of every 1024 rows; zrow0 = table row of xy[0]) or null
+    const float4* zones;
+    uint64_t zrow0;
+    float4 qbox;
+};
+void launch_block_codes(const uint16_t* label, int resx, int resy, int bs, int nbx, int nby, uint16_t* codes,
+                        int sms, cudaStream_t st);
+int label_count_shapes();
+size_t label_count_smem(int shape, int code_words, int P);
+bool launch_label_count(int shape, const LabelCountArgs& a, int sms, cudaStream_t st);
 
 // point side
 // smem_hist: histogram capacity decision done by the launcher.

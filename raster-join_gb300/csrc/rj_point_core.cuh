@@ -20,7 +20,6 @@
 // Per-polygon results accumulate in shared memory (count u32, sum f64) and are
 // flushed once per block with global atomics.
 #pragma once
-#include <cstdlib>
 
 #include "rj_device.cuh"
 #include "rj_launch.h"
@@ -288,7 +287,8 @@ k_points_pipe(PointArgs pa, M mp, int stages) {
             }
             // no copy may still be landing when the block exits
             const uint32_t first = it > (uint32_t)stages ? it - stages : 0u;
-            for (uint32_t j = first; j < it; ++j) mbar_wait(full + (j % stages), (j / stages) & 1u);
+            for (uint32_t j = first; j < it; ++j)
+                if (!mbar_wait(full + (j % stages), (j / stages) & 1u)) atomicOr(pa.err, 1);
         }
         return;
     }
@@ -542,29 +542,25 @@ static void launch_plain_t(const PointArgs& pa, const M& mp, int sms, cudaStream
     ++g_kernel_launches;
 }
 
-// Point-kernel variant: 0 = plain, 4 points x 256 threads; 2 = bulk-copy
+// Point-kernel shape: 0 = plain, 4 points x 256 threads; 2 = bulk-copy
 // pipeline; 3 = plain, 4 points x 512 threads.  Defaults measured on GB300
 // (config-2 query, 100M points): the hybrid pass is fastest with 3 (0.833 ms
 // vs 0.910 ms for 0), the raster-label and index passes with 0 (0.65 ms vs
 // 0.79 ms; 2.07 ms vs 2.36 ms).  Two more plain shapes were measured and
 // dropped: 8 points x 256 threads (hybrid 1.077 ms) and 4 points x 128
-// threads (0.949 ms).  RJ_POINT_VARIANT overrides the default for every
-// mapper (a tuning knob; every variant computes the same result).
+// threads (0.949 ms).  PointArgs::shape (rj_set_tuning RJ_TUNE_POINT_SHAPE)
+// overrides the default for every mapper; every shape computes the same
+// result.
 template <class M>
-static int point_variant() {
-    static int v = -2;
-    if (v == -2) {
-        const char* e = getenv("RJ_POINT_VARIANT");
-        v = e ? atoi(e) : -1;
-        if (v != 0 && v != 2 && v != 3) v = -1;
-    }
-    if (v >= 0) return v;
+static int point_variant(const PointArgs& pa) {
+    const int v = pa.shape;
+    if (v == 0 || v == 2 || v == 3) return v;
     return M::kDefer ? 3 : 0;   // the hybrid mapper defers border points to a block queue
 }
 
 template <class M, bool AGG, bool SMEM>
 static void launch_points_t(const PointArgs& pa, const M& mp, int sms, cudaStream_t st) {
-    if (point_variant<M>() == 3) launch_plain_t<M, AGG, SMEM, 1, 512>(pa, mp, sms, st);
+    if (point_variant<M>(pa) == 3) launch_plain_t<M, AGG, SMEM, 1, 512>(pa, mp, sms, st);
     else launch_plain_t<M, AGG, SMEM, 1, 256>(pa, mp, sms, st);
 }
 
@@ -599,7 +595,7 @@ static void launch_points(const PointArgs& pa, const M& mp, int sms, cudaStream_
     const bool agg = pa.f.aggr != 0;
     const bool smem_ok = hist_bytes(pa.P, agg) + queue_bytes(M::kDefer) <= (size_t)std::max(g_max_smem_optin - 1024, 0);
     // bulk-copy pipeline for tables of at least one tile per SM (columns are 16-byte aligned)
-    if (point_variant<M>() == 2 && pa.err && pa.n >= (uint64_t)kPipeTile * sms && smem_ok) {
+    if (point_variant<M>(pa) == 2 && pa.err && pa.n >= (uint64_t)kPipeTile * sms && smem_ok) {
         bool launched = agg ? launch_pipe_t<M, true, true>(pa, mp, sms, st) : launch_pipe_t<M, false, true>(pa, mp, sms, st);
         if (launched) return;
     }

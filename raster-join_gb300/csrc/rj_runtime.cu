@@ -25,14 +25,6 @@ using namespace rj;
 
 namespace rjh {
 
-// refinement of the query grid for the hybrid join's exact tests (override
-// with RJ_HYBRID_EXACT_SCALE: 1, 2, 4)
-static const int kHybridExactScale = [] {
-    const char* e = getenv("RJ_HYBRID_EXACT_SCALE");
-    const int v = e ? atoi(e) : 1;
-    return (v == 1 || v == 2 || v == 4) ? v : 1;
-}();
-
 
 int fail(rj_ctx* c, int code, const char* fmt, ...) {
     char buf[512];
@@ -282,9 +274,13 @@ int build_filter(rj_ctx* ctx, const rj_query* q, DevFilter& f, bool force_count,
         for (int c = 0; c < f.ncol; ++c)
             if (f.col[c] == f.aggr_col) f.aggr_ci = c;
         // fixed-point sums: |v| * 2^s * n < 2^62 for every value and any subset
-        const double amax = std::max((double)col->absmax, 1e-30);
-        int shift = (int)std::floor(62.0 - std::log2(amax) - std::log2((double)ctx->npts + 1.0));
-        shift = std::max(-90, std::min(150, shift));
+        int shift = rj_sum_shift_for((double)col->absmax, ctx->npts);
+        if (ctx->forced_shift != RJ_SUM_SHIFT_AUTO) {
+            if (ctx->forced_shift > shift)
+                return fail(ctx, RJ_E_INVALID, "sum shift %d too fine for this table (values up to %g over %llu rows: %d)",
+                            ctx->forced_shift, (double)col->absmax, (unsigned long long)ctx->npts, shift);
+            shift = ctx->forced_shift;
+        }
         ctx->sum_shift = shift;
         f.sum_scale = std::ldexp(1.0f, shift - 32);
     }
@@ -564,6 +560,7 @@ PointArgs make_point_args(rj_ctx* ctx, const DevFilter& f, unsigned long long* o
     pa.out_sum = os;
     pa.out_nonfinite = (double*)ctx->scratch["out_nonfinite"].p;
     pa.err = ctx->d_err;
+    pa.shape = ctx->point_shape;
     // the zone check costs a dependent load per iteration: skip it when the
     // query's reach holds every finite location of the table (nothing to skip)
     const float4 tb = ctx->table_box, qb = ctx->qbox;
@@ -820,6 +817,131 @@ int label_map(rj_ctx* ctx, PolyPassArgs& a, const char* key, size_t npix, const 
     return RJ_OK;
 }
 
+// Lean count pass over a label map (rj_count_kernels.cu): one canvas tile,
+// no filter, count only, a resident table.  Builds the block-code map(s) of
+// the label map and runs the count kernel; the shape and block size are the
+// ones forced with rj_set_tuning, else autotuned: on the first query of its
+// class (polygons, canvas, table size) on this context every candidate is
+// timed once on the table itself, into a scratch output, and the fastest is
+// kept.  *done = false: the pass does not apply (the caller takes the
+// generic label pass).
+int label_count_pass(rj_ctx* ctx, const DevFilter& f, const RasterPlan& rp, const uint16_t* label, ExecState& es,
+                     bool* done) {
+    *done = false;
+    ctx->last_count_shape = ctx->last_count_bshift = -1;
+    if (f.ncol != 0 || f.aggr || rp.splitx != 1 || rp.splity != 1 || ctx->streamed) return RJ_OK;
+    PointArgs pa = make_point_args(ctx, f, es.out_count, nullptr);
+    if (((uintptr_t)pa.xy & 15) != 0) return RJ_OK;
+    const int P = ctx->ps->P;
+    LabelCountArgs a{};
+    a.xy = reinterpret_cast<const float4*>(pa.xy);
+    a.n = pa.n;
+    a.col0 = rp.colxf[0];
+    a.row0 = rp.rowxf[0];
+    a.resx = rp.resx;
+    a.resy = rp.resy;
+    a.label = label;
+    a.P = P;
+    a.out_count = es.out_count;
+    a.zones = pa.zones;
+    a.zrow0 = pa.row0;
+    a.qbox = pa.qbox;
+    // candidate block sizes: the smallest whose code map leaves room in
+    // shared memory for the histogram, and the next one
+    int bs0 = 4;
+    auto code_words = [&](int bs) {
+        const long long nbx = ((long long)rp.resx + (1 << bs) - 1) >> bs, nby = ((long long)rp.resy + (1 << bs) - 1) >> bs;
+        return (nbx * nby + 1) / 2;
+    };
+    while (bs0 < 8 && code_words(bs0) * 4 + (long long)P * 4 > 160 * 1024) ++bs0;
+    std::vector<int> bss;
+    if (ctx->count_bshift >= 4 && ctx->count_bshift <= 8) bss.push_back(ctx->count_bshift);
+    else {
+        bss.push_back(bs0);
+        if (bs0 < 8) bss.push_back(bs0 + 1);
+    }
+    int rc;
+    std::map<int, uint16_t*> codes;
+    for (int bs : bss) {
+        const int nbx = (rp.resx + (1 << bs) - 1) >> bs, nby = (rp.resy + (1 << bs) - 1) >> bs;
+        uint16_t* c;
+        char key[32];
+        std::snprintf(key, sizeof key, "label_codes%d", bs);
+        if ((rc = scratch_t(ctx, key, (size_t)code_words(bs) * 2, &c))) return rc;
+        launch_block_codes(label, rp.resx, rp.resy, bs, nbx, nby, c, ctx->sms, ctx->stream);
+        codes[bs] = c;
+    }
+    es.ph->mark(2);   // the code maps belong to the polygon side
+    auto args_for = [&](int bs) {
+        LabelCountArgs b = a;
+        b.bs = bs;
+        b.nbx = (rp.resx + (1 << bs) - 1) >> bs;
+        b.codes = codes[bs];
+        b.code_words = (int)code_words(bs);
+        return b;
+    };
+    const int nshapes = label_count_shapes();
+    std::vector<std::pair<int, int>> cands;   // (shape, bs)
+    for (int bs : bss)
+        for (int sh = 0; sh < nshapes; ++sh)
+            if (ctx->count_shape < 0 || ctx->count_shape == sh)
+                if (label_count_smem(sh, (int)code_words(bs), P) <= 200 * 1024) cands.push_back({sh, bs});
+    if (cands.empty()) return RJ_OK;
+    std::pair<int, int> pick = cands[0];
+    if (cands.size() > 1) {
+        char key[160];
+        std::snprintf(key, sizeof key, "count:%d:%dx%d:%d:%d:%d", P, rp.resx, rp.resy,
+                      (int)std::log2((double)std::max<uint64_t>(a.n, 1)), ctx->count_shape, ctx->count_bshift);
+        auto it = ctx->tuned.find(key);
+        if (it != ctx->tuned.end()) {
+            pick = cands[std::min<size_t>((size_t)it->second, cands.size() - 1)];
+        } else {
+            // time each candidate once on (a prefix of) the table, into a scratch output
+            unsigned long long* tout;
+            if ((rc = scratch_t(ctx, "tune_count", (size_t)P, &tout))) return rc;
+            const uint64_t tn = std::min<uint64_t>(a.n & ~1ULL, 1ULL << 28);
+            cudaEvent_t e0, e1;
+            RJ_CUDA(cudaEventCreate(&e0));
+            RJ_CUDA(cudaEventCreate(&e1));
+            float best = 1e30f;
+            int besti = -1;
+            for (size_t i = 0; i < cands.size(); ++i) {
+                LabelCountArgs b = args_for(cands[i].second);
+                b.out_count = tout;
+                // first launch of a shape loads it: a tiny warm-up launch
+                LabelCountArgs w = b;
+                w.n = std::min<uint64_t>(b.n & ~1ULL, 1ULL << 16);
+                if (!launch_label_count(cands[i].first, w, ctx->sms, ctx->stream)) continue;
+                b.n = tn;
+                RJ_CUDA(cudaEventRecord(e0, ctx->stream));
+                launch_label_count(cands[i].first, b, ctx->sms, ctx->stream);
+                RJ_CUDA(cudaEventRecord(e1, ctx->stream));
+                RJ_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                RJ_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best) {
+                    best = ms;
+                    besti = (int)i;
+                }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            RJ_CUDA(cudaGetLastError());
+            if (besti < 0) return RJ_OK;
+            ctx->tuned[key] = besti;
+            pick = cands[(size_t)besti];
+        }
+    }
+    ctx->passes = 1;
+    ctx->copy_ms = 0;
+    if (!launch_label_count(pick.first, args_for(pick.second), ctx->sms, ctx->stream)) return RJ_OK;
+    RJ_CUDA(cudaGetLastError());
+    ctx->last_count_shape = pick.first;
+    ctx->last_count_bshift = pick.second;
+    *done = true;
+    return RJ_OK;
+}
+
 // Raster join (RasterJoin::performJoin RasterJoin.cpp:196-243) and the
 // error-bounds join (RasterJoinBounds::performJoin RasterJoinBounds.cpp:306-381).
 int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
@@ -872,9 +994,11 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
         if ((rc = label_map(ctx, a, "label", npix, nullptr, 0, ckey, &label, &overlap))) return rc;
         es.ph->mark(2);
         if (!overlap) {
-            if ((rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
-                     launch_raster_label(pa, cx, label, ctx->sms, ctx->stream);
-                 })))
+            bool lean = false;
+            if ((rc = label_count_pass(ctx, f, rp, label, es, &lean))) return rc;
+            if (!lean && (rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
+                              launch_raster_label(pa, cx, label, ctx->sms, ctx->stream);
+                          })))
                 return rc;
             RJ_CUDA(cudaGetLastError());
             es.ph->mark(3);
@@ -961,7 +1085,8 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     if (q->grid_res <= 0 || q->grid_res > 8192) return fail(ctx, RJ_E_INVALID, "grid resolution %d out of range", q->grid_res);
     es.ph->mark(1);
     ExactIndex ix{};
-    if ((rc = build_exact(ctx, q->grid_res, ix, kHybridExactScale))) return rc;
+    // refinement of the query grid for the exact tests (RJ_TUNE_HYBRID_EXACT_SCALE)
+    if ((rc = build_exact(ctx, q->grid_res, ix, ctx->hybrid_exact_scale))) return rc;
 
     // canvas: getResolution(bbox, fboSize) (HybridJoin.cpp:62-66, Utils.h:29-34)
     const double dx = ctx->ps->bbox[2] - ctx->ps->bbox[0], dy = ctx->ps->bbox[3] - ctx->ps->bbox[1];
@@ -1607,6 +1732,9 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
     RJ_CUDA(cudaGetLastError());
     if (derr) return fail(ctx, RJ_E_TIMEOUT, "a bounded device wait ran out (status 0x%x)", derr);
     decode_result(P, hc.data(), hq.data(), hnf.data(), ctx->sum_shift, hb.empty() ? nullptr : hb.data(), res);
+    ctx->last_fixed.assign(hq.begin(), hq.end());
+    ctx->last_nonfinite = hnf;
+    ctx->last_shift = ctx->sum_shift;
     // timings (GLHandler::printTimeStats fields)
     rj_timings& t = ctx->tm;
     std::memset(&t, 0, sizeof t);
@@ -1629,6 +1757,80 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
     t.accuracy = (q->function_type == RJ_RASTER_JOIN) ? (int)q->accuracy_m : 0;
     t.kernel_launches = g_kernel_launches;
     return RJ_OK;
+}
+
+int32_t rj_sum_shift_for(double max_abs, uint64_t rows) {
+    const double amax = std::max(std::isfinite(max_abs) ? std::fabs(max_abs) : 0.0, 1e-30);
+    const int shift = (int)std::floor(62.0 - std::log2(amax) - std::log2((double)rows + 1.0));
+    return std::max(-90, std::min(150, shift));
+}
+
+int rj_set_sum_shift(rj_ctx* ctx, int32_t shift) {
+    if (!ctx) return RJ_E_INVALID;
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    if (shift != RJ_SUM_SHIFT_AUTO && (shift < -90 || shift > 150))
+        return fail(ctx, RJ_E_INVALID, "sum shift %d out of range -90..150", shift);
+    ctx->forced_shift = shift;
+    return RJ_OK;
+}
+
+int rj_get_sum_partials(const rj_ctx* ctx, int64_t* fixed, double* nonfinite, int32_t* shift) {
+    if (!ctx) return RJ_E_INVALID;
+    const size_t P = ctx->last_fixed.size();
+    if (fixed && P) std::memcpy(fixed, ctx->last_fixed.data(), P * sizeof(int64_t));
+    if (nonfinite && P) std::memcpy(nonfinite, ctx->last_nonfinite.data(), P * sizeof(double));
+    if (shift) *shift = ctx->last_shift;
+    return RJ_OK;
+}
+
+int rj_column_absmax(const rj_ctx* ctx, int32_t attrib_id, double* out) {
+    if (!ctx || !out) return RJ_E_INVALID;
+    const Column* c = find_col(ctx, attrib_id);
+    if (!c) return RJ_E_INVALID;
+    *out = (double)c->absmax;
+    return RJ_OK;
+}
+
+int rj_set_tuning(rj_ctx* ctx, int32_t knob, int32_t value) {
+    if (!ctx) return RJ_E_INVALID;
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    switch (knob) {
+        case RJ_TUNE_POINT_SHAPE:
+            if (value != -1 && value != 0 && value != 2 && value != 3)
+                return fail(ctx, RJ_E_INVALID, "point shape %d: -1, 0, 2 or 3", value);
+            ctx->point_shape = value;
+            return RJ_OK;
+        case RJ_TUNE_COUNT_SHAPE:
+            if (value < -1 || value >= label_count_shapes())
+                return fail(ctx, RJ_E_INVALID, "count shape %d: -1..%d", value, label_count_shapes() - 1);
+            ctx->count_shape = value;
+            return RJ_OK;
+        case RJ_TUNE_COUNT_BLOCK_SHIFT:
+            if (value != -1 && (value < 4 || value > 8))
+                return fail(ctx, RJ_E_INVALID, "count block shift %d: -1 or 4..8", value);
+            ctx->count_bshift = value;
+            return RJ_OK;
+        case RJ_TUNE_HYBRID_EXACT_SCALE:
+            if (value != 1 && value != 2 && value != 4)
+                return fail(ctx, RJ_E_INVALID, "hybrid exact scale %d: 1, 2 or 4", value);
+            ctx->hybrid_exact_scale = value;
+            ctx->ps->exact.valid = false;
+            return RJ_OK;
+        default:
+            return fail(ctx, RJ_E_INVALID, "unknown tuning knob %d", knob);
+    }
+}
+
+int rj_get_tuning(const rj_ctx* ctx, int32_t knob, int32_t* value) {
+    if (!ctx || !value) return RJ_E_INVALID;
+    switch (knob) {
+        case RJ_TUNE_POINT_SHAPE: *value = ctx->point_shape; return RJ_OK;
+        case RJ_TUNE_COUNT_SHAPE: *value = ctx->last_count_shape; return RJ_OK;
+        case RJ_TUNE_COUNT_BLOCK_SHIFT: *value = ctx->last_count_bshift; return RJ_OK;
+        case RJ_TUNE_HYBRID_EXACT_SCALE: *value = ctx->hybrid_exact_scale; return RJ_OK;
+        case RJ_TUNE_COUNT_SHAPES: *value = label_count_shapes(); return RJ_OK;
+        default: return RJ_E_INVALID;
+    }
 }
 
 int rj_get_timings(const rj_ctx* ctx, rj_timings* out) {

@@ -33,6 +33,9 @@ STATUS = {0: "RJ_OK", -1: "RJ_E_INVALID", -2: "RJ_E_OOM", -3: "RJ_E_TOO_MANY_CON
           -4: "RJ_E_TIMEOUT", -5: "RJ_E_CUDA", -6: "RJ_E_NO_DATA", -7: "RJ_E_UNSUPPORTED",
           -8: "RJ_E_BUSY", 1: "RJ_PENDING"}
 RJ_PENDING = 1
+SUM_SHIFT_AUTO = -2147483648
+# rj_set_tuning knobs (include/rj.h)
+TUNE_POINT_SHAPE, TUNE_COUNT_SHAPE, TUNE_COUNT_BLOCK_SHIFT, TUNE_HYBRID_EXACT_SCALE, TUNE_COUNT_SHAPES = 0, 1, 2, 3, 4
 BATCH_AUTOTUNE = 0x1
 BATCH_NO_FUSE = 0x2
 MAX_CONSTRAINTS = 10
@@ -152,6 +155,12 @@ def load_library(path=LIB_PATH):
         "rj_submit": (C.c_int, [C.c_void_p, P(Query), C.c_void_p, P(Result), P(C.c_uint64)]),
         "rj_poll": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int32, P(RequestInfo)]),
         "rj_server_destroy": (None, [C.c_void_p]),
+        "rj_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+        "rj_get_sum_partials": (C.c_int, [C.c_void_p, P(C.c_int64), P(C.c_double), P(C.c_int32)]),
+        "rj_set_sum_shift": (C.c_int, [C.c_void_p, C.c_int32]),
+        "rj_sum_shift_for": (C.c_int32, [C.c_double, C.c_uint64]),
+        "rj_column_absmax": (C.c_int, [C.c_void_p, C.c_int32, P(C.c_double)]),
+        "rj_get_tuning": (C.c_int, [C.c_void_p, C.c_int32, P(C.c_int32)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -404,6 +413,35 @@ class GLHandler:
     def setStream(self, stream_ptr):
         self._check(self.lib.rj_set_stream(self.ctx, C.c_void_p(stream_ptr)))
 
+    # ---- exact partial sums (rj_get_sum_partials / rj_set_sum_shift) ----
+    def sumPartials(self):
+        """(fixed int64[P], nonfinite float64[P], shift) of the last execute."""
+        P = len(self.last.count) if self.last is not None else 0
+        fixed = np.zeros(P, np.int64)
+        nf = np.zeros(P, np.float64)
+        sh = C.c_int32(0)
+        self._check(self.lib.rj_get_sum_partials(self.ctx, fixed.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                 nf.ctypes.data_as(C.POINTER(C.c_double)), C.byref(sh)))
+        return fixed, nf, sh.value
+
+    def setSumShift(self, shift=None):
+        self._check(self.lib.rj_set_sum_shift(self.ctx, SUM_SHIFT_AUTO if shift is None else int(shift)))
+
+    def columnAbsMax(self, attrib_id):
+        self.upload()
+        v = C.c_double(0.0)
+        self._check(self.lib.rj_column_absmax(self.ctx, int(attrib_id), C.byref(v)))
+        return v.value
+
+    # ---- kernel tuning (rj_set_tuning / rj_get_tuning; results never change) ----
+    def setTuning(self, knob, value):
+        self._check(self.lib.rj_set_tuning(self.ctx, int(knob), int(value)))
+
+    def getTuning(self, knob):
+        v = C.c_int32(0)
+        self._check(self.lib.rj_get_tuning(self.ctx, int(knob), C.byref(v)))
+        return v.value
+
     # ---- data upload ----
     def upload(self, force=False):
         dh = self.dataHandler
@@ -573,6 +611,16 @@ class GLHandler:
         buf = C.create_string_buffer(512)
         self._check(self.lib.rj_format_time_stats(self.ctx, buf, 512))
         return buf.value.decode()
+
+
+def sum_shift_for(max_abs, rows):
+    """Fixed-point shift the library picks for |values| <= max_abs over `rows` rows."""
+    return int(load_library().rj_sum_shift_for(float(max_abs), int(rows)))
+
+
+def decode_sums(fixed, nonfinite, shift):
+    """Per-polygon sums from exact partials, as rj_execute decodes them."""
+    return np.ldexp(np.asarray(fixed, np.int64).astype(np.float64), -int(shift)) + np.asarray(nonfinite, np.float64)
 
 
 def decode_avg(agg):

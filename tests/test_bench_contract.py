@@ -1,5 +1,6 @@
 """bench.py's reference arm on a small sample: one JSON line with the keys the
-benchmark contract asks for, and the same metric string as the GPU arm."""
+benchmark contract asks for, and the same metric string and workload as the
+GPU arm."""
 import json
 import os
 import subprocess
@@ -24,5 +25,6 @@ def test_reference_arm_line(built):
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     sys.path.insert(0, ROOT)
     import bench
-    assert d["metric"] == bench.metric_name("hybrid")
-    assert d["config"]["join"] == "hybrid"
+    assert d["metric"] == bench.METRIC
+    # the GPU arm reports the same workload dict for the same sizes
+    assert d["config"] == bench.headline_config(200000, 200000)

@@ -125,6 +125,29 @@ def test_c1_error_bounds(handler, c1):
     assert np.all((exact.astype(np.int64) >= lo) & (exact.astype(np.int64) <= hi))
 
 
+@pytest.mark.parametrize("which", ["c1", "stars"])
+def test_error_bounds_reference_line_filter(handler, c1, stars, which):
+    """RJ_FLAG_LINE_FILTER: the reference's outline pass keeps an edge's
+    fragment only when the pixel centre is within 0.5 px of the edge
+    (line-bound.frag:221); bounds bit-exact against the oracle's restatement,
+    and never wider than the default (every intersected pixel) bounds."""
+    pts, verts, pidx = c1 if which == "c1" else stars
+    cell = 10.0 if which == "c1" else 25.0
+    handler.setDataHandler(make_dh(pts, verts, pidx))
+    handler.setCellSize(cell)
+    handler.flags = rj.FLAG_LINE_FILTER
+    try:
+        got = handler.execute(rj.RasterJoinBoundFn)
+    finally:
+        handler.flags = 0
+    c, _, b = oracle.raster_join(pts["xy"], verts, pidx, cell, bounds=True, line_filter=True)
+    np.testing.assert_array_equal(got.count, c)
+    np.testing.assert_array_equal(got.bounds.astype(np.int64), b)
+    full = handler.execute(rj.RasterJoinBoundFn)
+    assert np.all(got.bounds.astype(np.int64) <= full.bounds.astype(np.int64))
+    assert got.bounds.astype(np.int64).sum() < full.bounds.astype(np.int64).sum()
+
+
 def c2_query(dh):
     dh.setQueryConstraints([(4, rj.GT, 2), (5, rj.LT, 8), (3, rj.LT, 50.0)])
     dh.setTimeRange(2, synth.T0, synth.T0 + synth.YEAR // 2)
