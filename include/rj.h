@@ -264,8 +264,8 @@ RJ_API int rj_column_absmax(const rj_ctx *ctx, int32_t attrib_id, double *out);
  *   RJ_TUNE_POINT_SHAPE      generic point pass: -1 = default per join,
  *                            0 = 4 points x 256 threads, 2 = bulk-copy
  *                            pipeline, 3 = 4 points x 512 threads
- *   RJ_TUNE_COUNT_SHAPE      lean raster count pass (one canvas tile, label
- *                            map, no filter, count): -1 = autotuned (each
+ *   RJ_TUNE_COUNT_SHAPE      lean raster label pass (one canvas tile, label
+ *                            map, a resident table): -1 = autotuned (each
  *                            shape is timed once per context and query
  *                            class on the table itself, the fastest is
  *                            kept), else a shape index
@@ -274,7 +274,16 @@ RJ_API int rj_column_absmax(const rj_ctx *ctx, int32_t attrib_id, double *out);
  *                            else log2 of the block side (4..8)
  *   RJ_TUNE_HYBRID_EXACT_SCALE classified grid of the hybrid join's exact
  *                            tests: the query grid refined 1, 2 or 4 times
- *   RJ_TUNE_COUNT_SHAPES     (read only) number of count-pass shapes
+ *   RJ_TUNE_COUNT_SHAPES     (read only) number of plain count-pass shapes
+ *   RJ_TUNE_LEAN_SHAPES      (read only) number of shapes of the same pass
+ *                            with filters (interval form, <= 4 columns) or
+ *                            a summed aggregate; RJ_TUNE_COUNT_SHAPE indexes
+ *                            the shapes of the form the query takes
+ *   RJ_TUNE_WAIT_LIMIT       tries of a bounded device wait of the bulk-copy
+ *                            pipeline (RJ_TUNE_POINT_SHAPE 2) before it gives
+ *                            up and the call returns RJ_E_TIMEOUT (default
+ *                            4194304; the wait for copies still in flight at
+ *                            the end of a block keeps that default)
  * rj_get_tuning on RJ_TUNE_COUNT_SHAPE / _BLOCK_SHIFT reports the values the
  * last count pass ran with (-1 when the last query did not take it). */
 #define RJ_TUNE_POINT_SHAPE        0
@@ -282,8 +291,20 @@ RJ_API int rj_column_absmax(const rj_ctx *ctx, int32_t attrib_id, double *out);
 #define RJ_TUNE_COUNT_BLOCK_SHIFT  2
 #define RJ_TUNE_HYBRID_EXACT_SCALE 3
 #define RJ_TUNE_COUNT_SHAPES       4
+#define RJ_TUNE_LEAN_SHAPES        5
+#define RJ_TUNE_WAIT_LIMIT         6
 RJ_API int rj_set_tuning(rj_ctx *ctx, int32_t knob, int32_t value);
 RJ_API int rj_get_tuning(const rj_ctx *ctx, int32_t knob, int32_t *value);
+
+/* ---- failure handling ------------------------------------------------------
+ * Runs the library's bounded device wait alone: one block waits, at most
+ * `limit` tries, on a barrier that nothing completes, so the wait runs out
+ * and the call returns RJ_E_TIMEOUT the way a join does when a bounded wait
+ * of its pipeline runs out (the kernel returns; the context stays usable).
+ * RJ_OK would mean the wait did not run out.  The reference has no
+ * counterpart: it had no device-side waits and exit(0)ed on errors
+ * (GLData.cpp:18-23, GLFunction.cpp:251-252). */
+RJ_API int rj_selftest_bounded_wait(rj_ctx *ctx, uint32_t limit);
 
 /* ---- polygon sets --------------------------------------------------------
  * A polygon collection held on the device independently of the context's own

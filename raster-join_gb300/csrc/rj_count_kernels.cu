@@ -24,15 +24,12 @@
 //   * streams the location column with fully coalesced 128-bit evict-first
 //     loads (each lane two points per load), several loads in flight per
 //     thread before the first is used.
-// The pixel of a point is computed exactly as in the generic pass (per-tile
-// MVP in fp32, snap to 1/256 px, floor), with both coordinates of a point in
-// one packed fp32x2 instruction per operation, so the counts are identical.
-#include "rj_launch.h"
+// The pixel of a point is the generic pass's (per-tile MVP in fp32, snap to
+// 1/256 px, floor), computed with two exact rewrites that save operations
+// (rj_lean.cuh), so the counts are identical.
+#include "rj_lean.cuh"
 
 namespace rj {
-
-// Marker in a block-code map: the block's pixels carry different labels.
-constexpr uint16_t kCodeMixed = 0xFFFEu;
 
 // Block codes from a label map: one warp per block.
 __global__ void k_block_codes(const uint16_t* __restrict__ label, int resx, int resy, int bs, int nbx, int nby,
@@ -63,54 +60,6 @@ void launch_block_codes(const uint16_t* label, int resx, int resy, int bs, int n
     blocks = std::max(1LL, std::min(blocks, (long long)sms * 16));
     k_block_codes<<<(unsigned)blocks, 256, 0, st>>>(label, resx, resy, bs, nbx, nby, codes);
     ++g_kernel_launches;
-}
-
-// Pixel of (x, y) in the tile: the same operations as win_coord + snap_win +
-// pix_of, evaluated on the (x, y) pair at once with packed fp32x2
-// instructions (each lane of mul.rn.f32x2 / add.rn.f32x2 rounds like
-// __fmul_rn / __fadd_rn).  snap_win clamps the window coordinate to +-2^20 px
-// before the conversion; here the conversion saturates instead, which puts a
-// coordinate beyond the clamp on a pixel outside [0, res) just the same, and
-// NaN (which converts to 0) is tested apart.  Returns whether the pixel lies
-// in the canvas.
-__device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ float2 unpack2(unsigned long long v) {
-    float2 r;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
-    return r;
-}
-__device__ __forceinline__ unsigned long long fmul2_rn(unsigned long long a, unsigned long long b) {
-    unsigned long long r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ unsigned long long fadd2_rn(unsigned long long a, unsigned long long b) {
-    unsigned long long r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-
-struct TileXf2 {
-    unsigned long long s, t, h, sub;   // (x, y) pairs: scale, offset, half resolution, 256
-};
-
-__device__ __forceinline__ TileXf2 tile_xf2(const LabelCountArgs& a) {
-    return TileXf2{pack2(a.col0.x, a.row0.x), pack2(a.col0.y, a.row0.y), pack2(a.col0.z, a.row0.z),
-                   pack2((float)kSub, (float)kSub)};
-}
-
-__device__ __forceinline__ bool count_pixel(const LabelCountArgs& a, const TileXf2& xf, float x, float y, int& px,
-                                            int& py) {
-    const unsigned long long ndc = fadd2_rn(fmul2_rn(xf.s, pack2(x, y)), xf.t);
-    const unsigned long long w = fadd2_rn(fmul2_rn(xf.h, ndc), xf.h);
-    const float2 q = unpack2(fmul2_rn(w, xf.sub));
-    px = __float2int_rn(q.x) >> kSubpixelBits;
-    py = __float2int_rn(q.y) >> kSubpixelBits;
-    return (unsigned)px < (unsigned)a.resx && (unsigned)py < (unsigned)a.resy && !isnan(q.x) && !isnan(q.y);
 }
 
 template <int BLOCK, int NV, bool CODES, bool WARP_HIST>

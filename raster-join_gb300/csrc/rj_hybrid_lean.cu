@@ -1,0 +1,299 @@
+// rj_hybrid_lean.cu -- lean point pass of the hybrid join (hybrid.glsl:224-300,
+// HybridJoin::glJoin HybridJoin.cpp:87-195) over the hybrid canvas's polygon
+// label map, with interval-form filters on up to four columns and an optional
+// summed aggregate.
+//
+// Per point: the predicates, the hybrid canvas pixel (rasterize,
+// hybrid.glsl:187-200), then the pixel's label through the block-code map in
+// shared memory (the label map in L2 only for blocks whose pixels differ).
+// A labelled pixel is inside exactly one polygon and away from every
+// outline: the point goes to that polygon's histogram (plain shared-memory
+// atomics, count and two-word fixed-point sum as in rj_lean_kernels.cu).  A
+// pixel marked border (within the fp32 error radius of an outline, isBorder
+// hybrid.glsl:174-185) sends the point to the exact test through the
+// classified grid: such points are appended to a block-wide queue with one
+// atomic per warp (ballot + prefix, no divergent per-lane appends) and run
+// in full blocks, one point per thread, when the queue holds a block's worth.
+#include "rj_lean.cuh"
+#include "rj_point_core.cuh"
+
+namespace rj {
+
+namespace {
+
+// Hist-like adapter for exact_probe: adds to the block's histogram copy.
+template <bool AGG>
+struct LeanHist {
+    uint32_t* cnt;
+    uint32_t* lo;
+    uint32_t* hi;
+    const LeanCols* lc;
+    __device__ __forceinline__ void add(int p, float v) const {
+        atomicAdd(cnt + p, 1u);
+        if (AGG) {
+            if (isfinite(v)) {
+                const unsigned long long q = (unsigned long long)fixed_value(v, lc->scale);
+                const uint32_t qlo = (uint32_t)q;
+                const uint32_t old = atomicAdd(lo + p, qlo);
+                atomicAdd(hi + p, (uint32_t)(q >> 32) + ((old + qlo < old) ? 1u : 0u));
+            } else {
+                atomicAdd(lc->nonfinite + p, (double)v);
+            }
+        }
+    }
+};
+
+template <int NCOL>
+__device__ __forceinline__ bool hyb_pass(const LeanCols& lc, const uint32_t (&v)[NCOL > 0 ? NCOL : 1]) {
+    bool ok = true;
+    #pragma unroll
+    for (int c = 0; c < NCOL; ++c) {
+        const uint32_t key = v[c] ^ (((uint32_t)((int32_t)v[c] >> 31) & lc.fm[c]) ^ lc.xm[c]);
+        ok &= (key - lc.lo[c]) <= lc.span[c];
+    }
+    return ok;
+}
+
+// kind of a point: 0 none, 1 labelled (label in *lab), 2 border (exact test)
+__device__ __forceinline__ int hyb_classify(const HybLeanArgs& a, const uint16_t* sc, float x, float y, uint32_t& lab) {
+    int px, py;
+    if (!hyb_rasterize(a.h, x, y, px, py)) return 0;
+    if (px >= a.h.resx || py >= a.h.resy) return 2;
+    uint32_t c = sc[(py >> a.bs) * a.nbx + (px >> a.bs)];
+    if (c == kCodeMixed) c = __ldg(a.label + (size_t)py * a.h.resx + px);
+    if (c == kBorderLabel) return 2;
+    lab = c;
+    return c < (uint32_t)a.P ? 1 : 0;
+}
+
+}  // namespace
+
+template <int BLOCK, int NV, int NCOL, bool AGG>
+__global__ void __launch_bounds__(BLOCK) k_hybrid_lean(HybLeanArgs a, LeanCols lc) {
+    extern __shared__ uint32_t s_words[];
+    constexpr int HW = AGG ? 3 : 1;
+    constexpr int QCAP = BLOCK * (1 + 2 * NV);        // < BLOCK left over + every point of one iteration
+    uint32_t* s_code = s_words;
+    uint32_t* s_hist = s_code + a.code_words;          // lc.copies x HW x P
+    float* qx = reinterpret_cast<float*>(s_hist + lc.copies * HW * a.P);
+    float* qy = qx + QCAP;
+    float* qv = qy + QCAP;
+    int* qn = reinterpret_cast<int*>(qv + QCAP);
+    {
+        const uint32_t* g = reinterpret_cast<const uint32_t*>(a.codes);
+        for (int i = threadIdx.x; i < a.code_words; i += BLOCK) s_code[i] = __ldg(g + i);
+        for (int i = threadIdx.x; i < lc.copies * HW * a.P; i += BLOCK) s_hist[i] = 0u;
+        if (threadIdx.x == 0) *qn = 0;
+    }
+    __syncthreads();
+    const uint16_t* sc = reinterpret_cast<const uint16_t*>(s_code);
+    uint32_t* h_cnt = s_hist + ((threadIdx.x >> 5) & (lc.copies - 1)) * HW * a.P;
+    const LeanHist<AGG> hist{h_cnt, h_cnt + a.P, h_cnt + 2 * a.P, &lc};
+    const int lane = threadIdx.x & 31;
+
+    const uint64_t npairs = a.n >> 1;
+    constexpr uint64_t kPerIter = (uint64_t)BLOCK * NV;
+    const uint64_t warp_ofs = (uint64_t)(threadIdx.x >> 5) * 32 * NV;
+    const uint64_t lane_ofs = warp_ofs + lane;
+    // block-uniform trip count (the queue drain below has block barriers)
+    for (uint64_t base = (uint64_t)blockIdx.x * kPerIter; base < npairs; base += (uint64_t)gridDim.x * kPerIter) {
+        bool skip = false;
+        if (a.zones) {
+            const uint64_t r0 = a.zrow0 + 2 * (base + warp_ofs);
+            const uint64_t r1 = a.zrow0 + min(2 * (base + warp_ofs + 32 * NV), a.n) - 1;
+            bool meets = false;
+            if (r0 <= r1 && (uint64_t)lane <= (r1 >> kZoneShift) - (r0 >> kZoneShift)) {
+                const float4 b = __ldg(a.zones + (r0 >> kZoneShift) + lane);
+                meets = !(b.z < a.qbox.x || b.x > a.qbox.z || b.w < a.qbox.y || b.y > a.qbox.w);
+            }
+            skip = !__any_sync(0xffffffffu, meets);
+        }
+        if (!skip) {
+            float4 p[NV];
+            uint2 cv[NCOL > 0 ? NCOL : 1][NV];
+            uint2 av[NV];
+            #pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                const uint64_t i = base + lane_ofs + (uint64_t)k * 32;
+                const bool live = i < npairs;
+                p[k] = live ? __ldcs(a.xy + i) : make_float4(NAN, NAN, NAN, NAN);
+                #pragma unroll
+                for (int c = 0; c < NCOL; ++c) cv[c][k] = live ? __ldcs(lc.col[c] + i) : make_uint2(0u, 0u);
+                if (AGG) av[k] = (live && lc.aggr_ci < 0) ? __ldcs(lc.aggr_col + i) : make_uint2(0u, 0u);
+            }
+            #pragma unroll
+            for (int j = 0; j < 2 * NV; ++j) {
+                const int k = j >> 1;
+                const bool hi = (j & 1) != 0;
+                uint32_t v[NCOL > 0 ? NCOL : 1];
+                #pragma unroll
+                for (int c = 0; c < NCOL; ++c) v[c] = hi ? cv[c][k].y : cv[c][k].x;
+                const float x = hi ? p[k].z : p[k].x;
+                const float y = hi ? p[k].w : p[k].y;
+                float val = 0.f;
+                if (AGG) {
+                    uint32_t raw = hi ? av[k].y : av[k].x;
+                    #pragma unroll
+                    for (int cc = 0; cc < NCOL; ++cc)
+                        if (cc == lc.aggr_ci) raw = v[cc];
+                    val = agg_value(lc.aggr_typ, raw);
+                }
+                uint32_t lab = 0;
+                const int kind = hyb_pass<NCOL>(lc, v) ? hyb_classify(a, sc, x, y, lab) : 0;
+                if (kind == 1) hist.add((int)lab, val);
+                // border points: one queue reservation per warp
+                const unsigned m = __ballot_sync(0xffffffffu, kind == 2);
+                if (m) {
+                    int at = 0;
+                    if (lane == 0) at = atomicAdd(qn, __popc(m));
+                    at = __shfl_sync(0xffffffffu, at, 0);
+                    if (kind == 2) {
+                        const int s = at + __popc(m & ((1u << lane) - 1u));
+                        qx[s] = x;
+                        qy[s] = y;
+                        qv[s] = val;
+                    }
+                }
+            }
+        }
+        // drain full blocks of queued points, one point per thread
+        __syncthreads();
+        while (*qn >= BLOCK) {
+            const int s = *qn - BLOCK + (int)threadIdx.x;
+            exact_probe(a.ix, qx[s], qy[s], qv[s], hist);
+            __syncthreads();
+            if (threadIdx.x == 0) *qn -= BLOCK;
+            __syncthreads();
+        }
+    }
+    // the last point of an odd-sized table
+    if ((a.n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        const uint64_t i = a.n - 1;
+        const float2 q = __ldg(reinterpret_cast<const float2*>(a.xy) + i);
+        uint32_t v[NCOL > 0 ? NCOL : 1];
+        #pragma unroll
+        for (int c = 0; c < NCOL; ++c) v[c] = __ldg(reinterpret_cast<const uint32_t*>(lc.col[c]) + i);
+        float val = 0.f;
+        if (AGG) {
+            uint32_t raw = lc.aggr_ci < 0 ? __ldg(reinterpret_cast<const uint32_t*>(lc.aggr_col) + i) : 0u;
+            #pragma unroll
+            for (int cc = 0; cc < NCOL; ++cc)
+                if (cc == lc.aggr_ci) raw = v[cc];
+            val = agg_value(lc.aggr_typ, raw);
+        }
+        uint32_t lab = 0;
+        const int kind = hyb_pass<NCOL>(lc, v) ? hyb_classify(a, sc, q.x, q.y, lab) : 0;
+        if (kind == 1) hist.add((int)lab, val);
+        if (kind == 2) exact_probe(a.ix, q.x, q.y, val, hist);
+    }
+    __syncthreads();
+    {
+        const int cnt = *qn;
+        if ((int)threadIdx.x < cnt) exact_probe(a.ix, qx[threadIdx.x], qy[threadIdx.x], qv[threadIdx.x], hist);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < a.P; b += BLOCK) {
+        uint32_t cnt = 0;
+        unsigned long long sum = 0;
+        #pragma unroll 1
+        for (int w = 0; w < lc.copies; ++w) {
+            const uint32_t* h = s_hist + w * HW * a.P;
+            cnt += h[b];
+            if (AGG) sum += ((unsigned long long)h[2 * a.P + b] << 32) + h[a.P + b];
+        }
+        if (cnt) {
+            atomicAdd(a.out_count + b, (unsigned long long)cnt);
+            if (AGG) atomicAdd(lc.out_sum + b, sum);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+namespace {
+
+using HybKernel = void (*)(HybLeanArgs, LeanCols);
+
+struct HybShape {
+    int block;
+    int nv;
+};
+constexpr HybShape kHybShapes[] = {{512, 2}, {1024, 2}, {256, 4}};
+constexpr int kNumHybShapes = (int)(sizeof(kHybShapes) / sizeof(kHybShapes[0]));
+
+template <int NCOL, bool AGG>
+HybKernel pick_hyb(int shape) {
+    switch (shape) {
+        case 0: return k_hybrid_lean<512, 2, NCOL, AGG>;
+        case 1: return k_hybrid_lean<1024, 2, NCOL, AGG>;
+        default: return k_hybrid_lean<256, 4, NCOL, AGG>;
+    }
+}
+
+template <bool AGG>
+HybKernel pick_hyb_ncol(int ncol, int shape) {
+    switch (ncol) {
+        case 0: return pick_hyb<0, AGG>(shape);
+        case 1: return pick_hyb<1, AGG>(shape);
+        case 2: return pick_hyb<2, AGG>(shape);
+        case 3: return pick_hyb<3, AGG>(shape);
+        case 4: return pick_hyb<4, AGG>(shape);
+        default: return nullptr;
+    }
+}
+
+int g_hyb_optin = -1;
+
+int hyb_copies(int shape, int P, bool agg) {
+    const int warps = kHybShapes[shape].block / 32;
+    int copies = 1;
+    const size_t per = (size_t)P * (agg ? 3 : 1) * 4;
+    while (copies * 2 <= warps && per * copies * 2 <= 48 * 1024) copies *= 2;
+    return copies;
+}
+
+}  // namespace
+
+int hybrid_lean_shapes() { return kNumHybShapes; }
+
+size_t hybrid_lean_smem(int shape, int code_words, int P, bool agg) {
+    if (shape < 0 || shape >= kNumHybShapes) return 0;
+    const HybShape& s = kHybShapes[shape];
+    const size_t qcap = (size_t)s.block * (1 + 2 * s.nv);
+    return (size_t)code_words * 4 + (size_t)hyb_copies(shape, P, agg) * P * (agg ? 3 : 1) * 4 + qcap * 12 + 16;
+}
+
+bool launch_hybrid_lean(int shape, const HybLeanArgs& a, const LeanCols& lc_in, int sms, cudaStream_t st) {
+    if (shape < 0 || shape >= kNumHybShapes || lc_in.ncol < 0 || lc_in.ncol > 4) return false;
+    const bool agg = lc_in.aggr != 0;
+    HybKernel k = agg ? pick_hyb_ncol<true>(lc_in.ncol, shape) : pick_hyb_ncol<false>(lc_in.ncol, shape);
+    if (!k) return false;
+    if (g_hyb_optin < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_hyb_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    }
+    LeanCols lc = lc_in;
+    lc.copies = hyb_copies(shape, a.P, agg);
+    const size_t smem = hybrid_lean_smem(shape, a.code_words, a.P, agg);
+    if (smem > (size_t)g_hyb_optin) return false;
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    const int block = kHybShapes[shape].block;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, block, smem) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        return false;
+    }
+    const uint64_t per_iter = (uint64_t)block * kHybShapes[shape].nv;
+    const uint64_t need = ((a.n >> 1) + per_iter - 1) / per_iter;
+    uint64_t blocks = std::min<uint64_t>((uint64_t)sms * per_sm, std::max<uint64_t>(need, 1));
+    while (blocks < (uint64_t)sms * per_sm && a.n / blocks >= (1ull << 31)) ++blocks;
+    if (a.n / blocks >= (1ull << 31)) return false;
+    k<<<(unsigned)blocks, block, smem, st>>>(a, lc);
+    ++g_kernel_launches;
+    return true;
+}
+
+}  // namespace rj

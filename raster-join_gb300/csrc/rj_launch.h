@@ -144,9 +144,13 @@ struct PointArgs {
     uint64_t row0;
     float4 qbox;
     int shape = -1;              // kernel shape (-1: the default for the mapper)
+    uint32_t wait_limit = kWaitLimit;   // tries of a bounded pipeline wait before it gives up
 };
 constexpr int kZoneShift = 10;               // zones of 1024 rows
 void launch_zone_boxes(const float2* xy, uint64_t n, float4* zones, int sms, cudaStream_t st);
+// one CTA waits, bounded by `limit` tries, on an mbarrier nothing arrives on;
+// sets bit 0 of *err when the wait runs out
+void launch_wait_selftest(int* err, uint32_t limit, cudaStream_t st);
 
 // Exact point-in-polygon index (CSR over a uniform grid).
 struct IndexArgs {
@@ -205,8 +209,46 @@ struct LabelCountArgs {
     uint64_t zrow0;
     float4 qbox;
 };
+// Filters (interval form, <= 4 columns) and the summed aggregate of the lean
+// label pass with attributes (rj_lean_kernels.cu).
+struct LeanCols {
+    int ncol;
+    const uint2* col[4];         // filter columns, read as value pairs (8-byte aligned)
+    uint32_t lo[4], span[4];     // the predicates of column c hold iff key - lo <= span
+    uint32_t fm[4], xm[4];       // order key = v ^ ((sign(v) & fm) ^ xm)
+    int aggr;                    // 1: sum the aggregate
+    int aggr_ci;                 // the aggregate is filter column aggr_ci, or -1
+    const uint2* aggr_col;       // else this column
+    int aggr_typ;
+    float scale;                 // fixed-point scale 2^(s-32)
+    double* nonfinite;           // fp64 sums of non-finite values
+    unsigned long long* out_sum; // int64 fixed-point sums
+    int copies;                  // histogram copies (set by the launcher)
+};
 void launch_block_codes(const uint16_t* label, int resx, int resy, int bs, int nbx, int nby, uint16_t* codes,
                         int sms, cudaStream_t st);
+// Lean point pass of the hybrid join over its label map (rj_hybrid_lean.cu).
+struct HybLeanArgs {
+    const float4* xy;            // location column as point pairs, 16-byte aligned
+    uint64_t n;
+    HybXf h;                     // hybrid canvas (rasterize, hybrid.glsl:187-200)
+    const uint16_t* label;       // [resy][resx] label, kBorderLabel near outlines, kEmptyLabel
+    const uint16_t* codes;       // block codes of the label map
+    int bs, nbx, code_words;
+    int P;
+    unsigned long long* out_count;
+    const float4* zones;         // zone map or null
+    uint64_t zrow0;
+    float4 qbox;
+    ExactIndex ix;               // classified grid of the exact tests
+};
+int hybrid_lean_shapes();
+size_t hybrid_lean_smem(int shape, int code_words, int P, bool agg);
+bool launch_hybrid_lean(int shape, const HybLeanArgs& a, const LeanCols& lc, int sms, cudaStream_t st);
+int label_lean_shapes();
+int label_lean_max_cols();
+size_t label_lean_smem(int shape, int code_words, int P, bool agg);
+bool launch_label_lean(int shape, const LabelCountArgs& a, const LeanCols& lc, int sms, cudaStream_t st);
 int label_count_shapes();
 size_t label_count_smem(int shape, int code_words, int P);
 bool launch_label_count(int shape, const LabelCountArgs& a, int sms, cudaStream_t st);

@@ -275,7 +275,7 @@ k_points_pipe(PointArgs pa, M mp, int stages) {
             for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
                 const int s = (int)(it % stages);
                 const uint32_t k = it / stages;
-                if (it >= (uint32_t)stages && !mbar_wait(empty + s, (k - 1) & 1u)) atomicOr(pa.err, 1);
+                if (it >= (uint32_t)stages && !mbar_wait_n(empty + s, (k - 1) & 1u, pa.wait_limit)) atomicOr(pa.err, 1);
                 unsigned char* st = stage0 + (size_t)s * stage_bytes;
                 const uint64_t base = tile * kPipeTile;
                 mbar_arrive_expect_tx(full + s, stage_bytes);
@@ -285,7 +285,8 @@ k_points_pipe(PointArgs pa, M mp, int stages) {
                 if (AGG && f.aggr_ci < 0)
                     bulk_g2s(st + kPipeTile * 8 + f.ncol * col_bytes, f.aggr_col + base, col_bytes, full + s, pol);
             }
-            // no copy may still be landing when the block exits
+            // no copy may still be landing when the block exits: this wait keeps
+            // the fixed, generous limit whatever the phase-wait limit is
             const uint32_t first = it > (uint32_t)stages ? it - stages : 0u;
             for (uint32_t j = first; j < it; ++j)
                 if (!mbar_wait(full + (j % stages), (j / stages) & 1u)) atomicOr(pa.err, 1);
@@ -298,7 +299,7 @@ k_points_pipe(PointArgs pa, M mp, int stages) {
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
         const int s = (int)(it % stages);
         const uint32_t k = it / stages;
-        const bool ok = mbar_wait(full + s, k & 1u);
+        const bool ok = mbar_wait_n(full + s, k & 1u, pa.wait_limit);
         if (!ok && lane == 0) atomicOr(pa.err, 1);
         const unsigned char* st = stage0 + (size_t)s * stage_bytes;
         float x[4], y[4], val[4] = {0.f, 0.f, 0.f, 0.f};

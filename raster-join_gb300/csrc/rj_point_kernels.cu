@@ -72,6 +72,26 @@ void launch_col_absmax(const uint32_t* col, int typ, uint64_t n, unsigned* out_b
     ++g_kernel_launches;
 }
 
+// The bounded wait of the bulk-copy pipeline on its own: an mbarrier that
+// nothing arrives on, so the wait can only run out.  Host-side failure
+// handling (RJ_E_TIMEOUT, a context that stays usable) is tested with it
+// without copies in flight.
+__global__ void k_wait_selftest(int* err, uint32_t limit) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !mbar_wait_n(&bar, 0u, limit)) atomicOr(err, 1);
+    __syncthreads();
+}
+
+void launch_wait_selftest(int* err, uint32_t limit, cudaStream_t st) {
+    k_wait_selftest<<<1, 32, 0, st>>>(err, limit);
+    ++g_kernel_launches;
+}
+
 void launch_raster_label(const PointArgs& pa, const CanvasXf& cx, const uint16_t* label, int sms,
                          cudaStream_t st) {
     LabelMapper m{cx, label};

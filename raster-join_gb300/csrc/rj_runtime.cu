@@ -561,6 +561,7 @@ PointArgs make_point_args(rj_ctx* ctx, const DevFilter& f, unsigned long long* o
     pa.out_nonfinite = (double*)ctx->scratch["out_nonfinite"].p;
     pa.err = ctx->d_err;
     pa.shape = ctx->point_shape;
+    pa.wait_limit = ctx->wait_limit;
     // the zone check costs a dependent load per iteration: skip it when the
     // query's reach holds every finite location of the table (nothing to skip)
     const float4 tb = ctx->table_box, qb = ctx->qbox;
@@ -817,21 +818,86 @@ int label_map(rj_ctx* ctx, PolyPassArgs& a, const char* key, size_t npix, const 
     return RJ_OK;
 }
 
-// Lean count pass over a label map (rj_count_kernels.cu): one canvas tile,
-// no filter, count only, a resident table.  Builds the block-code map(s) of
-// the label map and runs the count kernel; the shape and block size are the
+// Filters and aggregate of a query in the lean passes' form (interval
+// predicates on value pairs); false when a column is not 8-byte aligned.
+bool lean_cols_of(const PointArgs& pa, unsigned long long* out_sum, LeanCols& lc) {
+    lc = LeanCols{};
+    lc.ncol = pa.f.ncol;
+    for (int c = 0; c < lc.ncol; ++c) {
+        if (((uintptr_t)pa.f.col[c] & 7) != 0) return false;
+        lc.col[c] = reinterpret_cast<const uint2*>(pa.f.col[c]);
+        lc.lo[c] = pa.f.lo[c];
+        lc.span[c] = pa.f.span[c];
+        const int t = pa.f.ctyp[c];
+        lc.fm[c] = (t == RJ_FLOAT) ? 0x7FFFFFFFu : 0u;
+        lc.xm[c] = (t == RJ_FLOAT || t == RJ_INT) ? 0x80000000u : 0u;
+    }
+    lc.aggr = pa.f.aggr ? 1 : 0;
+    if (lc.aggr) {
+        lc.aggr_ci = pa.f.aggr_ci;
+        if (lc.aggr_ci < 0) {
+            if (((uintptr_t)pa.f.aggr_col & 7) != 0) return false;
+            lc.aggr_col = reinterpret_cast<const uint2*>(pa.f.aggr_col);
+        }
+        lc.aggr_typ = pa.f.aggr_typ;
+        lc.scale = pa.f.sum_scale;
+        lc.nonfinite = pa.out_nonfinite;
+        lc.out_sum = out_sum;
+    }
+    return true;
+}
+
+// The autotuner of the lean passes: the candidate kept for `key` on this
+// context, else each candidate timed once by `timed(i)` (CUDA events on the
+// context's stream; returns false when it cannot run), the fastest kept.
+// Returns the index, or -1 when none ran.
+template <class Timed>
+int tune_pick(rj_ctx* ctx, const std::string& key, size_t ncand, Timed&& timed) {
+    if (ncand == 1) return 0;
+    auto it = ctx->tuned.find(key);
+    if (it != ctx->tuned.end()) return std::min<int>(it->second, (int)ncand - 1);
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return -1;
+    float best = 1e30f;
+    int besti = -1;
+    for (size_t i = 0; i < ncand; ++i) {
+        cudaEventRecord(e0, ctx->stream);
+        if (!timed(i)) continue;
+        cudaEventRecord(e1, ctx->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            besti = (int)i;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (besti >= 0) ctx->tuned[key] = besti;
+    return besti;
+}
+
+// Lean label pass (rj_count_kernels.cu for a plain count, rj_lean_kernels.cu
+// with interval-form filters on up to four columns and / or a summed
+// aggregate): one canvas tile, a resident table.  Builds the block-code
+// map(s) of the label map and runs the pass; the shape and block size are the
 // ones forced with rj_set_tuning, else autotuned: on the first query of its
-// class (polygons, canvas, table size) on this context every candidate is
-// timed once on the table itself, into a scratch output, and the fastest is
-// kept.  *done = false: the pass does not apply (the caller takes the
-// generic label pass).
+// class (form, polygons, canvas, table size) on this context every candidate
+// is timed once on the table itself, into scratch outputs, and the fastest is
+// kept.  *done = false: the pass does not apply (the caller takes the generic
+// label pass).
 int label_count_pass(rj_ctx* ctx, const DevFilter& f, const RasterPlan& rp, const uint16_t* label, ExecState& es,
                      bool* done) {
     *done = false;
     ctx->last_count_shape = ctx->last_count_bshift = -1;
-    if (f.ncol != 0 || f.aggr || rp.splitx != 1 || rp.splity != 1 || ctx->streamed) return RJ_OK;
-    PointArgs pa = make_point_args(ctx, f, es.out_count, nullptr);
+    if (rp.splitx != 1 || rp.splity != 1 || ctx->streamed) return RJ_OK;
+    if (f.general || f.ncol > label_lean_max_cols()) return RJ_OK;
+    const bool plain = f.ncol == 0 && !f.aggr;
+    PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
     if (((uintptr_t)pa.xy & 15) != 0) return RJ_OK;
+    LeanCols lc{};
+    if (!plain && !lean_cols_of(pa, es.out_sum, lc)) return RJ_OK;
     const int P = ctx->ps->P;
     LabelCountArgs a{};
     a.xy = reinterpret_cast<const float4*>(pa.xy);
@@ -846,23 +912,45 @@ int label_count_pass(rj_ctx* ctx, const DevFilter& f, const RasterPlan& rp, cons
     a.zones = pa.zones;
     a.zrow0 = pa.row0;
     a.qbox = pa.qbox;
-    // candidate block sizes: the smallest whose code map leaves room in
-    // shared memory for the histogram, and the next one
-    int bs0 = 4;
     auto code_words = [&](int bs) {
         const long long nbx = ((long long)rp.resx + (1 << bs) - 1) >> bs, nby = ((long long)rp.resy + (1 << bs) - 1) >> bs;
         return (nbx * nby + 1) / 2;
     };
-    while (bs0 < 8 && code_words(bs0) * 4 + (long long)P * 4 > 160 * 1024) ++bs0;
+    // candidate block sizes: the smallest whose code map leaves room in
+    // shared memory for the histograms, and the next one
+    int bs0 = 4;
+    while (bs0 < 8 && code_words(bs0) * 4 + (long long)P * 12 > 160 * 1024) ++bs0;
     std::vector<int> bss;
     if (ctx->count_bshift >= 4 && ctx->count_bshift <= 8) bss.push_back(ctx->count_bshift);
     else {
         bss.push_back(bs0);
         if (bs0 < 8) bss.push_back(bs0 + 1);
     }
+    const int nshapes = plain ? label_count_shapes() : label_lean_shapes();
+    auto smem_of = [&](int sh, int bs) {
+        return plain ? label_count_smem(sh, (int)code_words(bs), P)
+                     : label_lean_smem(sh, (int)code_words(bs), P, lc.aggr != 0);
+    };
+    std::vector<std::pair<int, int>> cands;   // (shape, bs)
+    for (int bs : bss)
+        for (int sh = 0; sh < nshapes; ++sh)
+            if (ctx->count_shape < 0 || ctx->count_shape == sh)
+                if (smem_of(sh, bs) > 0 && smem_of(sh, bs) <= 200 * 1024) cands.push_back({sh, bs});
+    if (cands.empty()) return RJ_OK;
     int rc;
+    char tkey[200];
+    std::snprintf(tkey, sizeof tkey, "lean:%d:%d:%d:%d:%d:%dx%d:%d:%d:%d", plain ? 0 : 1, lc.ncol, lc.aggr, lc.aggr_ci, P,
+                  rp.resx, rp.resy, (int)std::log2((double)std::max<uint64_t>(a.n, 1)), ctx->count_shape,
+                  ctx->count_bshift);
+    auto tuned = ctx->tuned.find(tkey);
+    const bool known = cands.size() == 1 || tuned != ctx->tuned.end();
+    std::pair<int, int> pick = cands[0];
+    if (cands.size() > 1 && tuned != ctx->tuned.end())
+        pick = cands[std::min<size_t>((size_t)tuned->second, cands.size() - 1)];
+    // code maps: the chosen block size only, or every candidate's for the tuner
     std::map<int, uint16_t*> codes;
     for (int bs : bss) {
+        if (known && bs != pick.second) continue;
         const int nbx = (rp.resx + (1 << bs) - 1) >> bs, nby = (rp.resy + (1 << bs) - 1) >> bs;
         uint16_t* c;
         char key[32];
@@ -880,61 +968,160 @@ int label_count_pass(rj_ctx* ctx, const DevFilter& f, const RasterPlan& rp, cons
         b.code_words = (int)code_words(bs);
         return b;
     };
-    const int nshapes = label_count_shapes();
-    std::vector<std::pair<int, int>> cands;   // (shape, bs)
-    for (int bs : bss)
-        for (int sh = 0; sh < nshapes; ++sh)
-            if (ctx->count_shape < 0 || ctx->count_shape == sh)
-                if (label_count_smem(sh, (int)code_words(bs), P) <= 200 * 1024) cands.push_back({sh, bs});
-    if (cands.empty()) return RJ_OK;
-    std::pair<int, int> pick = cands[0];
-    if (cands.size() > 1) {
-        char key[160];
-        std::snprintf(key, sizeof key, "count:%d:%dx%d:%d:%d:%d", P, rp.resx, rp.resy,
-                      (int)std::log2((double)std::max<uint64_t>(a.n, 1)), ctx->count_shape, ctx->count_bshift);
-        auto it = ctx->tuned.find(key);
-        if (it != ctx->tuned.end()) {
-            pick = cands[std::min<size_t>((size_t)it->second, cands.size() - 1)];
-        } else {
-            // time each candidate once on (a prefix of) the table, into a scratch output
-            unsigned long long* tout;
-            if ((rc = scratch_t(ctx, "tune_count", (size_t)P, &tout))) return rc;
-            const uint64_t tn = std::min<uint64_t>(a.n & ~1ULL, 1ULL << 28);
-            cudaEvent_t e0, e1;
-            RJ_CUDA(cudaEventCreate(&e0));
-            RJ_CUDA(cudaEventCreate(&e1));
-            float best = 1e30f;
-            int besti = -1;
-            for (size_t i = 0; i < cands.size(); ++i) {
-                LabelCountArgs b = args_for(cands[i].second);
-                b.out_count = tout;
-                // first launch of a shape loads it: a tiny warm-up launch
-                LabelCountArgs w = b;
-                w.n = std::min<uint64_t>(b.n & ~1ULL, 1ULL << 16);
-                if (!launch_label_count(cands[i].first, w, ctx->sms, ctx->stream)) continue;
-                b.n = tn;
-                RJ_CUDA(cudaEventRecord(e0, ctx->stream));
-                launch_label_count(cands[i].first, b, ctx->sms, ctx->stream);
-                RJ_CUDA(cudaEventRecord(e1, ctx->stream));
-                RJ_CUDA(cudaEventSynchronize(e1));
-                float ms = 0.f;
-                RJ_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                if (ms < best) {
-                    best = ms;
-                    besti = (int)i;
-                }
+    auto launch = [&](int sh, const LabelCountArgs& b, const LeanCols& l) {
+        return plain ? launch_label_count(sh, b, ctx->sms, ctx->stream)
+                     : launch_label_lean(sh, b, l, ctx->sms, ctx->stream);
+    };
+    if (!known) {
+        // time each candidate once on (a prefix of) the table, into scratch outputs
+        unsigned long long *tout, *tsum;
+        double* tnf;
+        if ((rc = scratch_t(ctx, "tune_count", (size_t)P, &tout))) return rc;
+        if ((rc = scratch_t(ctx, "tune_sum", (size_t)P, &tsum))) return rc;
+        if ((rc = scratch_t(ctx, "tune_nonfinite", (size_t)P, &tnf))) return rc;
+        LeanCols tl = lc;
+        tl.out_sum = tsum;
+        tl.nonfinite = tnf;
+        const uint64_t tn = std::min<uint64_t>(a.n & ~1ULL, 1ULL << 28);
+        cudaEvent_t e0, e1;
+        RJ_CUDA(cudaEventCreate(&e0));
+        RJ_CUDA(cudaEventCreate(&e1));
+        float best = 1e30f;
+        int besti = -1;
+        for (size_t i = 0; i < cands.size(); ++i) {
+            LabelCountArgs b = args_for(cands[i].second);
+            b.out_count = tout;
+            // first launch of a shape loads it: a tiny warm-up launch
+            LabelCountArgs w = b;
+            w.n = std::min<uint64_t>(b.n & ~1ULL, 1ULL << 16);
+            if (!launch(cands[i].first, w, tl)) continue;
+            b.n = tn;
+            RJ_CUDA(cudaEventRecord(e0, ctx->stream));
+            launch(cands[i].first, b, tl);
+            RJ_CUDA(cudaEventRecord(e1, ctx->stream));
+            RJ_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            RJ_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                besti = (int)i;
             }
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            RJ_CUDA(cudaGetLastError());
-            if (besti < 0) return RJ_OK;
-            ctx->tuned[key] = besti;
-            pick = cands[(size_t)besti];
         }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        RJ_CUDA(cudaGetLastError());
+        if (besti < 0) return RJ_OK;
+        ctx->tuned[tkey] = besti;
+        pick = cands[(size_t)besti];
     }
     ctx->passes = 1;
     ctx->copy_ms = 0;
-    if (!launch_label_count(pick.first, args_for(pick.second), ctx->sms, ctx->stream)) return RJ_OK;
+    if (!launch(pick.first, args_for(pick.second), lc)) return RJ_OK;
+    RJ_CUDA(cudaGetLastError());
+    ctx->last_count_shape = pick.first;
+    ctx->last_count_bshift = pick.second;
+    *done = true;
+    return RJ_OK;
+}
+
+// Lean point pass of the hybrid join over its label map (rj_hybrid_lean.cu):
+// a resident table, interval-form filters on at most four columns, count or
+// sum.  Shapes and block sizes as for the lean raster pass (forced with
+// rj_set_tuning, else autotuned per query class).  *done = false: the pass
+// does not apply (the caller takes the generic hybrid pass).
+int hybrid_lean_pass(rj_ctx* ctx, const DevFilter& f, const HybXf& h, const uint16_t* label, const ExactIndex& ix,
+                     ExecState& es, bool* done) {
+    *done = false;
+    ctx->last_count_shape = ctx->last_count_bshift = -1;
+    if (ctx->streamed || f.general || f.ncol > label_lean_max_cols()) return RJ_OK;
+    PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
+    if (((uintptr_t)pa.xy & 15) != 0) return RJ_OK;
+    LeanCols lc;
+    if (!lean_cols_of(pa, es.out_sum, lc)) return RJ_OK;
+    const int P = ctx->ps->P;
+    HybLeanArgs a{};
+    a.xy = reinterpret_cast<const float4*>(pa.xy);
+    a.n = pa.n;
+    a.h = h;
+    a.label = label;
+    a.P = P;
+    a.out_count = es.out_count;
+    a.zones = pa.zones;
+    a.zrow0 = pa.row0;
+    a.qbox = pa.qbox;
+    a.ix = ix;
+    auto code_words = [&](int bs) {
+        const long long nbx = ((long long)h.resx + (1 << bs) - 1) >> bs, nby = ((long long)h.resy + (1 << bs) - 1) >> bs;
+        return (nbx * nby + 1) / 2;
+    };
+    int bs0 = 4;
+    while (bs0 < 8 && code_words(bs0) * 4 > 64 * 1024) ++bs0;
+    std::vector<int> bss;
+    if (ctx->count_bshift >= 4 && ctx->count_bshift <= 8) bss.push_back(ctx->count_bshift);
+    else {
+        bss.push_back(bs0);
+        if (bs0 < 8) bss.push_back(bs0 + 1);
+    }
+    std::vector<std::pair<int, int>> cands;
+    for (int bs : bss)
+        for (int sh = 0; sh < hybrid_lean_shapes(); ++sh)
+            if (ctx->count_shape < 0 || ctx->count_shape == sh) {
+                const size_t sm = hybrid_lean_smem(sh, (int)code_words(bs), P, lc.aggr != 0);
+                if (sm > 0 && sm <= 200 * 1024) cands.push_back({sh, bs});
+            }
+    if (cands.empty()) return RJ_OK;
+    char key[200];
+    std::snprintf(key, sizeof key, "hyb:%d:%d:%d:%d:%dx%d:%d:%d:%d", lc.ncol, lc.aggr, lc.aggr_ci, P, h.resx, h.resy,
+                  (int)std::log2((double)std::max<uint64_t>(a.n, 1)), ctx->count_shape, ctx->count_bshift);
+    auto tuned = ctx->tuned.find(key);
+    const bool known = cands.size() == 1 || tuned != ctx->tuned.end();
+    int rc;
+    std::map<int, uint16_t*> codes;
+    for (int bs : bss) {
+        if (known && bs != cands[tuned != ctx->tuned.end() ? std::min<size_t>(tuned->second, cands.size() - 1) : 0].second)
+            continue;
+        const int nbx = (h.resx + (1 << bs) - 1) >> bs, nby = (h.resy + (1 << bs) - 1) >> bs;
+        uint16_t* c;
+        char ck[32];
+        std::snprintf(ck, sizeof ck, "hyb_codes%d", bs);
+        if ((rc = scratch_t(ctx, ck, (size_t)code_words(bs) * 2, &c))) return rc;
+        launch_block_codes(label, h.resx, h.resy, bs, nbx, nby, c, ctx->sms, ctx->stream);
+        codes[bs] = c;
+    }
+    es.ph->mark(2);   // the code maps belong to the polygon side
+    auto args_for = [&](int bs) {
+        HybLeanArgs b = a;
+        b.bs = bs;
+        b.nbx = (h.resx + (1 << bs) - 1) >> bs;
+        b.codes = codes[bs];
+        b.code_words = (int)code_words(bs);
+        return b;
+    };
+    unsigned long long *tout = nullptr, *tsum = nullptr;
+    double* tnf = nullptr;
+    if (!known) {
+        if ((rc = scratch_t(ctx, "tune_count", (size_t)P, &tout))) return rc;
+        if ((rc = scratch_t(ctx, "tune_sum", (size_t)P, &tsum))) return rc;
+        if ((rc = scratch_t(ctx, "tune_nonfinite", (size_t)P, &tnf))) return rc;
+    }
+    LeanCols tl = lc;
+    tl.out_sum = tsum;
+    tl.nonfinite = tnf;
+    const int pi = tune_pick(ctx, key, cands.size(), [&](size_t i) {
+        HybLeanArgs b = args_for(cands[i].second);
+        b.out_count = tout;
+        HybLeanArgs w = b;
+        w.n = std::min<uint64_t>(b.n & ~1ULL, 1ULL << 16);   // first launch of a shape loads it
+        if (!launch_hybrid_lean(cands[i].first, w, tl, ctx->sms, ctx->stream)) return false;
+        b.n = std::min<uint64_t>(a.n & ~1ULL, 1ULL << 27);
+        return launch_hybrid_lean(cands[i].first, b, tl, ctx->sms, ctx->stream);
+    });
+    RJ_CUDA(cudaGetLastError());
+    if (pi < 0) return RJ_OK;
+    const std::pair<int, int> pick = cands[(size_t)pi];
+    ctx->passes = 1;
+    ctx->copy_ms = 0;
+    if (!launch_hybrid_lean(pick.first, args_for(pick.second), lc, ctx->sms, ctx->stream)) return RJ_OK;
     RJ_CUDA(cudaGetLastError());
     ctx->last_count_shape = pick.first;
     ctx->last_count_bshift = pick.second;
@@ -1162,9 +1349,11 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     }
     es.ph->mark(2);
     if (use_label) {
-        if ((rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
-                 launch_hybrid_points(pa, ix, ha, ctx->sms, ctx->stream);
-             })))
+        bool lean = false;
+        if ((rc = hybrid_lean_pass(ctx, f, h, ha.label, ix, es, &lean))) return rc;
+        if (!lean && (rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
+                          launch_hybrid_points(pa, ix, ha, ctx->sms, ctx->stream);
+                      })))
             return rc;
         RJ_CUDA(cudaGetLastError());
         es.ph->mark(3);
@@ -1791,6 +1980,22 @@ int rj_column_absmax(const rj_ctx* ctx, int32_t attrib_id, double* out) {
     return RJ_OK;
 }
 
+int rj_selftest_bounded_wait(rj_ctx* ctx, uint32_t limit) {
+    if (!ctx) return RJ_E_INVALID;
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    ctx->err.clear();
+    if (limit < 1) return fail(ctx, RJ_E_INVALID, "limit must be at least 1");
+    cudaSetDevice(ctx->device);
+    int derr = 0;
+    RJ_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    launch_wait_selftest(ctx->d_err, limit, ctx->stream);
+    RJ_CUDA(cudaGetLastError());
+    RJ_CUDA(cudaMemcpyAsync(&derr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (derr) return fail(ctx, RJ_E_TIMEOUT, "a bounded device wait ran out after %u tries (status 0x%x)", limit, derr);
+    return RJ_OK;
+}
+
 int rj_set_tuning(rj_ctx* ctx, int32_t knob, int32_t value) {
     if (!ctx) return RJ_E_INVALID;
     std::lock_guard<std::recursive_mutex> lock(ctx->mu);
@@ -1809,6 +2014,10 @@ int rj_set_tuning(rj_ctx* ctx, int32_t knob, int32_t value) {
             if (value != -1 && (value < 4 || value > 8))
                 return fail(ctx, RJ_E_INVALID, "count block shift %d: -1 or 4..8", value);
             ctx->count_bshift = value;
+            return RJ_OK;
+        case RJ_TUNE_WAIT_LIMIT:
+            if (value < 1) return fail(ctx, RJ_E_INVALID, "wait limit %d: at least 1", value);
+            ctx->wait_limit = (uint32_t)value;
             return RJ_OK;
         case RJ_TUNE_HYBRID_EXACT_SCALE:
             if (value != 1 && value != 2 && value != 4)
@@ -1829,6 +2038,8 @@ int rj_get_tuning(const rj_ctx* ctx, int32_t knob, int32_t* value) {
         case RJ_TUNE_COUNT_BLOCK_SHIFT: *value = ctx->last_count_bshift; return RJ_OK;
         case RJ_TUNE_HYBRID_EXACT_SCALE: *value = ctx->hybrid_exact_scale; return RJ_OK;
         case RJ_TUNE_COUNT_SHAPES: *value = label_count_shapes(); return RJ_OK;
+        case RJ_TUNE_LEAN_SHAPES: *value = label_lean_shapes(); return RJ_OK;
+        case RJ_TUNE_WAIT_LIMIT: *value = (int32_t)std::min<uint32_t>(ctx->wait_limit, 0x7FFFFFFFu); return RJ_OK;
         default: return RJ_E_INVALID;
     }
 }

@@ -35,7 +35,8 @@ STATUS = {0: "RJ_OK", -1: "RJ_E_INVALID", -2: "RJ_E_OOM", -3: "RJ_E_TOO_MANY_CON
 RJ_PENDING = 1
 SUM_SHIFT_AUTO = -2147483648
 # rj_set_tuning knobs (include/rj.h)
-TUNE_POINT_SHAPE, TUNE_COUNT_SHAPE, TUNE_COUNT_BLOCK_SHIFT, TUNE_HYBRID_EXACT_SCALE, TUNE_COUNT_SHAPES = 0, 1, 2, 3, 4
+TUNE_POINT_SHAPE, TUNE_COUNT_SHAPE, TUNE_COUNT_BLOCK_SHIFT, TUNE_HYBRID_EXACT_SCALE = 0, 1, 2, 3
+TUNE_COUNT_SHAPES, TUNE_LEAN_SHAPES, TUNE_WAIT_LIMIT = 4, 5, 6
 BATCH_AUTOTUNE = 0x1
 BATCH_NO_FUSE = 0x2
 MAX_CONSTRAINTS = 10
@@ -156,6 +157,7 @@ def load_library(path=LIB_PATH):
         "rj_poll": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int32, P(RequestInfo)]),
         "rj_server_destroy": (None, [C.c_void_p]),
         "rj_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+        "rj_selftest_bounded_wait": (C.c_int, [C.c_void_p, C.c_uint32]),
         "rj_get_sum_partials": (C.c_int, [C.c_void_p, P(C.c_int64), P(C.c_double), P(C.c_int32)]),
         "rj_set_sum_shift": (C.c_int, [C.c_void_p, C.c_int32]),
         "rj_sum_shift_for": (C.c_int32, [C.c_double, C.c_uint64]),

@@ -1,7 +1,8 @@
-"""Lean raster count pass (one canvas tile, polygon label map, no filter,
-count only): every kernel shape and every block-code size gives the oracle's
-counts bit for bit, on tables with odd sizes and with points outside the
-canvas (NaN, infinities, far away, on the canvas edges)."""
+"""Lean raster label passes (one canvas tile, polygon label map): the plain
+count and the forms with filters and avg.  Every kernel shape and every
+block-code size gives the oracle's counts bit for bit (sums within 1e-6), on
+tables with odd sizes and with points outside the canvas (NaN, infinities,
+far away, on the canvas edges)."""
 import numpy as np
 import pytest
 
@@ -79,8 +80,79 @@ def test_small_and_ragged_tables(handler, voronoi, n):
     np.testing.assert_array_equal(got.count, want)
 
 
+def _columns_table(n, seed):
+    """Config-2 columns; the aggregate column carries a few non-finite values."""
+    pts = synth.points(n, seed=seed, columns=True)
+    a = pts["a"].copy()
+    rng = np.random.default_rng(seed)
+    a[rng.choice(n, 4, replace=False)] = np.inf
+    a[rng.choice(n, 2, replace=False)] = -np.inf
+    a[rng.choice(n, 2, replace=False)] = np.nan
+    pts["a"] = a
+    return pts
+
+
+FORMS = {
+    # name: (constraints, time range, aggregate attribute or None)
+    "time_count": ([], True, None),
+    "time_avg": ([], True, 3),
+    "config2": ([(4, rj.GT, 2), (5, rj.LT, 8), (3, rj.LT, 50.0)], True, 3),
+    "int_uint_float": ([(4, rj.GTE, 3), (5, rj.LTE, 6), (2, rj.GT, synth.T0 + 1000), (3, rj.GTE, 5.0)], False, 5),
+    "avg_no_filter": ([], False, 3),
+}
+
+
+@pytest.mark.parametrize("form", sorted(FORMS))
+def test_filtered_forms_every_shape_match_oracle(handler, voronoi, form):
+    """Filters on 1-4 columns (uint, int, float), with and without avg, the
+    aggregate inside or apart from the filter columns: every shape and block
+    size against the oracle (counts exact, sums within 1e-6)."""
+    verts, pidx = voronoi
+    cons, trange, aggr = FORMS[form]
+    pts = _columns_table(300_001, 17)
+    dh = rj.DataHandler()
+    dh.add_column(1, rj.Location, pts["xy"])
+    dh.add_column(2, rj.Uint, pts["t"])
+    dh.add_column(3, rj.Float, pts["a"])
+    dh.add_column(4, rj.Int, pts["f1"])
+    dh.add_column(5, rj.Int, pts["f2"])
+    dh.setPolygons(verts, pidx)
+    dh.setQueryConstraints(cons)
+    tr = (2, synth.T0, synth.T0 + synth.YEAR // 2) if trange else None
+    if tr:
+        dh.setTimeRange(*tr)
+    dh.setAggregation(rj.Avg if aggr else rj.Count, aggr if aggr else -1)
+    handler.setDataHandler(dh)
+    handler.setCellSize(10.0)
+    cols = oracle.Columns({2: (oracle.Uint, pts["t"]), 3: (oracle.Float, pts["a"]),
+                           4: (oracle.Int, pts["f1"]), 5: (oracle.Int, pts["f2"])})
+    f = cols.filt(cons, aggr_attrib=aggr, time_range=tr)
+    want_c, want_s, _ = oracle.raster_join(pts["xy"], verts, pidx, 10.0, f=f)
+    nshapes = handler.getTuning(rj.TUNE_LEAN_SHAPES)
+    taken = 0
+    try:
+        for bs in (4, 5):
+            handler.setTuning(rj.TUNE_COUNT_BLOCK_SHIFT, bs)
+            for sh in range(nshapes):
+                handler.setTuning(rj.TUNE_COUNT_SHAPE, sh)
+                got = handler.execute(rj.RasterJoinFn)
+                np.testing.assert_array_equal(got.count, want_c, err_msg="shape %d, block shift %d" % (sh, bs))
+                if aggr:
+                    np.testing.assert_allclose(got.sum, want_s, rtol=1e-6, atol=1e-6)
+                taken += handler.getTuning(rj.TUNE_COUNT_SHAPE) == sh
+    finally:
+        handler.setTuning(rj.TUNE_COUNT_SHAPE, -1)
+        handler.setTuning(rj.TUNE_COUNT_BLOCK_SHIFT, -1)
+    assert taken == 2 * nshapes
+    got = handler.execute(rj.RasterJoinFn)              # autotuned
+    np.testing.assert_array_equal(got.count, want_c)
+    if aggr:
+        np.testing.assert_allclose(got.sum, want_s, rtol=1e-6, atol=1e-6)
+
+
 def test_lean_pass_is_taken_only_where_it_applies(handler, voronoi):
-    """Filters, avg and multi-tile canvases keep the generic pass (and its results)."""
+    """Float-equality compat predicates (general form) and multi-tile canvases
+    keep the generic pass (and its results); interval filters take the lean one."""
     verts, pidx = voronoi
     pts = synth.points(200_001, seed=3, columns=True)
     dh = rj.DataHandler()
@@ -91,10 +163,18 @@ def test_lean_pass_is_taken_only_where_it_applies(handler, voronoi):
     handler.setCellSize(10.0)
     handler.execute(rj.RasterJoinFn)
     assert handler.getTuning(rj.TUNE_COUNT_SHAPE) >= 0
-    dh.setQueryConstraints([(4, rj.GT, 2)])
+    dh.setQueryConstraints([(4, rj.GTE, 2)])
+    f = oracle.Columns({4: (oracle.Int, pts["f1"])}).filt([(4, rj.GTE, 2)])
     got = handler.execute(rj.RasterJoinFn)
-    assert handler.getTuning(rj.TUNE_COUNT_SHAPE) == -1
-    f = oracle.Columns({4: (oracle.Int, pts["f1"])}).filt([(4, rj.GT, 2)])
+    assert handler.getTuning(rj.TUNE_COUNT_SHAPE) >= 0
+    np.testing.assert_array_equal(got.count, oracle.raster_join(pts["xy"], verts, pidx, 10.0, f=f)[0])
+    handler.flags = rj.FLAG_COMPAT_FLOAT_EQ
+    try:
+        got = handler.execute(rj.RasterJoinFn)
+        assert handler.getTuning(rj.TUNE_COUNT_SHAPE) == -1
+    finally:
+        handler.flags = 0
+    f = oracle.Columns({4: (oracle.Int, pts["f1"])}).filt([(4, rj.GTE, 2)], compat_float_eq=True)
     np.testing.assert_array_equal(got.count, oracle.raster_join(pts["xy"], verts, pidx, 10.0, f=f)[0])
     dh.setQueryConstraints([])
     handler.max_fbo_size = 2048         # 4000 px across: 2 x 2 tiles of 2000 px
@@ -104,3 +184,50 @@ def test_lean_pass_is_taken_only_where_it_applies(handler, voronoi):
     finally:
         handler.max_fbo_size = 8192
     np.testing.assert_array_equal(got.count, oracle.raster_join(pts["xy"], verts, pidx, 10.0, max_res=2048)[0])
+
+
+@pytest.mark.parametrize("form", ["time_count", "config2", "avg_no_filter"])
+def test_hybrid_lean_every_shape_matches_oracle(handler, voronoi, form):
+    """The hybrid join's lean pass (label map + border queue + exact tests):
+    every shape and block size against the oracle's exact join (counts
+    exact, sums within 1e-6), with points on and off the canvas."""
+    verts, pidx = voronoi
+    cons, trange, aggr = FORMS[form]
+    pts = _columns_table(300_001, 23)
+    xy = _table(300_001, 23)
+    dh = rj.DataHandler()
+    dh.add_column(1, rj.Location, xy)
+    dh.add_column(2, rj.Uint, pts["t"])
+    dh.add_column(3, rj.Float, pts["a"])
+    dh.add_column(4, rj.Int, pts["f1"])
+    dh.add_column(5, rj.Int, pts["f2"])
+    dh.setPolygons(verts, pidx)
+    dh.setQueryConstraints(cons)
+    tr = (2, synth.T0, synth.T0 + synth.YEAR // 2) if trange else None
+    if tr:
+        dh.setTimeRange(*tr)
+    dh.setAggregation(rj.Avg if aggr else rj.Count, aggr if aggr else -1)
+    handler.setDataHandler(dh)
+    handler.setPolyIndexResolution(256)
+    cols = oracle.Columns({2: (oracle.Uint, pts["t"]), 3: (oracle.Float, pts["a"]),
+                           4: (oracle.Int, pts["f1"]), 5: (oracle.Int, pts["f2"])})
+    f = cols.filt(cons, aggr_attrib=aggr, time_range=tr)
+    want_c, want_s = oracle.hybrid_join(xy, verts, pidx, 256, f=f)
+    taken = 0
+    try:
+        for bs in (4, 5):
+            handler.setTuning(rj.TUNE_COUNT_BLOCK_SHIFT, bs)
+            for sh in range(3):
+                handler.setTuning(rj.TUNE_COUNT_SHAPE, sh)
+                got = handler.execute(rj.HybridJoinFn)
+                np.testing.assert_array_equal(got.count, want_c, err_msg="shape %d, block shift %d" % (sh, bs))
+                if aggr:
+                    np.testing.assert_allclose(got.sum, want_s, rtol=1e-6, atol=1e-6)
+                taken += handler.getTuning(rj.TUNE_COUNT_SHAPE) == sh
+    finally:
+        handler.setTuning(rj.TUNE_COUNT_SHAPE, -1)
+        handler.setTuning(rj.TUNE_COUNT_BLOCK_SHIFT, -1)
+    assert taken == 6
+    got = handler.execute(rj.HybridJoinFn)
+    np.testing.assert_array_equal(got.count, want_c)
+    assert handler.getTuning(rj.TUNE_COUNT_SHAPE) >= 0
