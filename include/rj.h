@@ -279,11 +279,12 @@ RJ_API int rj_column_absmax(const rj_ctx *ctx, int32_t attrib_id, double *out);
  *                            with filters (interval form, <= 4 columns) or
  *                            a summed aggregate; RJ_TUNE_COUNT_SHAPE indexes
  *                            the shapes of the form the query takes
- *   RJ_TUNE_WAIT_LIMIT       tries of a bounded device wait of the bulk-copy
- *                            pipeline (RJ_TUNE_POINT_SHAPE 2) before it gives
- *                            up and the call returns RJ_E_TIMEOUT (default
- *                            4194304; the wait for copies still in flight at
- *                            the end of a block keeps that default)
+ *   RJ_TUNE_WAIT_LIMIT       microseconds a bounded device wait of the
+ *                            bulk-copy pipeline (RJ_TUNE_POINT_SHAPE 2) may
+ *                            take before it gives up and the call returns
+ *                            RJ_E_TIMEOUT (default 1000000, one second; the
+ *                            wait for copies still in flight at the end of a
+ *                            block keeps that default)
  * rj_get_tuning on RJ_TUNE_COUNT_SHAPE / _BLOCK_SHIFT reports the values the
  * last count pass ran with (-1 when the last query did not take it). */
 #define RJ_TUNE_POINT_SHAPE        0
@@ -298,13 +299,13 @@ RJ_API int rj_get_tuning(const rj_ctx *ctx, int32_t knob, int32_t *value);
 
 /* ---- failure handling ------------------------------------------------------
  * Runs the library's bounded device wait alone: one block waits, at most
- * `limit` tries, on a barrier that nothing completes, so the wait runs out
+ * limit_us microseconds, on a barrier that nothing completes, so the wait runs out
  * and the call returns RJ_E_TIMEOUT the way a join does when a bounded wait
  * of its pipeline runs out (the kernel returns; the context stays usable).
  * RJ_OK would mean the wait did not run out.  The reference has no
  * counterpart: it had no device-side waits and exit(0)ed on errors
  * (GLData.cpp:18-23, GLFunction.cpp:251-252). */
-RJ_API int rj_selftest_bounded_wait(rj_ctx *ctx, uint32_t limit);
+RJ_API int rj_selftest_bounded_wait(rj_ctx *ctx, uint32_t limit_us);
 
 /* ---- polygon sets --------------------------------------------------------
  * A polygon collection held on the device independently of the context's own

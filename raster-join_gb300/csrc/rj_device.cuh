@@ -264,7 +264,9 @@ struct HybXf {
 __device__ __forceinline__ bool hyb_rasterize(const HybXf& h, float x, float y, int& px, int& py) {
     float u = __fdiv_rn(__fsub_rn(x, h.ox), h.dx);
     float v = __fdiv_rn(__fsub_rn(y, h.oy), h.dy);
-    if (u < -1.0f || u >= 1.0f || v < -1.0f || v >= 1.0f) return false;
+    // outside [-1,1) -- and NaN, which lies in no polygon (the exact test's
+    // grid cell rejects it)
+    if (!(u >= -1.0f && u < 1.0f && v >= -1.0f && v < 1.0f)) return false;
     u = __fmul_rn(__fadd_rn(u, 1.0f), 0.5f);
     v = __fmul_rn(__fadd_rn(v, 1.0f), 0.5f);
     px = __float2int_rz(__fmul_rn(u, (float)h.resx));
@@ -327,27 +329,38 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+// One try on the phase of the given parity; a thread whose phase is not
+// complete may be suspended up to about hint_ns before the try returns false.
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity, uint32_t hint_ns) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
         : "memory");
     return ok != 0;
 }
-// Wait for the phase of the given parity to complete; false after the
-// iteration limit (the caller records an error and stops).
-constexpr uint32_t kWaitLimit = 1u << 22;
-__device__ __forceinline__ bool mbar_wait_n(uint64_t* bar, uint32_t parity, uint32_t limit) {
-    for (uint32_t i = 0; i < limit; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Wait for the phase of the given parity to complete, bounded in wall time:
+// false once limit_ns nanoseconds have passed (the caller records an error
+// and stops).  The bound is time, not tries: a try may suspend the thread.
+constexpr uint64_t kWaitLimitNs = 1000000000ull;   // 1 s
+__device__ __forceinline__ bool mbar_wait_ns(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+    if (mbar_try_wait(bar, parity, 1000u)) return true;
+    const uint64_t t0 = global_ns();
+    do {
+        if (mbar_try_wait(bar, parity, 2000u)) return true;
+    } while (global_ns() - t0 < limit_ns);
     return false;
 }
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    return mbar_wait_n(bar, parity, kWaitLimit);
+    return mbar_wait_ns(bar, parity, kWaitLimitNs);
 }
 __device__ __forceinline__ uint64_t l2_evict_first_policy() {
     uint64_t pol;

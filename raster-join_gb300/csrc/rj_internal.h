@@ -140,7 +140,7 @@ struct rj_ctx {
     int point_shape = -1;
     int count_shape = -1, count_bshift = -1;
     int hybrid_exact_scale = 1;
-    uint32_t wait_limit = rj::kWaitLimit;
+    uint64_t wait_ns = rj::kWaitLimitNs;   // bound of the pipeline's device waits
     int last_count_shape = -1, last_count_bshift = -1;
     std::map<std::string, int> tuned;   // autotuned choice per query class
     // exact partial sums of the last query (rj_get_sum_partials)

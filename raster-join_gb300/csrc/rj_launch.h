@@ -144,13 +144,13 @@ struct PointArgs {
     uint64_t row0;
     float4 qbox;
     int shape = -1;              // kernel shape (-1: the default for the mapper)
-    uint32_t wait_limit = kWaitLimit;   // tries of a bounded pipeline wait before it gives up
+    uint64_t wait_ns = kWaitLimitNs;    // wall time a bounded pipeline wait may take before it gives up
 };
 constexpr int kZoneShift = 10;               // zones of 1024 rows
 void launch_zone_boxes(const float2* xy, uint64_t n, float4* zones, int sms, cudaStream_t st);
-// one CTA waits, bounded by `limit` tries, on an mbarrier nothing arrives on;
-// sets bit 0 of *err when the wait runs out
-void launch_wait_selftest(int* err, uint32_t limit, cudaStream_t st);
+// one CTA waits, bounded by limit_ns of wall time, on an mbarrier nothing
+// arrives on; sets bit 0 of *err when the wait runs out
+void launch_wait_selftest(int* err, uint64_t limit_ns, cudaStream_t st);
 
 // Exact point-in-polygon index (CSR over a uniform grid).
 struct IndexArgs {

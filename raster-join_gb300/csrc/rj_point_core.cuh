@@ -275,7 +275,7 @@ k_points_pipe(PointArgs pa, M mp, int stages) {
             for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
                 const int s = (int)(it % stages);
                 const uint32_t k = it / stages;
-                if (it >= (uint32_t)stages && !mbar_wait_n(empty + s, (k - 1) & 1u, pa.wait_limit)) atomicOr(pa.err, 1);
+                if (it >= (uint32_t)stages && !mbar_wait_ns(empty + s, (k - 1) & 1u, pa.wait_ns)) atomicOr(pa.err, 1);
                 unsigned char* st = stage0 + (size_t)s * stage_bytes;
                 const uint64_t base = tile * kPipeTile;
                 mbar_arrive_expect_tx(full + s, stage_bytes);
@@ -299,7 +299,7 @@ k_points_pipe(PointArgs pa, M mp, int stages) {
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
         const int s = (int)(it % stages);
         const uint32_t k = it / stages;
-        const bool ok = mbar_wait_n(full + s, k & 1u, pa.wait_limit);
+        const bool ok = mbar_wait_ns(full + s, k & 1u, pa.wait_ns);
         if (!ok && lane == 0) atomicOr(pa.err, 1);
         const unsigned char* st = stage0 + (size_t)s * stage_bytes;
         float x[4], y[4], val[4] = {0.f, 0.f, 0.f, 0.f};
@@ -338,10 +338,13 @@ k_points_pipe(PointArgs pa, M mp, int stages) {
             }
         }
     }
-    // tail points (n not a multiple of the tile) with plain loads
+    // tail points (n not a multiple of the tile) with plain loads.  The trip
+    // count is uniform per warp (lanes past the end take an empty mask): the
+    // mappers' warp votes need every lane of the warp.
     if (blockIdx.x == 0) {
         const uint64_t t0 = ntiles * kPipeTile;
-        for (uint64_t base = t0 + (uint64_t)tid * 4; base < pa.n; base += (uint64_t)kPipeConsumers * 4) {
+        for (uint64_t wbase = t0 + (uint64_t)(tid - lane) * 4; wbase < pa.n; wbase += (uint64_t)kPipeConsumers * 4) {
+            const uint64_t base = wbase + (uint64_t)lane * 4;
             float x[4], y[4], val[4] = {0.f, 0.f, 0.f, 0.f};
             uint32_t mask = 0u;
             #pragma unroll

@@ -76,19 +76,19 @@ void launch_col_absmax(const uint32_t* col, int typ, uint64_t n, unsigned* out_b
 // nothing arrives on, so the wait can only run out.  Host-side failure
 // handling (RJ_E_TIMEOUT, a context that stays usable) is tested with it
 // without copies in flight.
-__global__ void k_wait_selftest(int* err, uint32_t limit) {
+__global__ void k_wait_selftest(int* err, uint64_t limit_ns) {
     __shared__ __align__(8) uint64_t bar;
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
         mbar_fence_init();
     }
     __syncthreads();
-    if (threadIdx.x == 0 && !mbar_wait_n(&bar, 0u, limit)) atomicOr(err, 1);
+    if (threadIdx.x == 0 && !mbar_wait_ns(&bar, 0u, limit_ns)) atomicOr(err, 1);
     __syncthreads();
 }
 
-void launch_wait_selftest(int* err, uint32_t limit, cudaStream_t st) {
-    k_wait_selftest<<<1, 32, 0, st>>>(err, limit);
+void launch_wait_selftest(int* err, uint64_t limit_ns, cudaStream_t st) {
+    k_wait_selftest<<<1, 32, 0, st>>>(err, limit_ns);
     ++g_kernel_launches;
 }
 

@@ -561,7 +561,7 @@ PointArgs make_point_args(rj_ctx* ctx, const DevFilter& f, unsigned long long* o
     pa.out_nonfinite = (double*)ctx->scratch["out_nonfinite"].p;
     pa.err = ctx->d_err;
     pa.shape = ctx->point_shape;
-    pa.wait_limit = ctx->wait_limit;
+    pa.wait_ns = ctx->wait_ns;
     // the zone check costs a dependent load per iteration: skip it when the
     // query's reach holds every finite location of the table (nothing to skip)
     const float4 tb = ctx->table_box, qb = ctx->qbox;
@@ -818,6 +818,13 @@ int label_map(rj_ctx* ctx, PolyPassArgs& a, const char* key, size_t npix, const 
     return RJ_OK;
 }
 
+// The lean passes' autotuner keys a choice by query class: the form, and
+// the polygon count, canvas size and table size in octave buckets.  Scans
+// below kTuneMinPoints take the default shape without timing anything.
+constexpr uint64_t kTuneMinPoints = 1ull << 22;
+constexpr int kCountDefaultShape = 5;     // 1024 threads, 4 pairs, block codes, per-warp histograms
+inline int tune_bucket(double v) { return (int)std::floor(std::log2(std::max(v, 1.0))); }
+
 // Filters and aggregate of a query in the lean passes' form (interval
 // predicates on value pairs); false when a column is not 8-byte aligned.
 bool lean_cols_of(const PointArgs& pa, unsigned long long* out_sum, LeanCols& lc) {
@@ -939,14 +946,19 @@ int label_count_pass(rj_ctx* ctx, const DevFilter& f, const RasterPlan& rp, cons
     if (cands.empty()) return RJ_OK;
     int rc;
     char tkey[200];
-    std::snprintf(tkey, sizeof tkey, "lean:%d:%d:%d:%d:%d:%dx%d:%d:%d:%d", plain ? 0 : 1, lc.ncol, lc.aggr, lc.aggr_ci, P,
-                  rp.resx, rp.resy, (int)std::log2((double)std::max<uint64_t>(a.n, 1)), ctx->count_shape,
-                  ctx->count_bshift);
+    std::snprintf(tkey, sizeof tkey, "lean:%d:%d:%d:%d:%d:%d:%d:%d:%d", plain ? 0 : 1, lc.ncol, lc.aggr, lc.aggr_ci >= 0,
+                  tune_bucket((double)P), tune_bucket((double)rp.resx * rp.resy), tune_bucket((double)a.n),
+                  ctx->count_shape, ctx->count_bshift);
     auto tuned = ctx->tuned.find(tkey);
-    const bool known = cands.size() == 1 || tuned != ctx->tuned.end();
+    // small scans are not worth timing candidates for: the default shape
+    const bool small = a.n < kTuneMinPoints;
+    const bool known = cands.size() == 1 || tuned != ctx->tuned.end() || small;
     std::pair<int, int> pick = cands[0];
     if (cands.size() > 1 && tuned != ctx->tuned.end())
         pick = cands[std::min<size_t>((size_t)tuned->second, cands.size() - 1)];
+    else if (small)
+        for (const auto& c : cands)
+            if (c.first == (plain ? kCountDefaultShape : 0) && c.second == bss.back()) pick = c;
     // code maps: the chosen block size only, or every candidate's for the tuner
     std::map<int, uint16_t*> codes;
     for (int bs : bss) {
@@ -1071,15 +1083,16 @@ int hybrid_lean_pass(rj_ctx* ctx, const DevFilter& f, const HybXf& h, const uint
             }
     if (cands.empty()) return RJ_OK;
     char key[200];
-    std::snprintf(key, sizeof key, "hyb:%d:%d:%d:%d:%dx%d:%d:%d:%d", lc.ncol, lc.aggr, lc.aggr_ci, P, h.resx, h.resy,
-                  (int)std::log2((double)std::max<uint64_t>(a.n, 1)), ctx->count_shape, ctx->count_bshift);
+    std::snprintf(key, sizeof key, "hyb:%d:%d:%d:%d:%d:%d:%d:%d", lc.ncol, lc.aggr, lc.aggr_ci >= 0, tune_bucket((double)P),
+                  tune_bucket((double)h.resx * h.resy), tune_bucket((double)a.n), ctx->count_shape, ctx->count_bshift);
     auto tuned = ctx->tuned.find(key);
-    const bool known = cands.size() == 1 || tuned != ctx->tuned.end();
+    const bool small = a.n < kTuneMinPoints;
+    const bool known = cands.size() == 1 || tuned != ctx->tuned.end() || small;
     int rc;
     std::map<int, uint16_t*> codes;
     for (int bs : bss) {
         if (known && bs != cands[tuned != ctx->tuned.end() ? std::min<size_t>(tuned->second, cands.size() - 1) : 0].second)
-            continue;
+            continue;   // (a small scan takes the first candidate)
         const int nbx = (h.resx + (1 << bs) - 1) >> bs, nby = (h.resy + (1 << bs) - 1) >> bs;
         uint16_t* c;
         char ck[32];
@@ -1107,7 +1120,7 @@ int hybrid_lean_pass(rj_ctx* ctx, const DevFilter& f, const HybXf& h, const uint
     LeanCols tl = lc;
     tl.out_sum = tsum;
     tl.nonfinite = tnf;
-    const int pi = tune_pick(ctx, key, cands.size(), [&](size_t i) {
+    const int pi = small && tuned == ctx->tuned.end() ? 0 : tune_pick(ctx, key, cands.size(), [&](size_t i) {
         HybLeanArgs b = args_for(cands[i].second);
         b.out_count = tout;
         HybLeanArgs w = b;
@@ -1980,19 +1993,19 @@ int rj_column_absmax(const rj_ctx* ctx, int32_t attrib_id, double* out) {
     return RJ_OK;
 }
 
-int rj_selftest_bounded_wait(rj_ctx* ctx, uint32_t limit) {
+int rj_selftest_bounded_wait(rj_ctx* ctx, uint32_t limit_us) {
     if (!ctx) return RJ_E_INVALID;
     std::lock_guard<std::recursive_mutex> lock(ctx->mu);
     ctx->err.clear();
-    if (limit < 1) return fail(ctx, RJ_E_INVALID, "limit must be at least 1");
+    if (limit_us < 1) return fail(ctx, RJ_E_INVALID, "limit must be at least 1 us");
     cudaSetDevice(ctx->device);
     int derr = 0;
     RJ_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
-    launch_wait_selftest(ctx->d_err, limit, ctx->stream);
+    launch_wait_selftest(ctx->d_err, (uint64_t)limit_us * 1000ull, ctx->stream);
     RJ_CUDA(cudaGetLastError());
     RJ_CUDA(cudaMemcpyAsync(&derr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     RJ_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (derr) return fail(ctx, RJ_E_TIMEOUT, "a bounded device wait ran out after %u tries (status 0x%x)", limit, derr);
+    if (derr) return fail(ctx, RJ_E_TIMEOUT, "a bounded device wait ran out after %u us (status 0x%x)", limit_us, derr);
     return RJ_OK;
 }
 
@@ -2016,8 +2029,8 @@ int rj_set_tuning(rj_ctx* ctx, int32_t knob, int32_t value) {
             ctx->count_bshift = value;
             return RJ_OK;
         case RJ_TUNE_WAIT_LIMIT:
-            if (value < 1) return fail(ctx, RJ_E_INVALID, "wait limit %d: at least 1", value);
-            ctx->wait_limit = (uint32_t)value;
+            if (value < 1) return fail(ctx, RJ_E_INVALID, "wait limit %d us: at least 1", value);
+            ctx->wait_ns = (uint64_t)value * 1000ull;
             return RJ_OK;
         case RJ_TUNE_HYBRID_EXACT_SCALE:
             if (value != 1 && value != 2 && value != 4)
@@ -2039,7 +2052,7 @@ int rj_get_tuning(const rj_ctx* ctx, int32_t knob, int32_t* value) {
         case RJ_TUNE_HYBRID_EXACT_SCALE: *value = ctx->hybrid_exact_scale; return RJ_OK;
         case RJ_TUNE_COUNT_SHAPES: *value = label_count_shapes(); return RJ_OK;
         case RJ_TUNE_LEAN_SHAPES: *value = label_lean_shapes(); return RJ_OK;
-        case RJ_TUNE_WAIT_LIMIT: *value = (int32_t)std::min<uint32_t>(ctx->wait_limit, 0x7FFFFFFFu); return RJ_OK;
+        case RJ_TUNE_WAIT_LIMIT: *value = (int32_t)std::min<uint64_t>(ctx->wait_ns / 1000ull, 0x7FFFFFFFull); return RJ_OK;
         default: return RJ_E_INVALID;
     }
 }
