@@ -142,7 +142,6 @@ struct rj_ctx {
     int hybrid_exact_scale = 1;
     uint64_t wait_ns = rj::kWaitLimitNs;   // bound of the pipeline's device waits
     int last_count_shape = -1, last_count_bshift = -1;
-    std::map<std::string, int> tuned;   // autotuned choice per query class
     // exact partial sums of the last query (rj_get_sum_partials)
     int forced_shift = RJ_SUM_SHIFT_AUTO;
     std::vector<long long> last_fixed;

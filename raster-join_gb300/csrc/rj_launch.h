@@ -241,7 +241,16 @@ struct HybLeanArgs {
     uint64_t zrow0;
     float4 qbox;
     ExactIndex ix;               // classified grid of the exact tests
+    // mode 0: the hybrid canvas; the pixel of a point comes from one FMA per
+    // axis, fast = (Ax, Bx, Ay, By) with pixel coordinate = v * A + B, inside
+    // the canvas less a 2-pixel rim (near the rim: the exact rasterize)
+    // mode 1: the classified grid's cells (index join); label holds per cell
+    // the one polygon a FULL cell lies in, kBorderLabel for cells with a
+    // candidate list, kEmptyLabel for empty cells
+    int mode;
+    float4 fast;
 };
+void launch_cell_labels(const uint32_t* code, int ncells, uint16_t* label, int sms, cudaStream_t st);
 int hybrid_lean_shapes();
 size_t hybrid_lean_smem(int shape, int code_words, int P, bool agg);
 bool launch_hybrid_lean(int shape, const HybLeanArgs& a, const LeanCols& lc, int sms, cudaStream_t st);

@@ -854,15 +854,31 @@ bool lean_cols_of(const PointArgs& pa, unsigned long long* out_sum, LeanCols& lc
     return true;
 }
 
-// The autotuner of the lean passes: the candidate kept for `key` on this
-// context, else each candidate timed once by `timed(i)` (CUDA events on the
-// context's stream; returns false when it cannot run), the fastest kept.
-// Returns the index, or -1 when none ran.
+// Autotuned choices per device and query class, shared by every context of
+// the process: a choice depends on the GPU and the class, not on the context.
+std::mutex g_tune_mu;
+std::map<std::string, int> g_tuned;
+bool tuned_get(const rj_ctx* ctx, const std::string& key, int* v) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tuned.find(std::to_string(ctx->device) + "/" + key);
+    if (it == g_tuned.end()) return false;
+    *v = it->second;
+    return true;
+}
+void tuned_put(const rj_ctx* ctx, const std::string& key, int v) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tuned[std::to_string(ctx->device) + "/" + key] = v;
+}
+
+// The autotuner of the lean passes: the candidate kept for `key`, else each
+// candidate timed once by `timed(i)` (CUDA events on the context's stream;
+// returns false when it cannot run), the fastest kept.  Returns the index,
+// or -1 when none ran.
 template <class Timed>
 int tune_pick(rj_ctx* ctx, const std::string& key, size_t ncand, Timed&& timed) {
     if (ncand == 1) return 0;
-    auto it = ctx->tuned.find(key);
-    if (it != ctx->tuned.end()) return std::min<int>(it->second, (int)ncand - 1);
+    int known = 0;
+    if (tuned_get(ctx, key, &known)) return std::min<int>(known, (int)ncand - 1);
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return -1;
     float best = 1e30f;
@@ -881,7 +897,7 @@ int tune_pick(rj_ctx* ctx, const std::string& key, size_t ncand, Timed&& timed) 
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (besti >= 0) ctx->tuned[key] = besti;
+    if (besti >= 0) tuned_put(ctx, key, besti);
     return besti;
 }
 
@@ -949,13 +965,14 @@ int label_count_pass(rj_ctx* ctx, const DevFilter& f, const RasterPlan& rp, cons
     std::snprintf(tkey, sizeof tkey, "lean:%d:%d:%d:%d:%d:%d:%d:%d:%d", plain ? 0 : 1, lc.ncol, lc.aggr, lc.aggr_ci >= 0,
                   tune_bucket((double)P), tune_bucket((double)rp.resx * rp.resy), tune_bucket((double)a.n),
                   ctx->count_shape, ctx->count_bshift);
-    auto tuned = ctx->tuned.find(tkey);
+    int tuned_i = -1;
+    const bool have = tuned_get(ctx, tkey, &tuned_i);
     // small scans are not worth timing candidates for: the default shape
     const bool small = a.n < kTuneMinPoints;
-    const bool known = cands.size() == 1 || tuned != ctx->tuned.end() || small;
+    const bool known = cands.size() == 1 || have || small;
     std::pair<int, int> pick = cands[0];
-    if (cands.size() > 1 && tuned != ctx->tuned.end())
-        pick = cands[std::min<size_t>((size_t)tuned->second, cands.size() - 1)];
+    if (cands.size() > 1 && have)
+        pick = cands[std::min<size_t>((size_t)tuned_i, cands.size() - 1)];
     else if (small)
         for (const auto& c : cands)
             if (c.first == (plain ? kCountDefaultShape : 0) && c.second == bss.back()) pick = c;
@@ -1023,7 +1040,7 @@ int label_count_pass(rj_ctx* ctx, const DevFilter& f, const RasterPlan& rp, cons
         cudaEventDestroy(e1);
         RJ_CUDA(cudaGetLastError());
         if (besti < 0) return RJ_OK;
-        ctx->tuned[tkey] = besti;
+        tuned_put(ctx, tkey, besti);
         pick = cands[(size_t)besti];
     }
     ctx->passes = 1;
@@ -1041,8 +1058,10 @@ int label_count_pass(rj_ctx* ctx, const DevFilter& f, const RasterPlan& rp, cons
 // sum.  Shapes and block sizes as for the lean raster pass (forced with
 // rj_set_tuning, else autotuned per query class).  *done = false: the pass
 // does not apply (the caller takes the generic hybrid pass).
-int hybrid_lean_pass(rj_ctx* ctx, const DevFilter& f, const HybXf& h, const uint16_t* label, const ExactIndex& ix,
-                     ExecState& es, bool* done) {
+// mode 0: the hybrid canvas h with its label map; mode 1: the classified
+// grid ix with its cell labels (index join).
+int hybrid_lean_pass(rj_ctx* ctx, const DevFilter& f, int mode, const HybXf& h, const uint16_t* label,
+                     const ExactIndex& ix, ExecState& es, bool* done) {
     *done = false;
     ctx->last_count_shape = ctx->last_count_bshift = -1;
     if (ctx->streamed || f.general || f.ncol > label_lean_max_cols()) return RJ_OK;
@@ -1062,11 +1081,18 @@ int hybrid_lean_pass(rj_ctx* ctx, const DevFilter& f, const HybXf& h, const uint
     a.zrow0 = pa.row0;
     a.qbox = pa.qbox;
     a.ix = ix;
+    a.mode = mode;
+    const int resx = mode == 0 ? h.resx : ix.res, resy = mode == 0 ? h.resy : ix.res;
+    if (mode == 0) {
+        // pixel coordinate = (u + 1) / 2 * res with u = (v - o) / d
+        const double ax = (double)h.resx / (2.0 * h.dx), ay = (double)h.resy / (2.0 * h.dy);
+        a.fast = make_float4((float)ax, (float)(0.5 * h.resx - ax * h.ox), (float)ay, (float)(0.5 * h.resy - ay * h.oy));
+    }
     auto code_words = [&](int bs) {
-        const long long nbx = ((long long)h.resx + (1 << bs) - 1) >> bs, nby = ((long long)h.resy + (1 << bs) - 1) >> bs;
+        const long long nbx = ((long long)resx + (1 << bs) - 1) >> bs, nby = ((long long)resy + (1 << bs) - 1) >> bs;
         return (nbx * nby + 1) / 2;
     };
-    int bs0 = 4;
+    int bs0 = mode == 0 ? 4 : 3;
     while (bs0 < 8 && code_words(bs0) * 4 > 64 * 1024) ++bs0;
     std::vector<int> bss;
     if (ctx->count_bshift >= 4 && ctx->count_bshift <= 8) bss.push_back(ctx->count_bshift);
@@ -1083,29 +1109,31 @@ int hybrid_lean_pass(rj_ctx* ctx, const DevFilter& f, const HybXf& h, const uint
             }
     if (cands.empty()) return RJ_OK;
     char key[200];
-    std::snprintf(key, sizeof key, "hyb:%d:%d:%d:%d:%d:%d:%d:%d", lc.ncol, lc.aggr, lc.aggr_ci >= 0, tune_bucket((double)P),
-                  tune_bucket((double)h.resx * h.resy), tune_bucket((double)a.n), ctx->count_shape, ctx->count_bshift);
-    auto tuned = ctx->tuned.find(key);
+    std::snprintf(key, sizeof key, "hyb:%d:%d:%d:%d:%d:%d:%d:%d:%d", mode, lc.ncol, lc.aggr, lc.aggr_ci >= 0,
+                  tune_bucket((double)P), tune_bucket((double)resx * resy), tune_bucket((double)a.n), ctx->count_shape,
+                  ctx->count_bshift);
+    int tuned_i = -1;
+    const bool have = tuned_get(ctx, key, &tuned_i);
     const bool small = a.n < kTuneMinPoints;
-    const bool known = cands.size() == 1 || tuned != ctx->tuned.end() || small;
+    const bool known = cands.size() == 1 || have || small;
     int rc;
     std::map<int, uint16_t*> codes;
     for (int bs : bss) {
-        if (known && bs != cands[tuned != ctx->tuned.end() ? std::min<size_t>(tuned->second, cands.size() - 1) : 0].second)
+        if (known && bs != cands[have ? std::min<size_t>((size_t)tuned_i, cands.size() - 1) : 0].second)
             continue;   // (a small scan takes the first candidate)
-        const int nbx = (h.resx + (1 << bs) - 1) >> bs, nby = (h.resy + (1 << bs) - 1) >> bs;
+        const int nbx = (resx + (1 << bs) - 1) >> bs, nby = (resy + (1 << bs) - 1) >> bs;
         uint16_t* c;
         char ck[32];
-        std::snprintf(ck, sizeof ck, "hyb_codes%d", bs);
+        std::snprintf(ck, sizeof ck, "hyb_codes%d_%d", mode, bs);
         if ((rc = scratch_t(ctx, ck, (size_t)code_words(bs) * 2, &c))) return rc;
-        launch_block_codes(label, h.resx, h.resy, bs, nbx, nby, c, ctx->sms, ctx->stream);
+        launch_block_codes(label, resx, resy, bs, nbx, nby, c, ctx->sms, ctx->stream);
         codes[bs] = c;
     }
     es.ph->mark(2);   // the code maps belong to the polygon side
     auto args_for = [&](int bs) {
         HybLeanArgs b = a;
         b.bs = bs;
-        b.nbx = (h.resx + (1 << bs) - 1) >> bs;
+        b.nbx = (resx + (1 << bs) - 1) >> bs;
         b.codes = codes[bs];
         b.code_words = (int)code_words(bs);
         return b;
@@ -1120,7 +1148,7 @@ int hybrid_lean_pass(rj_ctx* ctx, const DevFilter& f, const HybXf& h, const uint
     LeanCols tl = lc;
     tl.out_sum = tsum;
     tl.nonfinite = tnf;
-    const int pi = small && tuned == ctx->tuned.end() ? 0 : tune_pick(ctx, key, cands.size(), [&](size_t i) {
+    const int pi = small && !have ? 0 : tune_pick(ctx, key, cands.size(), [&](size_t i) {
         HybLeanArgs b = args_for(cands[i].second);
         b.out_count = tout;
         HybLeanArgs w = b;
@@ -1262,9 +1290,18 @@ int exec_index(rj_ctx* ctx, const rj_query* q, ExecState& es) {
         ExactIndex ix{};
         if ((rc = build_exact(ctx, q->grid_res, ix))) return rc;
         es.ph->mark(2);
-        if ((rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
-                 launch_exact_points(pa, ix, ctx->sms, ctx->stream);
-             })))
+        // the lean pass over the grid's cell labels; else the generic pass
+        bool lean = false;
+        if (ctx->ps->P <= kMaxLabelPolys && !ctx->streamed) {
+            uint16_t* cl;
+            const int ncells = ix.res * ix.res;
+            if ((rc = scratch_t(ctx, "cls_label16", (size_t)ncells, &cl))) return rc;
+            launch_cell_labels(ix.code, ncells, cl, ctx->sms, ctx->stream);
+            if ((rc = hybrid_lean_pass(ctx, f, 1, HybXf{}, cl, ix, es, &lean))) return rc;
+        }
+        if (!lean && (rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
+                          launch_exact_points(pa, ix, ctx->sms, ctx->stream);
+                      })))
             return rc;
     }
     RJ_CUDA(cudaGetLastError());
@@ -1363,7 +1400,7 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     es.ph->mark(2);
     if (use_label) {
         bool lean = false;
-        if ((rc = hybrid_lean_pass(ctx, f, h, ha.label, ix, es, &lean))) return rc;
+        if ((rc = hybrid_lean_pass(ctx, f, 0, h, ha.label, ix, es, &lean))) return rc;
         if (!lean && (rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
                           launch_hybrid_points(pa, ix, ha, ctx->sms, ctx->stream);
                       })))

@@ -234,3 +234,50 @@ def test_hybrid_lean_every_shape_matches_oracle(handler, voronoi, form):
     got = handler.execute(rj.HybridJoinFn)
     np.testing.assert_array_equal(got.count, want_c)
     assert handler.getTuning(rj.TUNE_COUNT_SHAPE) >= 0
+
+
+@pytest.mark.parametrize("form", ["time_count", "config2"])
+def test_index_lean_every_shape_matches_oracle(handler, voronoi, form):
+    """The index join through the lean pass over the classified grid's cell
+    labels (FULL cells straight into the histogram, cells with candidate lists
+    queued for the exact test): every shape and block size against the
+    oracle's index join."""
+    verts, pidx = voronoi
+    cons, trange, aggr = FORMS[form]
+    pts = _columns_table(300_001, 29)
+    xy = _table(300_001, 29)
+    dh = rj.DataHandler()
+    dh.add_column(1, rj.Location, xy)
+    dh.add_column(2, rj.Uint, pts["t"])
+    dh.add_column(3, rj.Float, pts["a"])
+    dh.add_column(4, rj.Int, pts["f1"])
+    dh.add_column(5, rj.Int, pts["f2"])
+    dh.setPolygons(verts, pidx)
+    dh.setQueryConstraints(cons)
+    tr = (2, synth.T0, synth.T0 + synth.YEAR // 2) if trange else None
+    if tr:
+        dh.setTimeRange(*tr)
+    dh.setAggregation(rj.Avg if aggr else rj.Count, aggr if aggr else -1)
+    handler.setDataHandler(dh)
+    handler.setPolyIndexResolution(256)
+    cols = oracle.Columns({2: (oracle.Uint, pts["t"]), 3: (oracle.Float, pts["a"]),
+                           4: (oracle.Int, pts["f1"]), 5: (oracle.Int, pts["f2"])})
+    f = cols.filt(cons, aggr_attrib=aggr, time_range=tr)
+    want_c, want_s = oracle.index_join(xy, verts, pidx, 256, f=f)
+    taken = 0
+    try:
+        for bs in (4, 5):
+            handler.setTuning(rj.TUNE_COUNT_BLOCK_SHIFT, bs)
+            for sh in range(3):
+                handler.setTuning(rj.TUNE_COUNT_SHAPE, sh)
+                got = handler.execute(rj.IndexJoinFn)
+                np.testing.assert_array_equal(got.count, want_c, err_msg="shape %d, block shift %d" % (sh, bs))
+                if aggr:
+                    np.testing.assert_allclose(got.sum, want_s, rtol=1e-6, atol=1e-6)
+                taken += handler.getTuning(rj.TUNE_COUNT_SHAPE) == sh
+    finally:
+        handler.setTuning(rj.TUNE_COUNT_SHAPE, -1)
+        handler.setTuning(rj.TUNE_COUNT_BLOCK_SHIFT, -1)
+    assert taken == 6
+    got = handler.execute(rj.IndexJoinFn)
+    np.testing.assert_array_equal(got.count, want_c)
