@@ -229,9 +229,26 @@ __host__ __device__ __forceinline__ bool cross_row(int32_t ay, int32_t by, int32
 // Crossing-number point-in-polygon, index.glsl:47-67 / GridIndexF.cpp:383-402,
 // evaluated in fp32 with the reference's expression order
 // (vj.x - vi.x) * (testy - vi.y) / (vj.y - vi.y) + vi.x.
+//
+// The comparison needs the exactly rounded crossing xi only when tx lies
+// close to it.  A fast quotient (__fdividef, within 2 ulp while |den| is in
+// [2^-126, 2^126]) gives xa with |xi - xa| <= 2^-21 (|q| + |vix|); when tx is
+// farther than twice that from xa the answer is the same as the exact one,
+// else the exact division decides.  Results are identical to the always
+// exact form; most tests skip the IEEE division.
 __device__ __forceinline__ bool edge_toggles(float vix, float viy, float vjx, float vjy, float tx, float ty) {
     if ((viy > ty) != (vjy > ty)) {
-        float xi = __fadd_rn(__fdiv_rn(__fmul_rn(__fsub_rn(vjx, vix), __fsub_rn(ty, viy)), __fsub_rn(vjy, viy)), vix);
+        const float num = __fmul_rn(__fsub_rn(vjx, vix), __fsub_rn(ty, viy));
+        const float den = __fsub_rn(vjy, viy);
+        const float ad = fabsf(den);
+        if (ad > 1e-30f && ad < 1e30f) {
+            const float qa = __fdividef(num, den);
+            const float xa = qa + vix;
+            const float tol = (fabsf(qa) + fabsf(vix)) * 1e-6f;
+            if (tx < xa - tol) return true;
+            if (tx > xa + tol) return false;
+        }
+        const float xi = __fadd_rn(__fdiv_rn(num, den), vix);
         return tx < xi;
     }
     return false;
