@@ -506,6 +506,25 @@ def run_headline(args, rj, torch, local, world):
     ms_per_step = total_ms / args.steps
     value = world * n / (ms_per_step / 1e3) / 1e9
 
+    # ---- the same step replayed as a prepared query (rj_prepare: one CUDA graph) ----
+    plan = h.prepare(rj.RasterJoinFn, query=q)
+    for _ in range(3):
+        plan.execute()
+    torch.cuda.synchronize()
+    pe0, pe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nrep = max(5, args.steps // 4)
+    pe0.record(stream)
+    for _ in range(nrep):
+        rp = plan.execute()
+    pe1.record(stream)
+    torch.cuda.synchronize()
+    prep_ms = pe0.elapsed_time(pe1) / nrep
+    prepared = {"ms_per_step": prep_ms, "gpoints_s": world * n / prep_ms / 1e6,
+                "same_result": bool(np.array_equal(rp.count, res.count)),
+                "method": "rj_prepare captures the step's device work (label map, block codes, count pass, "
+                          "result copies) as a CUDA graph; rj_execute_prepared replays it"}
+    plan.close()
+
     # ---- the full result against an independent path: point canvas + polygon pass ----
     qc = rj.default_query()
     qc.function_type = rj.RasterJoinFn
@@ -639,6 +658,7 @@ def run_headline(args, rj, torch, local, world):
                    "sample": "%d points of the host generator, joined alone on the GPU, against the oracle's "
                              "raster join (bit-exact counts)" % sample},
         "sample": {"points": sample, "gpu_gpoints_s": sample / sample_ms / 1e6, "gpu_ms": sample_ms},
+        "prepared": prepared,
     }
     return line, (sxy, verts, pidx)
 
@@ -788,9 +808,12 @@ def run_config3(args):
                     r = h.execute(fn, query=q)
                     ms.append((time.perf_counter() - t0) * 1e3)
                 P = len(p) - 1
+                tm = h.timings()
                 rec = {"polygons": name, "eps_m": eps, "join": "raster" if fn == rj.RasterJoinFn else "error-bounds",
                        "ms": float(np.median(ms)), "gpoints_s": n / float(np.median(ms)) / 1e6,
-                       "total_count": int(r.count.sum())}
+                       "total_count": int(r.count.sum()),
+                       "point_pass_ms": tm["pt_render_ms"], "polygon_side_ms": tm["poly_render_ms"],
+                       "kernel_launches": tm["kernel_launches"]}
                 if fn == rj.RasterJoinBoundFn:
                     b = r.bounds.astype(np.int64)
                     rec["mean_hard_range"] = float(np.mean(b[2 * P:3 * P] + b[3 * P:]))

@@ -297,6 +297,31 @@ RJ_API int rj_column_absmax(const rj_ctx *ctx, int32_t attrib_id, double *out);
 RJ_API int rj_set_tuning(rj_ctx *ctx, int32_t knob, int32_t value);
 RJ_API int rj_get_tuning(const rj_ctx *ctx, int32_t knob, int32_t *value);
 
+/* ---- prepared queries (CUDA graphs) ----------------------------------------
+ * rj_prepare runs q once (settling the caches the query uses: polygon-side
+ * structures, the polygon set's overlap status on the canvas, autotuned
+ * shapes) and captures the device work of one more execution -- polygon side,
+ * point pass, result copies -- into a CUDA graph.  rj_execute_prepared replays
+ * it on the context's stream: the same results as rj_execute(ctx, q, res),
+ * without host planning or per-kernel launch costs.  Work that rj_execute
+ * does with NO_CACHE is redone on every replay.
+ * The plan stays valid while the table keeps its buffers (rj_load_points
+ * with the same columns and size copies into them in place), the context
+ * keeps the same polygon set and stream, the aggregate's fixed-point scale is
+ * unchanged and, for a query whose rows the time index narrowed, that index
+ * still describes the rows (a reload drops it); else rj_execute_prepared
+ * returns RJ_E_INVALID.  The
+ * zone map is not used by a plan (a reloaded table needs none).
+ * Queries whose execution reads a value back to the host before it can go
+ * on cannot be captured (tiered canvases, an index or hybrid join that
+ * rebuilds its grid each call): rj_prepare returns RJ_E_UNSUPPORTED, as it
+ * does for host-streamed tables.  No counterpart in the reference (each
+ * GLHandler::executeFunction re-issues its draws, GLHandler.cpp:188-204). */
+typedef struct rj_plan rj_plan;
+RJ_API int rj_prepare(rj_ctx *ctx, const rj_query *q, rj_plan **out);
+RJ_API int rj_execute_prepared(rj_plan *plan, rj_result *res);
+RJ_API void rj_plan_destroy(rj_plan *plan);
+
 /* ---- failure handling ------------------------------------------------------
  * Runs the library's bounded device wait alone: one block waits, at most
  * limit_us microseconds, on a barrier that nothing completes, so the wait runs out
@@ -354,6 +379,10 @@ RJ_API int rj_cluster_points(rj_ctx *ctx, int32_t time_attrib, int32_t nbuckets,
  * query succeeded, else the first failing status. */
 #define RJ_BATCH_AUTOTUNE 0x1u   /* time the point-pass block shapes on this batch and keep the fastest */
 #define RJ_BATCH_NO_FUSE  0x2u   /* run every query through rj_execute (the plain path) */
+#define RJ_BATCH_FUSE_ALL 0x4u   /* fuse every raster query, also those the lean
+                                    single-query pass runs faster (by default
+                                    label-map queries over >= 2^22 rows take
+                                    rj_execute's lean pass; `fallback` counts them) */
 typedef struct {
     int32_t nqueries, fused, fallback;
     int32_t segments;              /* row ranges covered by one set of queries */

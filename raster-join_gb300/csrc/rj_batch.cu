@@ -155,7 +155,13 @@ size_t canvas_bytes(const QPlan& p) {
 
 // Host planning of one query (under the context lock: filters and canvas
 // plans report errors through the context).
-void plan_query(rj_ctx* ctx, QPlan& p, bool no_fuse) {
+// Label-map queries over at least this many rows run faster through the lean
+// single-query pass (block codes in shared memory, plain shared atomics) than
+// in the fused pass, whose shared row reads save little: the per-(point,
+// query) work dominates, not the row read.  They leave the fused pass.
+constexpr uint64_t kLeanQueryRows = 1ull << 22;
+
+void plan_query(rj_ctx* ctx, QPlan& p, bool no_fuse, bool fuse_all) {
     const rj_query* q = p.q;
     if (no_fuse || q->function_type != RJ_RASTER_JOIN || ctx->streamed) return;   // plain path
     int rc = plan_raster_bbox(ctx, p.ps->bbox, q, p.rp);
@@ -201,6 +207,9 @@ void plan_query(rj_ctx* ctx, QPlan& p, bool no_fuse) {
     } else {
         p.mode = (label_ok && known != 1) ? BQ_LABEL : BQ_SPLAT;
         p.check_overlap = p.mode == BQ_LABEL && known != 0;
+        if (!fuse_all && p.mode == BQ_LABEL && p.T == 1 && !p.f.general && p.f.ncol <= label_lean_max_cols() &&
+            p.r1 - p.r0 >= kLeanQueryRows)
+            p.fused = false;   // rj_execute's lean pass (same results)
     }
 }
 
@@ -783,7 +792,7 @@ int execute_batch(Engine& e, int nq, const rj_query* qs, const rj_query* const* 
                 p.status = fail(ctx, RJ_E_INVALID, "query %d: result sized for %d polygons, set has %d", i, p.res->npolys, p.ps->P);
                 continue;
             }
-            plan_query(ctx, p, (flags & RJ_BATCH_NO_FUSE) != 0);
+            plan_query(ctx, p, (flags & RJ_BATCH_NO_FUSE) != 0, (flags & RJ_BATCH_FUSE_ALL) != 0);
         }
         const int zrc = ensure_zones(ctx);   // lets the point pass skip rows far from a query
         if (zrc) return zrc;
@@ -1141,6 +1150,7 @@ int rj_cluster_points(rj_ctx* ctx, int32_t attrib, int32_t nbuckets, int32_t cel
     tix.valid = tc != nullptr;
     ctx->tix = tix;
     ctx->zones_valid = false;   // rows moved
+    ++ctx->table_gen;
     return RJ_OK;
 }
 

@@ -148,6 +148,37 @@ struct rj_ctx {
     std::vector<double> last_nonfinite;
     int last_shift = 0;
     void* batch_engine = nullptr;   // executor of rj_execute_batch
+    // prepared queries (rj_prepare): the table's buffers change generation
+    // whenever they are reallocated or reordered; while a query is captured
+    // into a CUDA graph, steps that would read a value back to the host
+    // refuse (RJ_E_UNSUPPORTED) and the zone map is left out
+    uint64_t table_gen = 0;
+    uint64_t tix_gen = 0;   // bumped when the time index stops matching the rows
+    bool capturing = false;
+};
+
+// A prepared query: the device work of one rj_execute captured as a CUDA
+// graph, replayed by rj_execute_prepared.
+struct rj_plan {
+    rj_ctx* ctx = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t stream = nullptr;
+    int P = 0;
+    int function_type = 0;
+    int shift = 0;
+    int aggr_attrib = -1;
+    uint64_t table_gen = 0, ps_version = 0;
+    uint64_t tix_gen = 0;
+    bool uses_tix = false;   // the captured row window came from the time index
+    const void* ps = nullptr;
+    uint64_t npts = 0;
+    // pinned host copies of the per-polygon outputs, written by the graph
+    unsigned long long* hc = nullptr;
+    unsigned long long* hq = nullptr;
+    double* hnf = nullptr;
+    long long* hb = nullptr;
+    int* derr = nullptr;
 };
 
 struct rj_polyset {

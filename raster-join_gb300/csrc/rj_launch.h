@@ -148,6 +148,13 @@ struct PointArgs {
 };
 constexpr int kZoneShift = 10;               // zones of 1024 rows
 void launch_zone_boxes(const float2* xy, uint64_t n, float4* zones, int sms, cudaStream_t st);
+// per-tile transforms written by a kernel from its arguments (no host copy;
+// used while a query is captured into a graph)
+constexpr int kXfArgs = 16;
+struct XfArgs {
+    float4 v[kXfArgs];
+};
+void launch_write_xf(const XfArgs& a, int n, float4* dst, cudaStream_t st);
 // one CTA waits, bounded by limit_ns of wall time, on an mbarrier nothing
 // arrives on; sets bit 0 of *err when the wait runs out
 void launch_wait_selftest(int* err, uint64_t limit_ns, cudaStream_t st);

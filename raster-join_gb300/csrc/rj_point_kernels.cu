@@ -92,6 +92,15 @@ void launch_wait_selftest(int* err, uint64_t limit_ns, cudaStream_t st) {
     ++g_kernel_launches;
 }
 
+__global__ void k_write_xf(XfArgs a, int n, float4* dst) {
+    if ((int)threadIdx.x < n) dst[threadIdx.x] = a.v[threadIdx.x];
+}
+
+void launch_write_xf(const XfArgs& a, int n, float4* dst, cudaStream_t st) {
+    k_write_xf<<<1, kXfArgs, 0, st>>>(a, n, dst);
+    ++g_kernel_launches;
+}
+
 void launch_raster_label(const PointArgs& pa, const CanvasXf& cx, const uint16_t* label, int sms,
                          cudaStream_t st) {
     LabelMapper m{cx, label};

@@ -39,6 +39,14 @@ int fail(rj_ctx* c, int code, const char* fmt, ...) {
     return code;
 }
 
+// Steps that read a value back to the host before the work can go on cannot
+// be captured into a graph (rj_prepare): they refuse while capturing.
+int readback_guard(rj_ctx* ctx, const char* what) {
+    if (ctx->capturing)
+        return fail(ctx, RJ_E_UNSUPPORTED, "%s reads a value back to the host: this query cannot be prepared", what);
+    return RJ_OK;
+}
+
 int dev_alloc(rj_ctx* ctx, DevBuf& b, size_t bytes) {
     if (b.p && b.bytes >= bytes) return RJ_OK;
     if (b.p) {
@@ -95,6 +103,7 @@ const Column* find_col(const rj_ctx* ctx, int attrib) {
 }
 
 void free_points(rj_ctx* ctx) {
+    ++ctx->table_gen;
     for (Column& c : ctx->cols) {
         if (c.owned && c.d) cudaFree(c.d);
     }
@@ -310,8 +319,20 @@ int transform_vertices(rj_ctx* ctx, const std::vector<float4>& colxf, const std:
     int rc;
     if ((rc = scratch_t(ctx, "colxf", colxf.size(), &dcol))) return rc;
     if ((rc = scratch_t(ctx, "rowxf", rowxf.size(), &drow))) return rc;
-    RJ_CUDA(cudaMemcpyAsync(dcol, colxf.data(), colxf.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
-    RJ_CUDA(cudaMemcpyAsync(drow, rowxf.data(), rowxf.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+    if (ctx->capturing) {
+        // a graph must not copy from host memory that is gone when it
+        // replays: the transforms travel as kernel arguments instead
+        if (colxf.size() > (size_t)kXfArgs || rowxf.size() > (size_t)kXfArgs)
+            return fail(ctx, RJ_E_UNSUPPORTED, "more than %d canvas tiles per axis: this query cannot be prepared", kXfArgs);
+        XfArgs ca{}, ra{};
+        for (size_t i = 0; i < colxf.size(); ++i) ca.v[i] = colxf[i];
+        for (size_t i = 0; i < rowxf.size(); ++i) ra.v[i] = rowxf[i];
+        launch_write_xf(ca, (int)colxf.size(), dcol, ctx->stream);
+        launch_write_xf(ra, (int)rowxf.size(), drow, ctx->stream);
+    } else {
+        RJ_CUDA(cudaMemcpyAsync(dcol, colxf.data(), colxf.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+        RJ_CUDA(cudaMemcpyAsync(drow, rowxf.data(), rowxf.size() * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+    }
     if ((rc = scratch_t(ctx, "wv", (size_t)T * ctx->ps->V, wv))) return rc;
     *wf = nullptr;
     if (want_float && (rc = scratch_t(ctx, "wf", (size_t)T * ctx->ps->V, wf))) return rc;
@@ -349,6 +370,7 @@ int build_grid(rj_ctx* ctx, int res, int clamp, IndexArgs& ia, bool with_pair_ce
         if (!launch_exclusive_scan(cnt, cell_start, (int)ncells, tmp, ctx->stream))
             return fail(ctx, RJ_E_INVALID, "grid too large to scan");
         int total = 0;
+        if ((rc = readback_guard(ctx, "building the grid index"))) return rc;
         RJ_CUDA(cudaMemcpyAsync(&total, cell_start + ncells, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         RJ_CUDA(cudaStreamSynchronize(ctx->stream));
         if ((rc = scratch_t(ctx, "grid_entries", (size_t)std::max(total, 1), &entries))) return rc;
@@ -503,6 +525,7 @@ int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix, int max_scale = 1024)
         if (!launch_exclusive_scan(cell_kept, start2, (int)ncells, tmp, ctx->stream))
             return fail(ctx, RJ_E_INVALID, "classified grid too large");
         int totals[2] = {0, 0};
+        if ((rc = readback_guard(ctx, "building the classified grid"))) return rc;
         if (npairs2 > 0) {
             if (!launch_exclusive_scan(ecount, eoff, npairs2, tmp, ctx->stream))
                 return fail(ctx, RJ_E_UNSUPPORTED, "too many cell/polygon pairs to scan (%d)", npairs2);
@@ -566,7 +589,7 @@ PointArgs make_point_args(rj_ctx* ctx, const DevFilter& f, unsigned long long* o
     // query's reach holds every finite location of the table (nothing to skip)
     const float4 tb = ctx->table_box, qb = ctx->qbox;
     const bool covers = qb.x <= tb.x && qb.y <= tb.y && qb.z >= tb.z && qb.w >= tb.w;
-    if (ctx->zones_valid && !ctx->streamed && !covers) {
+    if (ctx->zones_valid && !ctx->streamed && !covers && !ctx->capturing) {
         pa.zones = (const float4*)ctx->zones.p;
         pa.row0 = r0;
         pa.qbox = ctx->qbox;
@@ -734,6 +757,7 @@ int exec_raster_tier(rj_ctx* ctx, const rj_query* q, const RasterPlan& rp, const
         return fail(ctx, RJ_E_INVALID, "tier scan failed");
     launch_tier_codes(tr, nblk, cnt, ctx->sms, ctx->stream);
     int nslots = 0;
+    if ((rc = readback_guard(ctx, "the tiered canvas"))) return rc;
     RJ_CUDA(cudaMemcpyAsync(&nslots, slot + nblk, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     RJ_CUDA(cudaStreamSynchronize(ctx->stream));
     const size_t spx = (size_t)std::max(nslots, 1) * 256;
@@ -807,6 +831,7 @@ int label_map(rj_ctx* ctx, PolyPassArgs& a, const char* key, size_t npix, const 
     // overlaps (every covered pixel centre counted once per polygon vs the
     // labelled pixels); the answer is kept with the set.
     if (ctx->ps->overlap_on(canvas) == -1) {
+        if ((rc = readback_guard(ctx, "the first label map of a polygon set on a canvas"))) return rc;
         unsigned long long lc[2] = {0, 0};
         RJ_CUDA(cudaMemcpyAsync(lc, cnt, sizeof lc, cudaMemcpyDeviceToHost, ctx->stream));
         RJ_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -879,6 +904,7 @@ int tune_pick(rj_ctx* ctx, const std::string& key, size_t ncand, Timed&& timed) 
     if (ncand == 1) return 0;
     int known = 0;
     if (tuned_get(ctx, key, &known)) return std::min<int>(known, (int)ncand - 1);
+    if (ctx->capturing) return -1;   // nothing is timed inside a capture
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return -1;
     float best = 1e30f;
@@ -969,7 +995,7 @@ int label_count_pass(rj_ctx* ctx, const DevFilter& f, const RasterPlan& rp, cons
     const bool have = tuned_get(ctx, tkey, &tuned_i);
     // small scans are not worth timing candidates for: the default shape
     const bool small = a.n < kTuneMinPoints;
-    const bool known = cands.size() == 1 || have || small;
+    const bool known = cands.size() == 1 || have || small || ctx->capturing;
     std::pair<int, int> pick = cands[0];
     if (cands.size() > 1 && have)
         pick = cands[std::min<size_t>((size_t)tuned_i, cands.size() - 1)];
@@ -1533,7 +1559,7 @@ int ensure_zones(rj_ctx* ctx) {
     bool owned_all = !ctx->streamed;
     for (const Column& c : ctx->cols) owned_all = owned_all && c.owned;
     if (!owned_all) ctx->zones_valid = false;
-    if (ctx->zones_valid || !owned_all || ctx->npts == 0) return RJ_OK;
+    if (ctx->zones_valid || !owned_all || ctx->npts == 0 || ctx->capturing) return RJ_OK;
     const uint64_t nz = (ctx->npts + (1ull << kZoneShift) - 1) >> kZoneShift;
     int rc;
     // zones, then the bounds of the whole table's finite locations after them
@@ -1594,6 +1620,58 @@ void decode_result(int P, const unsigned long long* hc, const unsigned long long
 }  // namespace rjh
 
 using namespace rjh;
+
+// The device work of one query, queued on the context's stream: cache
+// upkeep, the outputs zeroed, the join's kernels.  The per-polygon outputs
+// stay on the device (oc, os, onf, ob) for the caller to copy back.
+int enqueue_query(rj_ctx* ctx, const rj_query* q, Phase& ph, unsigned long long** poc, unsigned long long** pos,
+                  double** ponf, long long** pob, double* t_setup) {
+    int rc;
+    const int P = ctx->ps->P;
+    if (ctx->cache_owner != ctx->ps || ctx->cache_version != ctx->ps->version) {
+        // the scratch holds another polygon set's grid structures
+        ctx->ps->grid.valid = false;
+        ctx->ps->exact.valid = false;
+        ctx->cache_owner = ctx->ps;
+        ctx->cache_version = ctx->ps->version;
+    }
+    query_rows(ctx, q, ctx->row0, ctx->row1);
+    if ((rc = ensure_zones(ctx))) return rc;
+    if (q->flags & RJ_FLAG_NO_CACHE) {
+        ctx->ps->grid.valid = false;
+        ctx->ps->exact.valid = false;
+    }
+    g_kernel_launches = 0;
+    unsigned long long* oc;
+    unsigned long long* os;
+    double* onf;
+    long long* ob;
+    if ((rc = scratch_t(ctx, "out_count", P, &oc))) return rc;
+    if ((rc = scratch_t(ctx, "out_sum", P, &os))) return rc;
+    if ((rc = scratch_t(ctx, "out_nonfinite", P, &onf))) return rc;
+    if ((rc = scratch_t(ctx, "out_bounds", (size_t)4 * P, &ob))) return rc;
+    ph.mark(0);
+    RJ_CUDA(cudaMemsetAsync(oc, 0, P * sizeof(unsigned long long), ctx->stream));
+    RJ_CUDA(cudaMemsetAsync(os, 0, P * sizeof(unsigned long long), ctx->stream));
+    RJ_CUDA(cudaMemsetAsync(onf, 0, P * sizeof(double), ctx->stream));
+    ctx->sum_shift = 0;
+    RJ_CUDA(cudaMemsetAsync(ob, 0, (size_t)4 * P * sizeof(long long), ctx->stream));
+    RJ_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    ExecState es{oc, os, ob, &ph};
+    *t_setup = now_ms();
+    switch (q->function_type) {
+        case RJ_RASTER_JOIN: rc = exec_raster(ctx, q, es, false); break;
+        case RJ_INDEX_JOIN: rc = exec_index(ctx, q, es); break;
+        case RJ_HYBRID_JOIN: rc = exec_hybrid(ctx, q, es); break;
+        default: rc = exec_raster(ctx, q, es, true); break;
+    }
+    if (rc) return rc;
+    *poc = oc;
+    *pos = os;
+    *ponf = onf;
+    *pob = ob;
+    return RJ_OK;
+}
 
 // ===========================================================================
 // C ABI
@@ -1773,6 +1851,7 @@ static int load_points_impl(rj_ctx* ctx, const rj_column* cols, int32_t ncols, u
     std::lock_guard<std::recursive_mutex> lock(ctx->mu);
     if (ctx->server_running) return fail(ctx, RJ_E_BUSY, "a serving loop owns the context");
     cudaSetDevice(ctx->device);
+    if (ctx->tix.valid) ++ctx->tix_gen;   // row ranges of time windows change meaning
     ctx->tix.valid = false;
     ctx->zones_valid = false;
     const bool was_streamed = ctx->streamed;
@@ -1791,6 +1870,7 @@ static int load_points_impl(rj_ctx* ctx, const rj_column* cols, int32_t ncols, u
         return column_stats(ctx);
     }
     // release the previous table
+    ++ctx->table_gen;
     for (Column& c : ctx->cols) {
         if (c.owned && c.d) {
             cudaFree(c.d);
@@ -1912,52 +1992,19 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
     cudaSetDevice(ctx->device);
     int rc;
     const int P = ctx->ps->P;
-    if (ctx->cache_owner != ctx->ps || ctx->cache_version != ctx->ps->version) {
-        // the scratch holds another polygon set's grid structures
-        ctx->ps->grid.valid = false;
-        ctx->ps->exact.valid = false;
-        ctx->cache_owner = ctx->ps;
-        ctx->cache_version = ctx->ps->version;
-    }
-    query_rows(ctx, q, ctx->row0, ctx->row1);
-    if ((rc = ensure_zones(ctx))) return rc;
-    if (q->flags & RJ_FLAG_NO_CACHE) {
-        ctx->ps->grid.valid = false;
-        ctx->ps->exact.valid = false;
-    }
-    g_kernel_launches = 0;
-    unsigned long long* oc;
-    unsigned long long* os;
+    Phase ph(ctx, (q->flags & RJ_FLAG_PHASE_TIMING) != 0);
+    unsigned long long *oc, *os;
     double* onf;
     long long* ob;
-    if ((rc = scratch_t(ctx, "out_count", P, &oc))) return rc;
-    if ((rc = scratch_t(ctx, "out_sum", P, &os))) return rc;
-    if ((rc = scratch_t(ctx, "out_nonfinite", P, &onf))) return rc;
-    if ((rc = scratch_t(ctx, "out_bounds", (size_t)4 * P, &ob))) return rc;
-    Phase ph(ctx, (q->flags & RJ_FLAG_PHASE_TIMING) != 0);
-    ph.mark(0);
-    RJ_CUDA(cudaMemsetAsync(oc, 0, P * sizeof(unsigned long long), ctx->stream));
-    RJ_CUDA(cudaMemsetAsync(os, 0, P * sizeof(unsigned long long), ctx->stream));
-    RJ_CUDA(cudaMemsetAsync(onf, 0, P * sizeof(double), ctx->stream));
-    ctx->sum_shift = 0;
-    RJ_CUDA(cudaMemsetAsync(ob, 0, (size_t)4 * P * sizeof(long long), ctx->stream));
-    RJ_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
-    ExecState es{oc, os, ob, &ph};
-    const double t_setup = now_ms();
+    double t_setup = 0;
+    if ((rc = enqueue_query(ctx, q, ph, &oc, &os, &onf, &ob, &t_setup))) {
+        cudaStreamSynchronize(ctx->stream);
+        return rc;
+    }
     std::vector<unsigned long long> hc(P), hq(P);
     std::vector<double> hnf(P);
     std::vector<long long> hb;
     int derr = 0;
-    switch (q->function_type) {
-        case RJ_RASTER_JOIN: rc = exec_raster(ctx, q, es, false); break;
-        case RJ_INDEX_JOIN: rc = exec_index(ctx, q, es); break;
-        case RJ_HYBRID_JOIN: rc = exec_hybrid(ctx, q, es); break;
-        default: rc = exec_raster(ctx, q, es, true); break;
-    }
-    if (rc) {
-        cudaStreamSynchronize(ctx->stream);
-        return rc;
-    }
     RJ_CUDA(cudaMemcpyAsync(hc.data(), oc, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
     RJ_CUDA(cudaMemcpyAsync(hq.data(), os, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
     RJ_CUDA(cudaMemcpyAsync(hnf.data(), onf, P * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -2028,6 +2075,147 @@ int rj_column_absmax(const rj_ctx* ctx, int32_t attrib_id, double* out) {
     if (!c) return RJ_E_INVALID;
     *out = (double)c->absmax;
     return RJ_OK;
+}
+
+static void plan_free(rj_plan* p) {
+    if (!p) return;
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    cudaFreeHost(p->hc);
+    cudaFreeHost(p->hq);
+    cudaFreeHost(p->hnf);
+    cudaFreeHost(p->hb);
+    cudaFreeHost(p->derr);
+    delete p;
+}
+
+int rj_prepare(rj_ctx* ctx, const rj_query* q, rj_plan** out) {
+    if (!ctx || !q || !out) return RJ_E_INVALID;
+    *out = nullptr;
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    if (ctx->streamed) return fail(ctx, RJ_E_UNSUPPORTED, "a host-streamed table cannot be prepared");
+    if (ctx->server_running) return fail(ctx, RJ_E_BUSY, "a serving loop owns the context");
+    // one ordinary run settles the caches the capture relies on: polygon-side
+    // structures, the set's overlap status on this canvas, the tuned shapes
+    int rc = rj_execute(ctx, q, nullptr);
+    if (rc) return rc;
+    const int P = ctx->ps->P;
+    rj_plan* p = new rj_plan();
+    p->ctx = ctx;
+    p->stream = ctx->stream;
+    p->P = P;
+    p->function_type = q->function_type;
+    p->aggr_attrib = q->aggregation != RJ_COUNT ? q->aggr_attrib : -1;
+    p->table_gen = ctx->table_gen;
+    p->tix_gen = ctx->tix_gen;
+    p->uses_tix = ctx->tix.valid && q->time_attrib >= 0 && q->time_attrib == ctx->tix.attrib;
+    p->ps = ctx->ps;
+    p->ps_version = ctx->ps->version;
+    p->npts = ctx->npts;
+    if (cudaHostAlloc(&p->hc, P * sizeof(unsigned long long), 0) != cudaSuccess ||
+        cudaHostAlloc(&p->hq, P * sizeof(unsigned long long), 0) != cudaSuccess ||
+        cudaHostAlloc(&p->hnf, P * sizeof(double), 0) != cudaSuccess ||
+        cudaHostAlloc(&p->hb, (size_t)4 * P * sizeof(long long), 0) != cudaSuccess ||
+        cudaHostAlloc(&p->derr, sizeof(int), 0) != cudaSuccess) {
+        cudaGetLastError();
+        plan_free(p);
+        return fail(ctx, RJ_E_OOM, "pinned result buffers of the plan");
+    }
+    rj_query qc = *q;
+    qc.flags &= ~RJ_FLAG_PHASE_TIMING;
+    Phase ph(ctx, false);
+    unsigned long long *oc = nullptr, *os = nullptr;
+    double* onf = nullptr;
+    long long* ob = nullptr;
+    double t_setup = 0;
+    cudaError_t ce = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed);
+    if (ce != cudaSuccess) {
+        cudaGetLastError();
+        plan_free(p);
+        return fail(ctx, RJ_E_CUDA, "cudaStreamBeginCapture: %s", cudaGetErrorString(ce));
+    }
+    ctx->capturing = true;
+    rc = enqueue_query(ctx, &qc, ph, &oc, &os, &onf, &ob, &t_setup);
+    if (!rc) {
+        cudaMemcpyAsync(p->hc, oc, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(p->hq, os, P * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(p->hnf, onf, P * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(p->hb, ob, (size_t)4 * P * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(p->derr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    }
+    p->shift = ctx->sum_shift;
+    ctx->capturing = false;
+    cudaGraph_t g = nullptr;
+    ce = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc || ce != cudaSuccess || !g) {
+        cudaGetLastError();
+        if (g) cudaGraphDestroy(g);
+        plan_free(p);
+        if (rc) return rc;
+        return fail(ctx, RJ_E_UNSUPPORTED, "the query's work could not be captured: %s", cudaGetErrorString(ce));
+    }
+    p->graph = g;
+    ce = cudaGraphInstantiate(&p->exec, g, 0);
+    if (ce != cudaSuccess) {
+        cudaGetLastError();
+        plan_free(p);
+        return fail(ctx, RJ_E_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(ce));
+    }
+    *out = p;
+    return RJ_OK;
+}
+
+int rj_execute_prepared(rj_plan* p, rj_result* res) {
+    if (!p || !p->ctx) return RJ_E_INVALID;
+    rj_ctx* ctx = p->ctx;
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    ctx->err.clear();
+    const double t0 = now_ms();
+    if (res && res->npolys != 0 && res->npolys != p->P)
+        return fail(ctx, RJ_E_INVALID, "result sized for %d polygons, the plan has %d", res->npolys, p->P);
+    if (ctx->table_gen != p->table_gen || ctx->npts != p->npts || ctx->ps != p->ps || ctx->ps->version != p->ps_version ||
+        ctx->stream != p->stream || (p->uses_tix && ctx->tix_gen != p->tix_gen))
+        return fail(ctx, RJ_E_INVALID, "the table, the polygon set or the stream changed since rj_prepare");
+    if (p->aggr_attrib >= 0) {
+        // a reload in place may change the aggregate's range and so the shift
+        const Column* col = find_col(ctx, p->aggr_attrib);
+        const int shift = ctx->forced_shift != RJ_SUM_SHIFT_AUTO
+                              ? ctx->forced_shift
+                              : rj_sum_shift_for(col ? (double)col->absmax : 0.0, ctx->npts);
+        if (shift != p->shift)
+            return fail(ctx, RJ_E_INVALID, "the aggregate's fixed-point scale changed since rj_prepare (%d -> %d)",
+                        p->shift, shift);
+    }
+    cudaSetDevice(ctx->device);
+    RJ_CUDA(cudaGraphLaunch(p->exec, ctx->stream));
+    RJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (*p->derr) return fail(ctx, RJ_E_TIMEOUT, "a bounded device wait ran out (status 0x%x)", *p->derr);
+    const int P = p->P;
+    decode_result(P, p->hc, p->hq, p->hnf, p->shift, p->function_type == RJ_RASTER_JOIN_BOUNDS ? p->hb : nullptr,
+                  res);
+    ctx->last_fixed.assign(p->hq, p->hq + P);
+    ctx->last_nonfinite.assign(p->hnf, p->hnf + P);
+    ctx->last_shift = p->shift;
+    rj_timings& t = ctx->tm;
+    std::memset(&t, 0, sizeof t);
+    t.pts_size = ctx->npts;
+    t.poly_size = P;
+    t.function = p->function_type;
+    t.no_pt_passes = 1;
+    t.execute_ms = now_ms() - t0;
+    t.kernel_launches = 0;
+    return RJ_OK;
+}
+
+void rj_plan_destroy(rj_plan* p) {
+    if (!p) return;
+    if (p->ctx) {
+        std::lock_guard<std::recursive_mutex> lock(p->ctx->mu);
+        cudaSetDevice(p->ctx->device);
+        plan_free(p);
+        return;
+    }
+    plan_free(p);
 }
 
 int rj_selftest_bounded_wait(rj_ctx* ctx, uint32_t limit_us) {

@@ -39,6 +39,7 @@ TUNE_POINT_SHAPE, TUNE_COUNT_SHAPE, TUNE_COUNT_BLOCK_SHIFT, TUNE_HYBRID_EXACT_SC
 TUNE_COUNT_SHAPES, TUNE_LEAN_SHAPES, TUNE_WAIT_LIMIT = 4, 5, 6
 BATCH_AUTOTUNE = 0x1
 BATCH_NO_FUSE = 0x2
+BATCH_FUSE_ALL = 0x4
 MAX_CONSTRAINTS = 10
 
 FLAG_COMPAT_INDEX_CLAMP = 0x1
@@ -158,6 +159,9 @@ def load_library(path=LIB_PATH):
         "rj_server_destroy": (None, [C.c_void_p]),
         "rj_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
         "rj_selftest_bounded_wait": (C.c_int, [C.c_void_p, C.c_uint32]),
+        "rj_prepare": (C.c_int, [C.c_void_p, P(Query), P(C.c_void_p)]),
+        "rj_execute_prepared": (C.c_int, [C.c_void_p, P(Result)]),
+        "rj_plan_destroy": (None, [C.c_void_p]),
         "rj_get_sum_partials": (C.c_int, [C.c_void_p, P(C.c_int64), P(C.c_double), P(C.c_int32)]),
         "rj_set_sum_shift": (C.c_int, [C.c_void_p, C.c_int32]),
         "rj_sum_shift_for": (C.c_int32, [C.c_double, C.c_uint64]),
@@ -244,6 +248,39 @@ class PolySet:
         if getattr(self, "ptr", None) and getattr(self.handler, "ctx", None):
             self.handler.lib.rj_polyset_destroy(self.ptr)
         self.ptr = None
+
+
+class Plan:
+    """A prepared query (rj_prepare): replays its captured CUDA graph."""
+
+    def __init__(self, handler, fn, query, P):
+        self.h = handler
+        self.fn = fn
+        self.P = P
+        self.ptr = C.c_void_p()
+        handler._check(handler.lib.rj_prepare(handler.ctx, C.byref(query), C.byref(self.ptr)))
+
+    def execute(self):
+        P = self.P
+        count = np.zeros(P, np.uint64)
+        sum_ = np.zeros(P, np.float64)
+        compat3 = np.zeros(3 * P, np.int32)
+        bounds = np.zeros(4 * P, np.int32)
+        r = Result(P, count.ctypes.data_as(C.POINTER(C.c_uint64)), sum_.ctypes.data_as(C.POINTER(C.c_double)),
+                   compat3.ctypes.data_as(C.POINTER(C.c_int32)), bounds.ctypes.data_as(C.POINTER(C.c_int32)))
+        self.h._check(self.h.lib.rj_execute_prepared(self.ptr, C.byref(r)))
+        return JoinResult(count, sum_, compat3, bounds if self.fn == RasterJoinBoundFn else None)
+
+    def close(self):
+        if self.ptr:
+            self.h.lib.rj_plan_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Server:
@@ -515,6 +552,14 @@ class GLHandler:
         self.last = JoinResult(count, sum_, compat3, bounds if fn == RasterJoinBoundFn else None)
         self.bounds = bounds if fn == RasterJoinBoundFn else None
         return self.last
+
+    def prepare(self, fn, query=None):
+        """rj_prepare: a Plan whose execute() replays the query's captured graph."""
+        if self.dataHandler is not None:
+            self.upload()
+        q = query if query is not None else self.make_query(fn)
+        P = self._bound.P if self._bound is not None else len(self.dataHandler.polys[1]) - 1
+        return Plan(self, fn, q, P)
 
     def executeFunction(self, fn):
         """GLHandler::executeFunction (GLHandler.cpp:188-204): int32[3P]."""

@@ -286,3 +286,31 @@ def test_batch_tiered_canvases(setup):
     for (c, sm), r in zip(flat, res):
         np.testing.assert_array_equal(r.count, c)
         np.testing.assert_array_equal(r.sum, sm)
+
+
+def test_point_heavy_label_queries_leave_the_fused_pass(built):
+    """Label-map queries over >= 2^22 rows run through rj_execute's lean pass
+    inside a batch (counted as fallback); RJ_BATCH_FUSE_ALL keeps them fused.
+    Both give the single-query results bit for bit."""
+    big = synth.points(5_000_001, seed=78, columns=True)
+    v, p = poly_sets()[0]
+    h = rj.GLHandler()
+    try:
+        h.setDataHandler(make_dh(big, v, p))
+        h.upload()
+        ps = h.polyset(v, p)
+        qs = [make_query(20.0), make_query(30.0, aggr=True, preds=((4, rj.GT, 2),)),
+              make_query(20.0, max_fbo=1000)]                     # a multi-tile canvas stays fused
+        alone = [single(h, ps, q) for q in qs]
+        res, status, stats = h.execute_batch(qs, [ps] * 3)
+        assert (status == 0).all() and stats["fused"] == 1 and stats["fallback"] == 2
+        res2, status2, stats2 = h.execute_batch(qs, [ps] * 3, flags=rj.BATCH_FUSE_ALL)
+        assert (status2 == 0).all() and stats2["fused"] == 3 and stats2["fallback"] == 0
+        for (c, s), r, r2 in zip(alone, res, res2):
+            np.testing.assert_array_equal(r.count, c)
+            np.testing.assert_array_equal(r.sum, s)
+            np.testing.assert_array_equal(r2.count, c)
+            np.testing.assert_array_equal(r2.sum, s)
+        ps.close()
+    finally:
+        h.close()
