@@ -324,35 +324,47 @@ def run_batched(rj, h, cum, n, nq):
     sets = [h.polyset(xy, p) for xy, p, _, _, _ in work]
     qs = [make_raster_query(rj, cell, win, avg) for _, _, cell, win, avg in work]
     pq = sum(window_rows(cum, *win) for _, _, _, win, _ in work)
-    # warm-up: overlap checks of the new polygon sets and the block-shape tuner
-    h.execute_batch(qs, sets, flags=rj.BATCH_AUTOTUNE)
-    fused_ms, stats = [], None
-    for _ in range(3):
-        t0 = time.perf_counter()
-        res, status, stats = h.execute_batch(qs, sets)
-        fused_ms.append((time.perf_counter() - t0) * 1e3)
-    plain_ms = []
-    for _ in range(2):
-        t0 = time.perf_counter()
-        res2, status2, stats2 = h.execute_batch(qs, sets, flags=rj.BATCH_NO_FUSE)
-        plain_ms.append((time.perf_counter() - t0) * 1e3)
-    same = all(np.array_equal(a.count, b.count) and np.array_equal(a.sum, b.sum) for a, b in zip(res, res2))
+
+    def timed(flags, reps):
+        ms, out = [], None
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            out = h.execute_batch(qs, sets, flags=flags)
+            ms.append((time.perf_counter() - t0) * 1e3)
+        return float(np.median(ms)), out
+
+    # warm-up: overlap checks of the new polygon sets, the lean passes' tuner
+    # (on the lanes) and the fused pass's block-shape tuner
+    h.execute_batch(qs, sets)
+    h.execute_batch(qs, sets, flags=rj.BATCH_FUSE | rj.BATCH_AUTOTUNE)
+    b_ms, (res, status, stats) = timed(0, 3)                      # the batch API's default route: lanes
+    f_ms, (res_f, status_f, stats_f) = timed(rj.BATCH_FUSE, 2)    # fused pass for the small queries
+    p_ms, (res_p, status_p, _) = timed(rj.BATCH_NO_FUSE, 2)       # plain: rj_execute in turn
+    same = all(np.array_equal(a.count, b.count) and np.array_equal(a.sum, b.sum) and
+               np.array_equal(a.count, c.count) and np.array_equal(a.sum, c.sum)
+               for a, b, c in zip(res, res_f, res_p))
     for s in sets:
         s.close()
-    f, pl = float(np.median(fused_ms)), float(np.median(plain_ms))
     return {
         "workload": "%d raster queries over a %d-point resident table; per query 1-5000 star polygons "
                     "(4-2000 vertices), eps log-uniform 1-1000 m, time window of 1e4-5e8 points, "
                     "count or avg" % (nq, n),
-        "point_queries": pq, "fused_ms": f, "plain_ms": pl,
-        "fused_gpoints_s": pq / f / 1e6, "plain_gpoints_s": pq / pl / 1e6, "speedup": pl / f,
-        "rows_read": stats["rows_read"], "segments": stats["segments"], "point_pass_ms": stats["point_ms"],
-        "polygon_side_ms": stats["poly_ms"], "canvas_reduce_ms": stats["reduce_ms"],
-        "shape": {"threads": stats["threads"], "rows_per_item": stats["rows_per_item"],
-                  "variant": "direct" if stats["direct"] else "staged"},
+        "point_queries": pq, "batched_ms": b_ms, "plain_ms": p_ms, "speedup": p_ms / b_ms,
+        "batched_gpoints_s": pq / b_ms / 1e6, "plain_gpoints_s": pq / p_ms / 1e6,
+        "route": "every query on the lanes: rj_execute's device path on 4 streams with their own scratch, "
+                 "queued without host waits, one wait per batch",
         "kernel_launches": stats["kernel_launches"],
-        "status_ok": bool((status == 0).all() and (status2 == 0).all()), "same_result": bool(same),
-        "plain": "each query through rj_execute in turn (one query per launch sequence)",
+        "fused_variant": {"ms": f_ms, "speedup": p_ms / f_ms, "fused_queries": stats_f["fused"],
+                          "rows_read": stats_f["rows_read"], "segments": stats_f["segments"],
+                          "point_pass_ms": stats_f["point_ms"], "polygon_side_ms": stats_f["poly_ms"],
+                          "canvas_reduce_ms": stats_f["reduce_ms"], "kernel_launches": stats_f["kernel_launches"],
+                          "shape": {"threads": stats_f["threads"], "rows_per_item": stats_f["rows_per_item"],
+                                    "variant": "direct" if stats_f["direct"] else "staged"},
+                          "route": "queries under 2^22 rows in one fused point pass per wave, the others on "
+                                   "the lanes (RJ_BATCH_FUSE)"},
+        "status_ok": bool((status == 0).all() and (status_f == 0).all() and (status_p == 0).all()),
+        "same_result": bool(same),
+        "plain": "each query through rj_execute in turn (one query per launch sequence, RJ_BATCH_NO_FUSE)",
     }
 
 
@@ -797,10 +809,16 @@ def run_config3(args):
         ps = h.polyset(v, p)
         h.usePolySet(ps)
         for eps in (10.0, 1.0):
-            for fn in (rj.RasterJoinFn, rj.RasterJoinBoundFn):
+            forms = [(rj.RasterJoinFn, 0), (rj.RasterJoinBoundFn, 0)]
+            if eps == 1.0:
+                # both canvas forms of the 40000 x 40000 canvas: flat (a label
+                # map or count canvas per pixel) and tiered (16 x 16 blocks)
+                forms += [(rj.RasterJoinFn, rj.FLAG_FLAT_CANVAS), (rj.RasterJoinFn, rj.FLAG_TIERED_CANVAS)]
+            for fn, form in forms:
                 q = rj.default_query()
                 q.function_type = fn
                 q.cell_size = eps
+                q.flags |= rj.FLAG_PHASE_TIMING | form   # per-phase CUDA events (point pass, polygon side)
                 h.execute(fn, query=q)                 # warm-up (builds the polygon structures once)
                 ms = []
                 for _ in range(max(1, args.steps)):
@@ -810,6 +828,7 @@ def run_config3(args):
                 P = len(p) - 1
                 tm = h.timings()
                 rec = {"polygons": name, "eps_m": eps, "join": "raster" if fn == rj.RasterJoinFn else "error-bounds",
+                       "canvas": {0: "default", rj.FLAG_FLAT_CANVAS: "flat", rj.FLAG_TIERED_CANVAS: "tiered"}[form],
                        "ms": float(np.median(ms)), "gpoints_s": n / float(np.median(ms)) / 1e6,
                        "total_count": int(r.count.sum()),
                        "point_pass_ms": tm["pt_render_ms"], "polygon_side_ms": tm["poly_render_ms"],

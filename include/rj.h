@@ -97,6 +97,9 @@ typedef struct {
 #define RJ_FLAG_FLAT_CANVAS        0x80u /* raster: one entry per pixel even for
                                            large canvases (no 16 x 16 block
                                            tiers; same results)              */
+#define RJ_FLAG_TIERED_CANVAS      0x100u /* raster: 16 x 16 block tiers for any
+                                           canvas of at least 2^24 pixels,
+                                           whatever the rows (same results)  */
 
 /* One query: everything GLHandler + DataHandler held between calls
  * (setAccuracyDistance GLHandler.cpp:250, setPolyIndexResolution :259,
@@ -279,6 +282,12 @@ RJ_API int rj_column_absmax(const rj_ctx *ctx, int32_t attrib_id, double *out);
  *                            with filters (interval form, <= 4 columns) or
  *                            a summed aggregate; RJ_TUNE_COUNT_SHAPE indexes
  *                            the shapes of the form the query takes
+ *   RJ_TUNE_SPLAT_SHAPES     (read only) number of shapes of the lean pass
+ *                            onto a point canvas (one canvas tile: polygon
+ *                            sets that overlap on it, the error-bounds
+ *                            join); RJ_TUNE_COUNT_SHAPE indexes them there
+ *                            too (canvas copies in shared memory, or
+ *                            atomics into the canvas in global memory)
  *   RJ_TUNE_WAIT_LIMIT       microseconds a bounded device wait of the
  *                            bulk-copy pipeline (RJ_TUNE_POINT_SHAPE 2) may
  *                            take before it gives up and the call returns
@@ -294,6 +303,7 @@ RJ_API int rj_column_absmax(const rj_ctx *ctx, int32_t attrib_id, double *out);
 #define RJ_TUNE_COUNT_SHAPES       4
 #define RJ_TUNE_LEAN_SHAPES        5
 #define RJ_TUNE_WAIT_LIMIT         6
+#define RJ_TUNE_SPLAT_SHAPES       7
 RJ_API int rj_set_tuning(rj_ctx *ctx, int32_t knob, int32_t value);
 RJ_API int rj_get_tuning(const rj_ctx *ctx, int32_t knob, int32_t *value);
 
@@ -377,12 +387,20 @@ RJ_API int rj_cluster_points(rj_ctx *ctx, int32_t time_attrib, int32_t nbuckets,
  * through rj_execute.  res[i] is filled like rj_execute's result; status[i]
  * (may be NULL) receives each query's status.  Returns RJ_OK when every
  * query succeeded, else the first failing status. */
-#define RJ_BATCH_AUTOTUNE 0x1u   /* time the point-pass block shapes on this batch and keep the fastest */
-#define RJ_BATCH_NO_FUSE  0x2u   /* run every query through rj_execute (the plain path) */
-#define RJ_BATCH_FUSE_ALL 0x4u   /* fuse every raster query, also those the lean
-                                    single-query pass runs faster (by default
-                                    label-map queries over >= 2^22 rows take
-                                    rj_execute's lean pass; `fallback` counts them) */
+#define RJ_BATCH_AUTOTUNE 0x1u   /* time the fused pass's block shapes on this batch and keep the fastest */
+#define RJ_BATCH_NO_FUSE  0x2u   /* run every query through rj_execute in turn (the plain path) */
+#define RJ_BATCH_FUSE_ALL 0x4u   /* fuse every raster query */
+#define RJ_BATCH_FUSE     0x8u   /* fuse the raster queries over fewer than 2^22
+                                    rows or on multi-tile canvases; the others
+                                    take the lanes */
+/* By default every raster query of a batch takes rj_execute's device path on
+ * one of four lanes: streams with their own scratch, so that the work of
+ * several queries overlaps on the GPU (and, with RJ_BATCH_FUSE, with the
+ * fused pass); each lane's outputs come back through pinned staging, with one
+ * wait for the whole batch.  Queries of one polygon set share a lane.
+ * Results are those of rj_execute, bit for bit, on every route; `fallback`
+ * counts the queries that did not run fused.  A serving loop's batches use
+ * the fused pass (its slots allocate nothing while serving). */
 typedef struct {
     int32_t nqueries, fused, fallback;
     int32_t segments;              /* row ranges covered by one set of queries */

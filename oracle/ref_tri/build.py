@@ -11,7 +11,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(os.path.dirname(HERE), "_ref")
 LIB = os.path.join(OUT_DIR, "libreftri.so")
-REF = "/root/reference/RasterJoin/triangulation"
+# the reference tree: RJ_REFERENCE_DIR, else its usual mount point
+REF = os.path.join(os.environ.get("RJ_REFERENCE_DIR", "/root/reference"), "RasterJoin", "triangulation")
 SOURCES = ["clip2tri/clip2tri.cpp", "clipper/clipper.cpp", "poly2tri/common/shapes.cc",
            "poly2tri/sweep/advancing_front.cc", "poly2tri/sweep/cdt.cc", "poly2tri/sweep/sweep.cc",
            "poly2tri/sweep/sweep_context.cc"]

@@ -20,6 +20,8 @@
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <map>
+#include <string>
 #include <thread>
 #include <unordered_map>
 
@@ -52,6 +54,12 @@ size_t al256(size_t b) { return (std::max<size_t>(b, 1) + 255) & ~size_t(255); }
 // label-map query, or pixels of a small splat canvas)
 constexpr int kBatchHistCap = 4096;
 
+// Streams of the queries that leave the fused pass: each lane has its own
+// scratch (keys suffixed with the lane) and error word, so that the device
+// work of several such queries -- and of the fused pass on the engine's own
+// stream -- overlaps on the GPU.
+constexpr int kLanes = 4;
+
 struct Engine {
     rj_ctx* ctx = nullptr;
     cudaStream_t st = nullptr;
@@ -63,6 +71,13 @@ struct Engine {
     size_t h_pin_bytes = 0;
     BatchShape shape{256, 16384, 1};
     bool tuned = false;
+    bool lanes = false;          // rj_execute_batch's engine; a serving slot (fixed
+                                 // arena, no allocation while serving) runs them in turn
+    cudaStream_t lane_st[kLanes]{};
+    int* lane_err = nullptr;     // device: one error word per lane
+    cudaEvent_t lane_ev = nullptr;
+    void* lane_pin = nullptr;    // pinned staging of the lanes' outputs
+    size_t lane_pin_bytes = 0;
 };
 
 int engine_init(rj_ctx* ctx, Engine& e, cudaStream_t st, size_t cap) {
@@ -81,6 +96,19 @@ int engine_init(rj_ctx* ctx, Engine& e, cudaStream_t st, size_t cap) {
 
 void engine_free(Engine& e) {
     if (e.st) cudaStreamSynchronize(e.st);
+    for (auto& s : e.lane_st) {
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+        s = nullptr;
+    }
+    if (e.lane_err) cudaFree(e.lane_err);
+    e.lane_err = nullptr;
+    if (e.lane_ev) cudaEventDestroy(e.lane_ev);
+    e.lane_ev = nullptr;
+    if (e.lane_pin) cudaFreeHost(e.lane_pin);
+    e.lane_pin = nullptr;
     if (e.ar.buf.p) dev_free(e.ctx, e.ar.buf);
     if (e.h_pin) cudaFreeHost(e.h_pin);
     e.h_pin = nullptr;
@@ -155,10 +183,12 @@ size_t canvas_bytes(const QPlan& p) {
 
 // Host planning of one query (under the context lock: filters and canvas
 // plans report errors through the context).
-// Label-map queries over at least this many rows run faster through the lean
-// single-query pass (block codes in shared memory, plain shared atomics) than
-// in the fused pass, whose shared row reads save little: the per-(point,
-// query) work dominates, not the row read.  They leave the fused pass.
+// Single-tile queries over at least this many rows run faster through the
+// lean single-query passes (label map: block codes in shared memory, plain
+// shared atomics; point canvas: canvas copies in shared memory or plain
+// atomics) than in the fused pass, whose shared row reads save little: the
+// per-(point, query) work dominates, not the row read.  They leave the fused
+// pass.
 constexpr uint64_t kLeanQueryRows = 1ull << 22;
 
 void plan_query(rj_ctx* ctx, QPlan& p, bool no_fuse, bool fuse_all) {
@@ -179,7 +209,7 @@ void plan_query(rj_ctx* ctx, QPlan& p, bool no_fuse, bool fuse_all) {
     p.r0 &= ~3ULL;
     p.r1 = std::min<uint64_t>(ctx->npts, (p.r1 + 3) & ~3ULL);
     // large canvases: tiered form (per-block work instead of per-pixel work)
-    p.tier = use_tier(p.npix, p.r1 - p.r0) && !(q->flags & RJ_FLAG_FLAT_CANVAS);
+    p.tier = query_tier(q->flags, p.npix, p.r1 - p.r0);
     if (p.tier) {
         p.tr.bw = (p.rp.resx + 15) / 16;
         p.tr.bh = (p.rp.resy + 15) / 16;
@@ -207,8 +237,8 @@ void plan_query(rj_ctx* ctx, QPlan& p, bool no_fuse, bool fuse_all) {
     } else {
         p.mode = (label_ok && known != 1) ? BQ_LABEL : BQ_SPLAT;
         p.check_overlap = p.mode == BQ_LABEL && known != 0;
-        if (!fuse_all && p.mode == BQ_LABEL && p.T == 1 && !p.f.general && p.f.ncol <= label_lean_max_cols() &&
-            p.r1 - p.r0 >= kLeanQueryRows)
+        if (!fuse_all && (p.mode == BQ_LABEL || p.mode == BQ_SPLAT) && p.T == 1 && !p.f.general &&
+            p.f.ncol <= label_lean_max_cols() && p.r1 - p.r0 >= kLeanQueryRows)
             p.fused = false;   // rj_execute's lean pass (same results)
     }
 }
@@ -760,6 +790,135 @@ int run_fused(Engine& e, std::vector<QPlan>& plans, uint32_t flags, BatchOut& bo
     return RJ_OK;
 }
 
+// Raster queries that leave the fused pass, queued on the lanes: the device
+// work of rj_execute (enqueue_query_untimed) with the query's polygon set
+// bound, the outputs copied to pinned staging on the lane, nothing waited
+// for.  Queries of one polygon set share a lane (the set's host-side caches
+// are filled in stream order).  lanes_finish waits for the lanes and decodes.
+struct LaneRun {
+    std::vector<QPlan*> q;
+    std::vector<size_t> off;     // staging offset of each query's outputs
+    std::vector<int> shift;
+    std::vector<bool> bounds;
+    bool queued = false;
+};
+
+int lanes_enqueue(Engine& e, LaneRun& lr, int& launches) {
+    rj_ctx* ctx = e.ctx;
+    if (lr.q.empty()) return RJ_OK;
+    if (!e.lane_err) {
+        for (auto& s : e.lane_st)
+            if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return fail(ctx, RJ_E_CUDA, "lane stream");
+        if (cudaEventCreateWithFlags(&e.lane_ev, cudaEventDisableTiming) != cudaSuccess) return fail(ctx, RJ_E_CUDA, "lane event");
+        if (cudaMalloc(&e.lane_err, kLanes * sizeof(int)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(ctx, RJ_E_OOM, "lane error words");
+        }
+    }
+    const size_t nq = lr.q.size();
+    lr.off.assign(nq, 0);
+    lr.shift.assign(nq, 0);
+    lr.bounds.assign(nq, false);
+    size_t bytes = 0;
+    for (size_t i = 0; i < nq; ++i) {
+        lr.off[i] = bytes;
+        lr.bounds[i] = lr.q[i]->q->function_type == RJ_RASTER_JOIN_BOUNDS;
+        const size_t P = (size_t)lr.q[i]->ps->P;
+        bytes += al256(P * 24 + (lr.bounds[i] ? P * 32 : 0) + 8);
+    }
+    if (e.lane_pin_bytes < bytes) {
+        if (e.lane_pin) cudaFreeHost(e.lane_pin);
+        e.lane_pin = nullptr;
+        e.lane_pin_bytes = 0;
+        if (cudaMallocHost(&e.lane_pin, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(ctx, RJ_E_OOM, "pinned staging of the lanes");
+        }
+        e.lane_pin_bytes = bytes;
+    }
+    char* h = (char*)e.lane_pin;
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    // the lanes start after the work already queued on the context's stream
+    RJ_CUDA(cudaEventRecord(e.lane_ev, ctx->stream));
+    for (auto& s : e.lane_st) RJ_CUDA(cudaStreamWaitEvent(s, e.lane_ev, 0));
+    cudaStream_t saved_st = ctx->stream;
+    int* saved_err = ctx->d_err;
+    PolySet* saved_ps = ctx->ps;
+    const std::string saved_ns = ctx->scratch_ns;
+    std::map<const PolySet*, int> lane_of;
+    int next = 0;
+    for (size_t i = 0; i < nq; ++i) {
+        QPlan& p = *lr.q[i];
+        auto it = lane_of.find(p.ps);
+        const int l = it != lane_of.end() ? it->second : (lane_of[p.ps] = (next++) % kLanes);
+        ctx->stream = e.lane_st[l];
+        ctx->d_err = e.lane_err + l;
+        ctx->scratch_ns = "#lane" + std::to_string(l);
+        ctx->ps = p.ps;
+        unsigned long long *oc = nullptr, *os = nullptr;
+        double* onf = nullptr;
+        long long* ob = nullptr;
+        int rc = enqueue_query_untimed(ctx, p.q, &oc, &os, &onf, &ob);
+        launches += g_kernel_launches;
+        if (!rc) {
+            lr.shift[i] = ctx->sum_shift;
+            const size_t P = (size_t)p.ps->P;
+            char* b = h + lr.off[i];
+            cudaStream_t st = ctx->stream;
+            if (cudaMemcpyAsync(b, oc, P * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaMemcpyAsync(b + P * 8, os, P * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaMemcpyAsync(b + P * 16, onf, P * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                (lr.bounds[i] && cudaMemcpyAsync(b + P * 24, ob, P * 32, cudaMemcpyDeviceToHost, st) != cudaSuccess) ||
+                cudaMemcpyAsync(b + P * (lr.bounds[i] ? 56 : 24), ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost,
+                                st) != cudaSuccess) {
+                cudaGetLastError();
+                rc = fail(ctx, RJ_E_CUDA, "query %d: copying its outputs back", p.idx);
+            }
+        }
+        if (rc) {
+            cudaStreamSynchronize(ctx->stream);
+            p.status = rc;
+        }
+    }
+    ctx->stream = saved_st;
+    ctx->d_err = saved_err;
+    ctx->ps = saved_ps;
+    ctx->scratch_ns = saved_ns;
+    lr.queued = true;
+    return RJ_OK;
+}
+
+int lanes_finish(Engine& e, LaneRun& lr) {
+    if (!lr.queued) return RJ_OK;
+    int rc = RJ_OK;
+    for (auto& s : e.lane_st)
+        if (s && cudaStreamSynchronize(s) != cudaSuccess) rc = RJ_E_CUDA;
+    if (rc) {
+        cudaGetLastError();
+        for (QPlan* p : lr.q)
+            if (p->status == RJ_OK) p->status = RJ_E_CUDA;
+        return fail(e.ctx, RJ_E_CUDA, "a lane of the batch failed");
+    }
+    const char* h = (const char*)e.lane_pin;
+    for (size_t i = 0; i < lr.q.size(); ++i) {
+        QPlan& p = *lr.q[i];
+        if (p.status != RJ_OK) continue;
+        const size_t P = (size_t)p.ps->P;
+        const char* b = h + lr.off[i];
+        int derr = 0;
+        std::memcpy(&derr, b + P * (lr.bounds[i] ? 56 : 24), sizeof derr);
+        if (derr) {
+            p.status = fail(e.ctx, RJ_E_TIMEOUT, "query %d: a bounded device wait ran out (status 0x%x)", p.idx, derr);
+            continue;
+        }
+        decode_result((int)P, (const unsigned long long*)b, (const unsigned long long*)(b + P * 8),
+                      (const double*)(b + P * 16), lr.shift[i],
+                      lr.bounds[i] ? (const long long*)(b + P * 24) : nullptr, p.res);
+    }
+    lr.queued = false;
+    return RJ_OK;
+}
+
 // One query through rj_execute with its polygon set bound.
 int run_plain(rj_ctx* ctx, QPlan& p) {
     std::lock_guard<std::recursive_mutex> lock(ctx->mu);
@@ -776,6 +935,9 @@ int execute_batch(Engine& e, int nq, const rj_query* qs, const rj_query* const* 
     const double t0 = now_ms();
     std::vector<QPlan> plans(nq);
     g_kernel_launches = 0;
+    // rj_execute_batch's engine sends every raster query to the lanes unless
+    // the fused pass is asked for; a serving slot fuses
+    const bool lanes_all = e.lanes && !(flags & (RJ_BATCH_FUSE | RJ_BATCH_FUSE_ALL | RJ_BATCH_NO_FUSE));
     {
         std::lock_guard<std::recursive_mutex> lock(ctx->mu);
         if (ctx->npts == 0 && ctx->cols.empty()) return fail(ctx, RJ_E_NO_DATA, "point table not loaded");
@@ -792,26 +954,45 @@ int execute_batch(Engine& e, int nq, const rj_query* qs, const rj_query* const* 
                 p.status = fail(ctx, RJ_E_INVALID, "query %d: result sized for %d polygons, set has %d", i, p.res->npolys, p.ps->P);
                 continue;
             }
-            plan_query(ctx, p, (flags & RJ_BATCH_NO_FUSE) != 0, (flags & RJ_BATCH_FUSE_ALL) != 0);
+            plan_query(ctx, p, (flags & RJ_BATCH_NO_FUSE) != 0 || lanes_all, (flags & RJ_BATCH_FUSE_ALL) != 0);
         }
         const int zrc = ensure_zones(ctx);   // lets the point pass skip rows far from a query
         if (zrc) return zrc;
     }
     const double t_setup = now_ms();
     BatchOut bo;
-    int rc = run_fused(e, plans, flags, bo);
+    // raster queries that leave the fused pass go to the lanes first (queued,
+    // not waited for), so that they overlap with the fused pass; with
+    // RJ_BATCH_NO_FUSE every query runs through rj_execute in turn instead
+    LaneRun lr;
+    int plain_launches = 0;
+    if (e.lanes && !(flags & RJ_BATCH_NO_FUSE) && !ctx->streamed)
+        for (QPlan& p : plans)
+            if (p.status == RJ_OK && !p.fused &&
+                (p.q->function_type == RJ_RASTER_JOIN || p.q->function_type == RJ_RASTER_JOIN_BOUNDS))
+                lr.q.push_back(&p);
+    int rc = lanes_enqueue(e, lr, plain_launches);
+    if (rc) {
+        for (QPlan* p : lr.q)
+            if (p->status == RJ_OK) p->status = rc;
+        lr.q.clear();
+    }
+    g_kernel_launches = 0;
+    rc = run_fused(e, plans, flags, bo);
     if (rc) {
         for (QPlan& p : plans)
             if (p.fused && p.status == RJ_OK) p.status = rc;
     }
     const int launches_fused = g_kernel_launches;
-    int plain_launches = 0;
     for (QPlan& p : plans) {
         if (p.status != RJ_OK || p.fused) continue;
+        if (std::find(lr.q.begin(), lr.q.end(), &p) != lr.q.end()) continue;
         p.status = run_plain(ctx, p);
         plain_launches += ctx->tm.kernel_launches;
         ++bo.fallback;
     }
+    lanes_finish(e, lr);
+    bo.fallback += (int)lr.q.size();
     int first = RJ_OK;
     for (QPlan& p : plans) {
         if (status) status[p.idx] = p.status;
@@ -1174,6 +1355,7 @@ int rj_execute_batch(rj_ctx* ctx, int32_t nq, const rj_query* q, rj_polyset* con
             ctx->batch_engine = nullptr;
             return fail(ctx, RJ_E_CUDA, "batch engine setup failed");
         }
+        e->lanes = true;
     }
     int rc = execute_batch(*e, nq, q, nullptr, sets, res, nullptr, status, flags, stats);
     // a large arena (label maps / canvases of a big batch) is not kept between calls

@@ -78,7 +78,7 @@ __device__ __forceinline__ void load_query_cols(const BatchArgs& a, const BatchQ
 // The four points x/y/v/mask of one thread through the mapper of MODE.
 template <int MODE, bool AGG, bool SMEM>
 __device__ __forceinline__ void map_points4(const BatchQuery* __restrict__ Q, const CanvasXf& cx, const float* x,
-                                            const float* y, const float* v, uint32_t mask, const Hist<AGG, SMEM>& h) {
+                                            const float* y, const float* v, uint32_t mask, const Hist<AGG, SMEM, true>& h) {
     const DeferQ dq{nullptr, nullptr, nullptr, nullptr};
     if constexpr (MODE == BQ_TLABEL) {
         const TierLabelMapper tm{cx, Q->tr};

@@ -17,7 +17,7 @@ namespace rj {
 // per mode, so only that mapper's state is live in it).
 template <int MODE, bool AGG, bool SMEM, int BLOCK>
 __device__ __forceinline__ void direct_rows(const BatchArgs& a, const BatchQuery* __restrict__ Q, uint64_t r0,
-                                            uint64_t r1, bool last, const Hist<AGG, SMEM>& h, const QueryCols* dc) {
+                                            uint64_t r1, bool last, const Hist<AGG, SMEM, true>& h, const QueryCols* dc) {
     const int tid = threadIdx.x;
     const int ncu = dc->n, aggc = dc->aggr;
     const int aggr_typ = Q->aggr_typ;
@@ -89,7 +89,7 @@ __device__ __forceinline__ void direct_query(const BatchArgs& a, const BatchQuer
                                              uint64_t r1, bool last, uint32_t* s_cnt, unsigned long long* s_sum,
                                              int* s_touch, int* s_ntouch, QueryCols* dc) {
     load_query_cols(a, Q, dc);
-    Hist<AGG, SMEM> h{s_cnt, s_sum, Q->out_count, Q->out_sum, Q->out_nonfinite, Q->sum_scale};
+    Hist<AGG, SMEM, true> h{s_cnt, s_sum, Q->out_count, Q->out_sum, Q->out_nonfinite, Q->sum_scale};
     h.s_touched = s_touch;
     h.s_ntouched = s_ntouch;
     switch (Q->mode) {

@@ -33,7 +33,7 @@ size_t batch_smem_bytes(const BatchShape& s, int nu, int hist_cap) {
 // mode, so only that mapper's state is live in it).
 template <int MODE, bool AGG, bool SMEM, int BLOCK>
 __device__ __forceinline__ void staged_rows(const BatchArgs& a, const BatchQuery* __restrict__ Q, const float2* s_xy,
-                                            const uint32_t* s_col, int nrows, const Hist<AGG, SMEM>& h,
+                                            const uint32_t* s_col, int nrows, const Hist<AGG, SMEM, true>& h,
                                             const QueryCols* qc) {
     const int tid = threadIdx.x;
     const int ncu = qc->n, aggc = qc->aggr;
@@ -69,7 +69,7 @@ __device__ __forceinline__ void batch_query(const BatchArgs& a, const BatchQuery
                                             uint32_t* s_cnt, unsigned long long* s_sum, int* s_touch,
                                             int* s_ntouch, QueryCols* qc) {
     load_query_cols(a, Q, qc);
-    Hist<AGG, SMEM> h{s_cnt, s_sum, Q->out_count, Q->out_sum, Q->out_nonfinite, Q->sum_scale};
+    Hist<AGG, SMEM, true> h{s_cnt, s_sum, Q->out_count, Q->out_sum, Q->out_nonfinite, Q->sum_scale};
     h.s_touched = s_touch;
     h.s_ntouched = s_ntouch;
     switch (Q->mode) {

@@ -129,6 +129,9 @@ struct rj_ctx {
     uint64_t cache_version = 0;
 
     std::map<std::string, rjh::DevBuf> scratch;
+    // suffix of the scratch keys: queries issued on another stream (the
+    // batched plain lanes) keep their buffers apart
+    std::string scratch_ns;
 
     rj_timings tm{};
     cudaEvent_t ev[8]{};
@@ -194,8 +197,22 @@ constexpr size_t kTierMinPixels = (size_t)1 << 24;
 // The tiered form also costs the point pass a little per point (a block code
 // before the pixel); it pays when the canvas has more pixels than about twice
 // the rows the query scans (measured on GB300: flat polygon side ~1.6 ps per
-// pixel, tiered point lookups ~3.1 ps per point more).
-inline bool use_tier(size_t npix, uint64_t rows) { return npix >= kTierMinPixels && npix > 2 * rows; }
+// pixel, tiered point lookups ~3.1 ps per point more while the flat canvas
+// stays in L2).  Beyond kTierFlatMaxPixels a flat canvas no longer stays in
+// L2 and every point's lookup goes to DRAM: 2B points on a 40000 x 40000
+// canvas took 52.7 ms flat against 21.5 ms tiered (260 Voronoi cells; 2000
+// overlapping stars: 97.3 against 56.7 ms).
+constexpr size_t kTierFlatMaxPixels = (size_t)1 << 25;
+inline bool use_tier(size_t npix, uint64_t rows) {
+    return npix >= kTierMinPixels && (npix > 2 * rows || npix > kTierFlatMaxPixels);
+}
+// the form a raster query takes: flat or tiered canvas (RJ_FLAG_FLAT_CANVAS /
+// RJ_FLAG_TIERED_CANVAS force one)
+inline bool query_tier(uint32_t flags, size_t npix, uint64_t rows) {
+    if (flags & RJ_FLAG_FLAT_CANVAS) return false;
+    if (flags & RJ_FLAG_TIERED_CANVAS) return npix >= kTierMinPixels;
+    return use_tier(npix, rows);
+}
 
 int fail(rj_ctx* c, int code, const char* fmt, ...);
 
@@ -233,6 +250,12 @@ void free_polyset(rj_ctx* ctx, PolySet& s);
 void decode_result(int P, const unsigned long long* hc, const unsigned long long* hq, const double* hnf, int shift,
                    const long long* hb, rj_result* res);
 void free_batch_engine(rj_ctx* ctx);
+// One query's device work queued on ctx->stream (the readbacks some forms
+// need aside, no host synchronisation) with the context's scratch and error
+// word; the per-polygon outputs stay on the device for the caller to copy.
+// ctx->sum_shift holds the query's fixed-point shift on return.
+int enqueue_query_untimed(rj_ctx* ctx, const rj_query* q, unsigned long long** oc, unsigned long long** os,
+                          double** onf, long long** ob);
 void query_rows(const rj_ctx* ctx, const rj_query* q, uint64_t& r0, uint64_t& r1);
 int ensure_zones(rj_ctx* ctx);
 

@@ -265,6 +265,24 @@ int label_lean_shapes();
 int label_lean_max_cols();
 size_t label_lean_smem(int shape, int code_words, int P, bool agg);
 bool launch_label_lean(int shape, const LabelCountArgs& a, const LeanCols& lc, int sms, cudaStream_t st);
+// Lean point pass onto a point canvas (rj_splat_kernels.cu): one canvas tile,
+// interval-form filters on at most four columns (LeanCols), count and sum.
+struct SplatLeanArgs {
+    const float4* xy;            // location column as point pairs, 16-byte aligned
+    uint64_t n;
+    float4 col0, row0;           // the tile transform (s, t, h) per axis
+    int resx, resy;
+    uint32_t* canvas_c;          // [resy][resx] counts
+    unsigned long long* canvas_s; // [resy][resx] int64 fixed-point sums, or null
+    const float4* zones;         // zone map or null (as LabelCountArgs)
+    uint64_t zrow0;
+    float4 qbox;
+};
+int splat_lean_shapes();
+// shared memory of a shape for a canvas (1 for the global-atomic shapes), 0
+// when the canvas does not fit
+size_t splat_lean_smem(int shape, size_t npix, bool agg);
+bool launch_splat_lean(int shape, const SplatLeanArgs& a, const LeanCols& lc, int sms, cudaStream_t st);
 int label_count_shapes();
 size_t label_count_smem(int shape, int code_words, int P);
 bool launch_label_count(int shape, const LabelCountArgs& a, int sms, cudaStream_t st);

@@ -42,7 +42,10 @@ __device__ __forceinline__ long long group_sum(unsigned active, unsigned peers, 
     return (long long)((unsigned long long)s0 + ((unsigned long long)s1 << 22) + ((unsigned long long)s2 << 44));
 }
 
-template <bool AGG, bool SMEM>
+// TOUCH: record the keys whose shared count leaves zero, so that a flush
+// visits only them (the batched passes); the add then needs the old count
+// back, so the single-query passes keep the plain, non-returning add.
+template <bool AGG, bool SMEM, bool TOUCH = false>
 struct Hist {
     uint32_t* s_cnt;
     unsigned long long* s_sum;
@@ -50,12 +53,15 @@ struct Hist {
     unsigned long long* g_sum;
     double* g_nonfinite;
     float scale;
-    // optional: keys whose shared count left zero, so a flush visits only them
     int* s_touched = nullptr;
     int* s_ntouched = nullptr;
     __device__ __forceinline__ void count(int p, unsigned c) const {
-        const unsigned old = atomicAdd(s_cnt + p, c);
-        if (s_touched && old == 0u) s_touched[atomicAdd(s_ntouched, 1)] = p;
+        if (TOUCH) {
+            const unsigned old = atomicAdd(s_cnt + p, c);
+            if (old == 0u) s_touched[atomicAdd(s_ntouched, 1)] = p;
+        } else {
+            atomicAdd(s_cnt + p, c);
+        }
     }
     __device__ __forceinline__ long long fixq(int p, float v) const {
         if (!isfinite(v)) {

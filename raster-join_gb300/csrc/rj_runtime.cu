@@ -80,8 +80,12 @@ void dev_free(rj_ctx* ctx, DevBuf& b) {
     b.bytes = 0;
 }
 
+DevBuf& scratch_buf(rj_ctx* ctx, const char* key) {
+    return ctx->scratch_ns.empty() ? ctx->scratch[key] : ctx->scratch[std::string(key) + ctx->scratch_ns];
+}
+
 int scratch(rj_ctx* ctx, const char* key, size_t bytes, void** out) {
-    DevBuf& b = ctx->scratch[key];
+    DevBuf& b = scratch_buf(ctx, key);
     int rc = dev_alloc(ctx, b, bytes);
     if (rc) return rc;
     *out = b.p;
@@ -556,7 +560,7 @@ int build_exact(rj_ctx* ctx, int user_res, ExactIndex& ix, int max_scale = 1024)
         if ((rc = scratch_t(ctx, "cls_entries", std::max<size_t>(xc.nentries, 1), &entries2))) return rc;
         if ((rc = scratch_t(ctx, "cls_edges", std::max<size_t>(xc.nedges, 1), &edges))) return rc;
     }
-    ix.code = (const uint32_t*)ctx->scratch["cls_code"].p;
+    ix.code = (const uint32_t*)scratch_buf(ctx, "cls_code").p;
     ix.cell_start = start2;
     ix.entries = entries2;
     ix.edges = edges;
@@ -581,7 +585,7 @@ PointArgs make_point_args(rj_ctx* ctx, const DevFilter& f, unsigned long long* o
     pa.P = ctx->ps->P;
     pa.out_count = oc;
     pa.out_sum = os;
-    pa.out_nonfinite = (double*)ctx->scratch["out_nonfinite"].p;
+    pa.out_nonfinite = (double*)scratch_buf(ctx, "out_nonfinite").p;
     pa.err = ctx->d_err;
     pa.shape = ctx->point_shape;
     pa.wait_ns = ctx->wait_ns;
@@ -1196,6 +1200,75 @@ int hybrid_lean_pass(rj_ctx* ctx, const DevFilter& f, int mode, const HybXf& h, 
     return RJ_OK;
 }
 
+// Lean point pass onto the point canvas (rj_splat_kernels.cu): one canvas
+// tile, a resident table, interval-form filters on at most four columns,
+// count or sum.  The shape (canvas copies in shared memory, or atomics
+// straight into the canvas; block size) is the one forced with rj_set_tuning
+// (RJ_TUNE_COUNT_SHAPE), else autotuned per query class.  Tuning runs write
+// into the canvas, which is cleared again after them.  *done = false: the
+// pass does not apply (the caller takes the generic splat).
+int splat_lean_pass(rj_ctx* ctx, const DevFilter& f, const RasterPlan& rp, uint32_t* canvas_c, long long* canvas_s,
+                    ExecState& es, bool* done) {
+    *done = false;
+    ctx->last_count_shape = ctx->last_count_bshift = -1;
+    if (rp.splitx != 1 || rp.splity != 1 || ctx->streamed) return RJ_OK;
+    if (f.general || f.ncol > label_lean_max_cols()) return RJ_OK;
+    PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
+    if (((uintptr_t)pa.xy & 15) != 0) return RJ_OK;
+    LeanCols lc{};
+    if (!lean_cols_of(pa, es.out_sum, lc)) return RJ_OK;
+    SplatLeanArgs a{};
+    a.xy = reinterpret_cast<const float4*>(pa.xy);
+    a.n = pa.n;
+    a.col0 = rp.colxf[0];
+    a.row0 = rp.rowxf[0];
+    a.resx = rp.resx;
+    a.resy = rp.resy;
+    a.canvas_c = canvas_c;
+    a.canvas_s = reinterpret_cast<unsigned long long*>(canvas_s);
+    a.zones = pa.zones;
+    a.zrow0 = pa.row0;
+    a.qbox = pa.qbox;
+    const size_t npix = (size_t)rp.resx * rp.resy;
+    const bool agg = lc.aggr != 0;
+    std::vector<int> cands;
+    for (int sh = 0; sh < splat_lean_shapes(); ++sh)
+        if (ctx->count_shape < 0 || ctx->count_shape == sh) {
+            const size_t sm = splat_lean_smem(sh, npix, agg);
+            if (sm > 0 && sm <= 200 * 1024) cands.push_back(sh);
+        }
+    if (cands.empty()) return RJ_OK;
+    char key[200];
+    std::snprintf(key, sizeof key, "splat:%d:%d:%d:%d:%d:%d", lc.ncol, lc.aggr, lc.aggr_ci >= 0,
+                  tune_bucket((double)npix), tune_bucket((double)a.n), ctx->count_shape);
+    int tuned_i = -1;
+    const bool have = tuned_get(ctx, key, &tuned_i);
+    const bool small = a.n < kTuneMinPoints;
+    bool timed_any = false;
+    const int pi = small && !have ? 0 : tune_pick(ctx, key, cands.size(), [&](size_t i) {
+        timed_any = true;
+        SplatLeanArgs w = a;
+        w.n = std::min<uint64_t>(a.n & ~1ULL, 1ULL << 16);   // first launch of a shape loads it
+        if (!launch_splat_lean(cands[i], w, lc, ctx->sms, ctx->stream)) return false;
+        SplatLeanArgs b = a;
+        b.n = std::min<uint64_t>(a.n & ~1ULL, 1ULL << 27);
+        return launch_splat_lean(cands[i], b, lc, ctx->sms, ctx->stream);
+    });
+    RJ_CUDA(cudaGetLastError());
+    if (timed_any) {
+        RJ_CUDA(cudaMemsetAsync(canvas_c, 0, npix * sizeof(uint32_t), ctx->stream));
+        if (canvas_s) RJ_CUDA(cudaMemsetAsync(canvas_s, 0, npix * sizeof(long long), ctx->stream));
+    }
+    if (pi < 0) return RJ_OK;
+    ctx->passes = 1;
+    ctx->copy_ms = 0;
+    if (!launch_splat_lean(cands[(size_t)pi], a, lc, ctx->sms, ctx->stream)) return RJ_OK;
+    RJ_CUDA(cudaGetLastError());
+    ctx->last_count_shape = cands[(size_t)pi];
+    *done = true;
+    return RJ_OK;
+}
+
 // Raster join (RasterJoin::performJoin RasterJoin.cpp:196-243) and the
 // error-bounds join (RasterJoinBounds::performJoin RasterJoinBounds.cpp:306-381).
 int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
@@ -1218,8 +1291,8 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
     int2* wv;
     float2* wf;
     if ((rc = transform_vertices(ctx, rp.colxf, rp.rowxf, &wv, &wf, bounds))) return rc;
-    const float4* dcol = (const float4*)ctx->scratch["colxf"].p;
-    const float4* drow = (const float4*)ctx->scratch["rowxf"].p;
+    const float4* dcol = (const float4*)scratch_buf(ctx, "colxf").p;
+    const float4* drow = (const float4*)scratch_buf(ctx, "rowxf").p;
     CanvasXf cx = make_canvas_xf(ctx, rp, dcol, drow);
 
     PolyPassArgs a{};
@@ -1238,7 +1311,7 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
 
     const uint64_t ckey = canvas_key(rp.colxf, rp.rowxf, rp.resx, rp.resy);
     const uint64_t rows = std::min(ctx->row1, ctx->npts) - std::min(ctx->row0, ctx->npts);
-    if (!bounds && use_tier(npix, rows) && !(q->flags & RJ_FLAG_FLAT_CANVAS))
+    if (!bounds && query_tier(q->flags, npix, rows))
         return exec_raster_tier(ctx, q, rp, f, es, a, cx, ckey);
     bool use_label = !bounds && !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->ps->overlap_on(ckey) != 1 &&
                      ctx->ps->P <= kMaxLabelPolys;
@@ -1271,9 +1344,11 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
         if ((rc = scratch_t(ctx, "canvas_s", npix, &canvas_s))) return rc;
         RJ_CUDA(cudaMemsetAsync(canvas_s, 0, npix * sizeof(long long), ctx->stream));
     }
-    if ((rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
-             launch_raster_splat(pa, cx, canvas_c, canvas_s, ctx->sms, ctx->stream);
-         })))
+    bool lean = false;
+    if ((rc = splat_lean_pass(ctx, f, rp, canvas_c, canvas_s, es, &lean))) return rc;
+    if (!lean && (rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
+                      launch_raster_splat(pa, cx, canvas_c, canvas_s, ctx->sms, ctx->stream);
+                  })))
         return rc;
     RJ_CUDA(cudaGetLastError());
     es.ph->mark(3);
@@ -1672,6 +1747,15 @@ int enqueue_query(rj_ctx* ctx, const rj_query* q, Phase& ph, unsigned long long*
     *pob = ob;
     return RJ_OK;
 }
+
+namespace rjh {
+int enqueue_query_untimed(rj_ctx* ctx, const rj_query* q, unsigned long long** oc, unsigned long long** os,
+                          double** onf, long long** ob) {
+    Phase ph(ctx, false);
+    double t_setup = 0;
+    return enqueue_query(ctx, q, ph, oc, os, onf, ob, &t_setup);
+}
+}  // namespace rjh
 
 // ===========================================================================
 // C ABI
@@ -2277,6 +2361,7 @@ int rj_get_tuning(const rj_ctx* ctx, int32_t knob, int32_t* value) {
         case RJ_TUNE_HYBRID_EXACT_SCALE: *value = ctx->hybrid_exact_scale; return RJ_OK;
         case RJ_TUNE_COUNT_SHAPES: *value = label_count_shapes(); return RJ_OK;
         case RJ_TUNE_LEAN_SHAPES: *value = label_lean_shapes(); return RJ_OK;
+        case RJ_TUNE_SPLAT_SHAPES: *value = splat_lean_shapes(); return RJ_OK;
         case RJ_TUNE_WAIT_LIMIT: *value = (int32_t)std::min<uint64_t>(ctx->wait_ns / 1000ull, 0x7FFFFFFFull); return RJ_OK;
         default: return RJ_E_INVALID;
     }

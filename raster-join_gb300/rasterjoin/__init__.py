@@ -36,10 +36,11 @@ RJ_PENDING = 1
 SUM_SHIFT_AUTO = -2147483648
 # rj_set_tuning knobs (include/rj.h)
 TUNE_POINT_SHAPE, TUNE_COUNT_SHAPE, TUNE_COUNT_BLOCK_SHIFT, TUNE_HYBRID_EXACT_SCALE = 0, 1, 2, 3
-TUNE_COUNT_SHAPES, TUNE_LEAN_SHAPES, TUNE_WAIT_LIMIT = 4, 5, 6
+TUNE_COUNT_SHAPES, TUNE_LEAN_SHAPES, TUNE_WAIT_LIMIT, TUNE_SPLAT_SHAPES = 4, 5, 6, 7
 BATCH_AUTOTUNE = 0x1
 BATCH_NO_FUSE = 0x2
 BATCH_FUSE_ALL = 0x4
+BATCH_FUSE = 0x8
 MAX_CONSTRAINTS = 10
 
 FLAG_COMPAT_INDEX_CLAMP = 0x1
@@ -50,6 +51,7 @@ FLAG_PHASE_TIMING = 0x10
 FLAG_NO_CELL_CLASSIFY = 0x20
 FLAG_NO_CACHE = 0x40
 FLAG_FLAT_CANVAS = 0x80
+FLAG_TIERED_CANVAS = 0x100
 
 
 class RJError(RuntimeError):
@@ -634,7 +636,7 @@ class GLHandler:
         for i, ps in enumerate(polysets):
             sa[i] = ps.ptr if ps is not None else None
             P = ps.P if ps is not None else len(self.dataHandler.polys[1]) - 1
-            bufs.append(_ResultBuffers(P))
+            bufs.append(_ResultBuffers(P, bounds=queries[i].function_type == RasterJoinBoundFn))
         ra = (Result * max(n, 1))()
         for i, b in enumerate(bufs):
             ra[i] = b.r

@@ -107,7 +107,7 @@ def test_batch_equals_single_and_oracle(setup, table):
     h, sets, raw = setup
     mix = query_mix()
     alone = [single(h, sets[s], q) for s, q in mix]
-    res, status, stats = h.execute_batch([q for _, q in mix], [sets[s] for s, _ in mix])
+    res, status, stats = h.execute_batch([q for _, q in mix], [sets[s] for s, _ in mix], flags=rj.BATCH_FUSE)
     assert (status == 0).all()
     assert stats["fused"] == len(mix) and stats["fallback"] == 0
     for (c, s), r in zip(alone, res):
@@ -138,7 +138,7 @@ def test_batch_mixed_join_types_fall_back(setup):
           make_query(20.0, preds=((4, rj.GTE, 3),), flags=rj.FLAG_COMPAT_FLOAT_EQ)]
     ss = [sets[0], sets[3], sets[0], sets[3], sets[1]]
     alone = [single(h, s, q) for s, q in zip(ss, qs)]
-    res, status, stats = h.execute_batch(qs, ss)
+    res, status, stats = h.execute_batch(qs, ss, flags=rj.BATCH_FUSE)
     assert (status == 0).all()
     assert stats["fused"] == 1 and stats["fallback"] == 4
     for (c, s), r in zip(alone, res):
@@ -149,8 +149,9 @@ def test_batch_mixed_join_types_fall_back(setup):
 def test_batch_autotune_same_result(setup):
     h, sets, _ = setup
     mix = query_mix()
-    base, _, _ = h.execute_batch([q for _, q in mix], [sets[s] for s, _ in mix])
-    tuned, status, stats = h.execute_batch([q for _, q in mix], [sets[s] for s, _ in mix], flags=rj.BATCH_AUTOTUNE)
+    base, _, _ = h.execute_batch([q for _, q in mix], [sets[s] for s, _ in mix], flags=rj.BATCH_FUSE)
+    tuned, status, stats = h.execute_batch([q for _, q in mix], [sets[s] for s, _ in mix],
+                                           flags=rj.BATCH_FUSE | rj.BATCH_AUTOTUNE)
     assert (status == 0).all() and stats["tuned"] == 1
     for a, b in zip(base, tuned):
         np.testing.assert_array_equal(a.count, b.count)
@@ -160,7 +161,7 @@ def test_batch_autotune_same_result(setup):
 def test_batch_no_fuse_equals_fused(setup):
     h, sets, _ = setup
     mix = query_mix()
-    fused, _, _ = h.execute_batch([q for _, q in mix], [sets[s] for s, _ in mix])
+    fused, _, _ = h.execute_batch([q for _, q in mix], [sets[s] for s, _ in mix], flags=rj.BATCH_FUSE)
     plain, status, stats = h.execute_batch([q for _, q in mix], [sets[s] for s, _ in mix], flags=rj.BATCH_NO_FUSE)
     assert (status == 0).all() and stats["fused"] == 0
     for a, b in zip(fused, plain):
@@ -281,7 +282,7 @@ def test_batch_tiered_canvases(setup):
         C.pointer(q2)[0] = q
         q2.flags = rj.FLAG_FLAT_CANVAS
         flat.append(single(h, s, q2))
-    res, status, stats = h.execute_batch(qs, ss)
+    res, status, stats = h.execute_batch(qs, ss, flags=rj.BATCH_FUSE)
     assert (status == 0).all() and stats["fused"] == len(qs) and stats["fallback"] == 0
     for (c, sm), r in zip(flat, res):
         np.testing.assert_array_equal(r.count, c)
@@ -289,9 +290,10 @@ def test_batch_tiered_canvases(setup):
 
 
 def test_point_heavy_label_queries_leave_the_fused_pass(built):
-    """Label-map queries over >= 2^22 rows run through rj_execute's lean pass
-    inside a batch (counted as fallback); RJ_BATCH_FUSE_ALL keeps them fused.
-    Both give the single-query results bit for bit."""
+    """With RJ_BATCH_FUSE, single-tile queries over >= 2^22 rows leave the
+    fused pass for rj_execute's lean passes on the lanes (counted as
+    fallback); RJ_BATCH_FUSE_ALL keeps them fused.  Both give the
+    single-query results bit for bit."""
     big = synth.points(5_000_001, seed=78, columns=True)
     v, p = poly_sets()[0]
     h = rj.GLHandler()
@@ -302,7 +304,7 @@ def test_point_heavy_label_queries_leave_the_fused_pass(built):
         qs = [make_query(20.0), make_query(30.0, aggr=True, preds=((4, rj.GT, 2),)),
               make_query(20.0, max_fbo=1000)]                     # a multi-tile canvas stays fused
         alone = [single(h, ps, q) for q in qs]
-        res, status, stats = h.execute_batch(qs, [ps] * 3)
+        res, status, stats = h.execute_batch(qs, [ps] * 3, flags=rj.BATCH_FUSE)
         assert (status == 0).all() and stats["fused"] == 1 and stats["fallback"] == 2
         res2, status2, stats2 = h.execute_batch(qs, [ps] * 3, flags=rj.BATCH_FUSE_ALL)
         assert (status2 == 0).all() and stats2["fused"] == 3 and stats2["fallback"] == 0
@@ -314,3 +316,26 @@ def test_point_heavy_label_queries_leave_the_fused_pass(built):
         ps.close()
     finally:
         h.close()
+
+
+def test_lanes_equal_single(setup):
+    """The default route: every raster query (and the error-bounds query)
+    runs rj_execute's device path on the lanes -- four streams with their own
+    scratch -- and gives the single-query results bit for bit, bounds
+    included; the other join types still run through rj_execute in turn."""
+    h, sets, _ = setup
+    mix = query_mix() + [(3, make_query(20.0, fn=rj.RasterJoinBoundFn)), (0, make_query(20.0, fn=rj.IndexJoinFn)),
+                         (1, make_query(6.0, fn=rj.RasterJoinBoundFn, window=(T0, T0 + 90 * DAY)))]
+    alone = []
+    for s, q in mix:
+        h.usePolySet(sets[s])
+        r = h.execute(q.function_type, query=q)
+        alone.append((r.count.copy(), r.sum.copy(), None if r.bounds is None else r.bounds.copy()))
+    for rnd in range(2):                                   # the second round reuses the lanes' scratch
+        res, status, stats = h.execute_batch([q for _, q in mix], [sets[s] for s, _ in mix])
+        assert (status == 0).all() and stats["fused"] == 0 and stats["fallback"] == len(mix)
+        for (c, sm, b), r in zip(alone, res):
+            np.testing.assert_array_equal(r.count, c)
+            np.testing.assert_array_equal(r.sum, sm)
+            if b is not None:
+                np.testing.assert_array_equal(r.bounds, b)

@@ -73,14 +73,15 @@ def test_in_place_reload_keeps_the_plan(handler, data):
     """rj_load_points with the same columns and size copies into the plan's
     buffers: a replay joins the new rows (equal to a fresh rj_execute)."""
     pts, verts, pidx = data
-    handler.setDataHandler(_dh(pts, verts, pidx))
+    dh = _dh(pts, verts, pidx)
+    handler.setDataHandler(dh)
     handler.setCellSize(10.0)
     handler.flags = rj.FLAG_NO_CACHE
     try:
         plan = handler.prepare(rj.RasterJoinFn)
         try:
             other = synth.points(len(pts["xy"]), seed=52)["xy"]
-            handler.setDataHandler(_dh(pts, verts, pidx, xy=other))
+            dh.add_column(1, rj.Location, other)          # the same polygons stay on the device
             handler.upload()                              # same layout: copied in place
             got = plan.execute()
             want = handler.execute(rj.RasterJoinFn)
@@ -123,19 +124,18 @@ def test_reload_refuses_plans_narrowed_by_the_time_index(handler, data):
     """A reload in place drops the time index: a plan whose rows it narrowed
     is refused, a plan over every row stays valid."""
     pts, verts, pidx = data
-    handler.setDataHandler(_dh(pts, verts, pidx))
+    dh = _dh(pts, verts, pidx)
+    handler.setDataHandler(dh)
     handler.upload(force=True)
     handler.buildTimeIndex(2)
     handler.setCellSize(10.0)
     try:
         plan_all = handler.prepare(rj.RasterJoinFn)
-        dh = _dh(pts, verts, pidx)
         dh.setTimeRange(2, synth.T0, synth.T0 + synth.YEAR // 4)
-        handler.setDataHandler(dh)
         plan_t = handler.prepare(rj.RasterJoinFn)
         try:
             other = synth.points(len(pts["xy"]), seed=53)["xy"]
-            handler.setDataHandler(_dh(pts, verts, pidx, xy=other))
+            dh.add_column(1, rj.Location, other)
             handler.upload()                              # same layout: copied in place
             got = plan_all.execute()
             np.testing.assert_array_equal(got.count, oracle.raster_join(other, verts, pidx, 10.0)[0])
