@@ -713,12 +713,13 @@ def run_config2(args, rj, torch, local, join, pts, verts, pidx):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.c2_steps
     res = h.last
+    shape = h.getTuning(rj.TUNE_COUNT_SHAPE)              # the lean pass's autotuned shape (-1: generic pass)
     h.close()
     peak, _ = measured_peaks()
     mean_pt = float(np.mean(pt))
     achieved = (n * C2_BYTES_PER_POINT / 1e9) / (mean_pt / 1e3)
     out = {"workload": C2_WORKLOAD, "join": join, "gpoints_s": n / ms / 1e6, "ms_per_step": ms,
-           "point_pass_ms": mean_pt,
+           "point_pass_ms": mean_pt, "lean_shape": shape,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "traffic": profiled_traffic(join, n)}}
     return out, res

@@ -434,6 +434,12 @@ typedef struct {
     int64_t canvas_mb;             /* device memory per slot (0 = 8192)         */
     int32_t max_batch;             /* requests per batch (0 = 256)              */
     double max_wait_ms;            /* hold a batch open for more arrivals (0 = launch at once) */
+    uint32_t batch_flags;          /* how a slot runs its batch: 0 = the lanes
+                                      (each request's own device path on four
+                                      streams of the slot, whose scratch is
+                                      allocated on first use), RJ_BATCH_FUSE =
+                                      the fused pass in the slot's fixed arena
+                                      (nothing allocated while serving)       */
 } rj_server_config;
 typedef struct {
     double submit_ms, start_ms, done_ms;   /* steady-clock milliseconds            */

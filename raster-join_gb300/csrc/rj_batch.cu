@@ -14,6 +14,7 @@
 // every queued request that fits its arena when it becomes free, so batches
 // grow with the arrival rate and slots overlap on the device.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstdarg>
@@ -71,8 +72,8 @@ struct Engine {
     size_t h_pin_bytes = 0;
     BatchShape shape{256, 16384, 1};
     bool tuned = false;
-    bool lanes = false;          // rj_execute_batch's engine; a serving slot (fixed
-                                 // arena, no allocation while serving) runs them in turn
+    bool lanes = false;          // may queue queries on the lanes
+    int id = 0;                  // names the lanes' scratch apart from other engines'
     cudaStream_t lane_st[kLanes]{};
     int* lane_err = nullptr;     // device: one error word per lane
     cudaEvent_t lane_ev = nullptr;
@@ -80,9 +81,12 @@ struct Engine {
     size_t lane_pin_bytes = 0;
 };
 
+std::atomic<int> g_engine_ids{0};
+
 int engine_init(rj_ctx* ctx, Engine& e, cudaStream_t st, size_t cap) {
     e.ctx = ctx;
     e.cap = cap;
+    e.id = g_engine_ids.fetch_add(1);
     if (st) {
         e.st = st;
     } else {
@@ -853,7 +857,7 @@ int lanes_enqueue(Engine& e, LaneRun& lr, int& launches) {
         const int l = it != lane_of.end() ? it->second : (lane_of[p.ps] = (next++) % kLanes);
         ctx->stream = e.lane_st[l];
         ctx->d_err = e.lane_err + l;
-        ctx->scratch_ns = "#lane" + std::to_string(l);
+        ctx->scratch_ns = "#e" + std::to_string(e.id) + "." + std::to_string(l);
         ctx->ps = p.ps;
         unsigned long long *oc = nullptr, *os = nullptr;
         double* onf = nullptr;
@@ -935,8 +939,7 @@ int execute_batch(Engine& e, int nq, const rj_query* qs, const rj_query* const* 
     const double t0 = now_ms();
     std::vector<QPlan> plans(nq);
     g_kernel_launches = 0;
-    // rj_execute_batch's engine sends every raster query to the lanes unless
-    // the fused pass is asked for; a serving slot fuses
+    // every raster query goes to the lanes unless the fused pass is asked for
     const bool lanes_all = e.lanes && !(flags & (RJ_BATCH_FUSE | RJ_BATCH_FUSE_ALL | RJ_BATCH_NO_FUSE));
     {
         std::lock_guard<std::recursive_mutex> lock(ctx->mu);
@@ -1123,7 +1126,8 @@ void server_worker(rj_server* s, Engine* e) {
             sp[i] = batch[i]->ps;
             rp[i] = batch[i]->res;
         }
-        execute_batch(*e, n, nullptr, qp.data(), sp.data(), nullptr, rp.data(), st.data(), 0, nullptr);
+        execute_batch(*e, n, nullptr, qp.data(), sp.data(), nullptr, rp.data(), st.data(), s->cfg.batch_flags,
+                      nullptr);
         {
             std::lock_guard<std::mutex> lk(s->mu);
             const double t = now_ms();
@@ -1381,7 +1385,9 @@ int rj_server_create(rj_ctx* ctx, const rj_server_config* cfg, rj_server** out) 
     for (int i = 0; i < s->cfg.slots; ++i) {
         Engine* e = new Engine();
         int rc = engine_init(ctx, *e, nullptr, cap);
-        if (!rc) rc = dev_alloc(ctx, e->ar.buf, cap);
+        e->lanes = !(s->cfg.batch_flags & (RJ_BATCH_FUSE | RJ_BATCH_FUSE_ALL | RJ_BATCH_NO_FUSE));
+        // the fused pass works in the slot's fixed arena; the lanes in scratch
+        if (!rc && !e->lanes) rc = dev_alloc(ctx, e->ar.buf, cap);
         if (rc) {
             engine_free(*e);
             delete e;

@@ -96,17 +96,47 @@ __device__ __forceinline__ int hyb_classify(const HybLeanArgs& a, const uint16_t
 
 }  // namespace
 
-template <int BLOCK, int NV, int NCOL, bool AGG>
-__global__ void __launch_bounds__(BLOCK) k_hybrid_lean(HybLeanArgs a, LeanCols lc) {
+// A classified point: a labelled one into the histogram, a border one into
+// the block's queue (one reservation per warp: ballot + prefix; every lane of
+// the warp calls this).
+template <bool AGG>
+__device__ __forceinline__ void hyb_take(const LeanHist<AGG>& hist, int* qn, float* qx, float* qy, float* qv,
+                                         int lane, int kind, uint32_t lab, float x, float y, float val) {
+    if (kind == 1) hist.add((int)lab, val);
+    const unsigned m = __ballot_sync(0xffffffffu, kind == 2);
+    if (m) {
+        int at = 0;
+        if (lane == 0) at = atomicAdd(qn, __popc(m));
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if (kind == 2) {
+            const int s = at + __popc(m & ((1u << lane) - 1u));
+            qx[s] = x;
+            qy[s] = y;
+            qv[s] = val;
+        }
+    }
+}
+
+// COMPACT: the points that pass the filters are first packed per warp into
+// shared memory (ballot + prefix), then classified and counted 32 at a time,
+// so that the pixel, label and histogram work runs on full warps even when
+// the filters drop most points.
+template <int BLOCK, int NV, int NCOL, bool AGG, bool COMPACT>
+__device__ __forceinline__ void hybrid_lean_body(const HybLeanArgs& a, const LeanCols& lc) {
     extern __shared__ uint32_t s_words[];
     constexpr int HW = AGG ? 3 : 1;
     constexpr int QCAP = BLOCK * (1 + 2 * NV);        // < BLOCK left over + every point of one iteration
+    constexpr int WCAP = 32 * 2 * NV;                 // one warp's points of one iteration
     uint32_t* s_code = s_words;
     uint32_t* s_hist = s_code + a.code_words;          // lc.copies x HW x P
     float* qx = reinterpret_cast<float*>(s_hist + lc.copies * HW * a.P);
     float* qy = qx + QCAP;
     float* qv = qy + QCAP;
     int* qn = reinterpret_cast<int*>(qv + QCAP);
+    // per-warp staging of the points that pass the filters (COMPACT)
+    float* wx = reinterpret_cast<float*>(qn + 4) + (threadIdx.x >> 5) * WCAP * (AGG ? 3 : 2);
+    float* wy = wx + WCAP;
+    float* wv = wy + WCAP;
     {
         const uint32_t* g = reinterpret_cast<const uint32_t*>(a.codes);
         for (int i = threadIdx.x; i < a.code_words; i += BLOCK) s_code[i] = __ldg(g + i);
@@ -149,6 +179,7 @@ __global__ void __launch_bounds__(BLOCK) k_hybrid_lean(HybLeanArgs a, LeanCols l
                 for (int c = 0; c < NCOL; ++c) cv[c][k] = live ? __ldcs(lc.col[c] + i) : make_uint2(0u, 0u);
                 if (AGG) av[k] = (live && lc.aggr_ci < 0) ? __ldcs(lc.aggr_col + i) : make_uint2(0u, 0u);
             }
+            int nst = 0;                               // staged points of this warp (COMPACT)
             #pragma unroll
             for (int j = 0; j < 2 * NV; ++j) {
                 const int k = j >> 1;
@@ -166,22 +197,34 @@ __global__ void __launch_bounds__(BLOCK) k_hybrid_lean(HybLeanArgs a, LeanCols l
                         if (cc == lc.aggr_ci) raw = v[cc];
                     val = agg_value(lc.aggr_typ, raw);
                 }
-                uint32_t lab = 0;
-                const int kind = hyb_pass<NCOL>(lc, v) ? hyb_classify(a, sc, x, y, lab) : 0;
-                if (kind == 1) hist.add((int)lab, val);
-                // border points: one queue reservation per warp
-                const unsigned m = __ballot_sync(0xffffffffu, kind == 2);
-                if (m) {
-                    int at = 0;
-                    if (lane == 0) at = atomicAdd(qn, __popc(m));
-                    at = __shfl_sync(0xffffffffu, at, 0);
-                    if (kind == 2) {
-                        const int s = at + __popc(m & ((1u << lane) - 1u));
-                        qx[s] = x;
-                        qy[s] = y;
-                        qv[s] = val;
+                if (COMPACT) {
+                    const bool ok = hyb_pass<NCOL>(lc, v);
+                    const unsigned m = __ballot_sync(0xffffffffu, ok);
+                    if (ok) {
+                        const int s = nst + __popc(m & ((1u << lane) - 1u));
+                        wx[s] = x;
+                        wy[s] = y;
+                        if (AGG) wv[s] = val;
                     }
+                    nst += __popc(m);
+                } else {
+                    uint32_t lab = 0;
+                    const int kind = hyb_pass<NCOL>(lc, v) ? hyb_classify(a, sc, x, y, lab) : 0;
+                    hyb_take<AGG>(hist, qn, qx, qy, qv, lane, kind, lab, x, y, val);
                 }
+            }
+            if (COMPACT) {
+                __syncwarp();
+                for (int kb = 0; kb < nst; kb += 32) {
+                    const int k = kb + lane;
+                    const bool live = k < nst;
+                    const float x = live ? wx[k] : 0.f, y = live ? wy[k] : 0.f;
+                    const float val = (AGG && live) ? wv[k] : 0.f;
+                    uint32_t lab = 0;
+                    const int kind = live ? hyb_classify(a, sc, x, y, lab) : 0;
+                    hyb_take<AGG>(hist, qn, qx, qy, qv, lane, kind, lab, x, y, val);
+                }
+                __syncwarp();
             }
         }
         // drain full blocks of queued points, one point per thread
@@ -236,6 +279,18 @@ __global__ void __launch_bounds__(BLOCK) k_hybrid_lean(HybLeanArgs a, LeanCols l
     }
 }
 
+template <int BLOCK, int NV, int NCOL, bool AGG, bool COMPACT>
+__global__ void __launch_bounds__(BLOCK) k_hybrid_lean(HybLeanArgs a, LeanCols lc) {
+    hybrid_lean_body<BLOCK, NV, NCOL, AGG, COMPACT>(a, lc);
+}
+
+// The same pass with a register budget of two blocks per SM (64 registers at
+// 512 threads): no spills, fewer resident warps.  The tuner decides.
+template <int BLOCK, int NV, int NCOL, bool AGG, bool COMPACT>
+__global__ void __launch_bounds__(BLOCK, 2) k_hybrid_lean_r2(HybLeanArgs a, LeanCols lc) {
+    hybrid_lean_body<BLOCK, NV, NCOL, AGG, COMPACT>(a, lc);
+}
+
 // 16-bit cell labels of the classified grid for the lean pass (mode 1).
 __global__ void k_cell_labels(const uint32_t* __restrict__ code, int ncells, uint16_t* __restrict__ label) {
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += gridDim.x * blockDim.x) {
@@ -258,16 +313,23 @@ using HybKernel = void (*)(HybLeanArgs, LeanCols);
 struct HybShape {
     int block;
     int nv;
+    bool compact;
 };
-constexpr HybShape kHybShapes[] = {{512, 2}, {1024, 2}, {256, 4}};
+// 3 and 6: the register budget of two blocks per SM
+constexpr HybShape kHybShapes[] = {{512, 2, false}, {1024, 2, false}, {256, 4, false}, {512, 2, false},
+                                   {512, 2, true},  {256, 4, true},   {512, 2, true}};
 constexpr int kNumHybShapes = (int)(sizeof(kHybShapes) / sizeof(kHybShapes[0]));
 
 template <int NCOL, bool AGG>
 HybKernel pick_hyb(int shape) {
     switch (shape) {
-        case 0: return k_hybrid_lean<512, 2, NCOL, AGG>;
-        case 1: return k_hybrid_lean<1024, 2, NCOL, AGG>;
-        default: return k_hybrid_lean<256, 4, NCOL, AGG>;
+        case 0: return k_hybrid_lean<512, 2, NCOL, AGG, false>;
+        case 1: return k_hybrid_lean<1024, 2, NCOL, AGG, false>;
+        case 2: return k_hybrid_lean<256, 4, NCOL, AGG, false>;
+        case 3: return k_hybrid_lean_r2<512, 2, NCOL, AGG, false>;
+        case 4: return k_hybrid_lean<512, 2, NCOL, AGG, true>;
+        case 5: return k_hybrid_lean<256, 4, NCOL, AGG, true>;
+        default: return k_hybrid_lean_r2<512, 2, NCOL, AGG, true>;
     }
 }
 
@@ -301,7 +363,8 @@ size_t hybrid_lean_smem(int shape, int code_words, int P, bool agg) {
     if (shape < 0 || shape >= kNumHybShapes) return 0;
     const HybShape& s = kHybShapes[shape];
     const size_t qcap = (size_t)s.block * (1 + 2 * s.nv);
-    return (size_t)code_words * 4 + (size_t)hyb_copies(shape, P, agg) * P * (agg ? 3 : 1) * 4 + qcap * 12 + 16;
+    const size_t stage = s.compact ? (size_t)s.block * 2 * s.nv * (agg ? 3 : 2) * 4 : 0;   // per-warp staging
+    return (size_t)code_words * 4 + (size_t)hyb_copies(shape, P, agg) * P * (agg ? 3 : 1) * 4 + qcap * 12 + 16 + stage;
 }
 
 bool launch_hybrid_lean(int shape, const HybLeanArgs& a, const LeanCols& lc_in, int sms, cudaStream_t st) {

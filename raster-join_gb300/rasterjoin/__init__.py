@@ -112,7 +112,7 @@ class BatchStats(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("slots", C.c_int32), ("canvas_mb", C.c_int64), ("max_batch", C.c_int32),
-                ("max_wait_ms", C.c_double)]
+                ("max_wait_ms", C.c_double), ("batch_flags", C.c_uint32)]
 
 
 class RequestInfo(C.Structure):
@@ -291,10 +291,10 @@ class Server:
     submit(query, polyset) -> ticket; poll(ticket, timeout_ms) -> (JoinResult,
     info dict) or None while pending."""
 
-    def __init__(self, handler, slots=0, canvas_mb=0, max_batch=0, max_wait_ms=0.0):
+    def __init__(self, handler, slots=0, canvas_mb=0, max_batch=0, max_wait_ms=0.0, batch_flags=0):
         self.handler = handler
         self.lib = handler.lib
-        cfg = ServerConfig(slots, canvas_mb, max_batch, max_wait_ms)
+        cfg = ServerConfig(slots, canvas_mb, max_batch, max_wait_ms, batch_flags)
         h = C.c_void_p()
         handler._check(self.lib.rj_server_create(handler.ctx, C.byref(cfg), C.byref(h)))
         self.ptr = h

@@ -193,12 +193,14 @@ def test_time_index_preserves_results(table, built):
         h.close()
 
 
-def test_server_results_alone_and_in_mix(setup):
-    """Requests submitted while others run give the result they give alone."""
+@pytest.mark.parametrize("batch_flags", [0, rj.BATCH_FUSE])
+def test_server_results_alone_and_in_mix(setup, batch_flags):
+    """Requests submitted while others run give the result they give alone,
+    on the lanes (default) and through the fused pass."""
     h, sets, _ = setup
     mix = query_mix()
     alone = [single(h, sets[s], q) for s, q in mix]
-    srv = h.server(slots=2, canvas_mb=2048, max_batch=8)
+    srv = h.server(slots=2, canvas_mb=2048, max_batch=8, batch_flags=batch_flags)
     try:
         tickets = []
         for rep in range(3):
