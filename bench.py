@@ -81,6 +81,9 @@ def parse():
     ap.add_argument("--saturate-qps", type=float, default=5000.0,
                     help="offered rate of the saturation run of the served configuration (0: skip)")
     ap.add_argument("--saturate-requests", type=int, default=4000)
+    ap.add_argument("--saturate-slots", type=int, default=2, help="serving slots of the saturation run")
+    ap.add_argument("--saturate-clients", type=int, default=2,
+                    help="client threads submitting the saturation run's requests (each uploads its polygons)")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--config3", action="store_true",
@@ -368,7 +371,7 @@ def run_batched(rj, h, cum, n, nq):
     }
 
 
-def run_served(rj, h, cum, n, nreq, qps, seed=20261205):
+def run_served(rj, h, cum, n, nreq, qps, seed=20261205, slots=2, clients=1):
     from rasterjoin import workloads as W
     reqs = W.served_requests(nreq, qps, seed=seed)
     rows = [window_rows(cum, *r[4]) for r in reqs]
@@ -392,24 +395,27 @@ def run_served(rj, h, cum, n, nreq, qps, seed=20261205):
         free_at = done[i]
     plain_lat = (done - arrivals) * 1e3
     # ---- served: requests submitted at their arrival times
-    srv = h.server(slots=2, canvas_mb=16384, max_batch=64)
+    srv = h.server(slots=slots, canvas_mb=16384, max_batch=64)
     tickets = [None] * nreq
     arrive_ms = np.zeros(nreq)
     live = []
+    base = time.monotonic()
 
-    def submitter():
-        base = time.monotonic()
-        for i, ((arr, xy, p, cell, win), q) in enumerate(zip(reqs, qs)):
+    def submitter(k):
+        # client k submits requests k, k + clients, ... at their arrival times
+        for i in range(k, nreq, clients):
+            arr, xy, p, cell, win = reqs[i]
             now = time.monotonic() - base
             if arr > now:
                 time.sleep(arr - now)
             arrive_ms[i] = time.monotonic() * 1e3
             ps = h.polyset(xy, p)            # the request's polygons go to the device on arrival
             live.append(ps)
-            tickets[i] = srv.submit(q, ps)
+            tickets[i] = srv.submit(qs[i], ps)
 
-    th = threading.Thread(target=submitter)
-    th.start()
+    ths = [threading.Thread(target=submitter, args=(k,)) for k in range(clients)]
+    for th in ths:
+        th.start()
     lat, sizes, last_done = [], [], 0.0
     for i in range(nreq):
         while tickets[i] is None:
@@ -418,11 +424,12 @@ def run_served(rj, h, cum, n, nreq, qps, seed=20261205):
         lat.append(info["done_ms"] - arrive_ms[i])
         sizes.append(info["batch_size"])
         last_done = max(last_done, info["done_ms"])
-    th.join()
+    for th in ths:
+        th.join()
     srv.close()
     for ps in live:
         ps.close()
-    span_s = (last_done - arrive_ms[0]) / 1e3
+    span_s = (last_done - arrive_ms.min()) / 1e3
     lat = np.array(lat)
     pct = lambda a, q: float(np.percentile(a, q))
     return {
@@ -438,6 +445,7 @@ def run_served(rj, h, cum, n, nreq, qps, seed=20261205):
                   "method": "each request alone through rj_execute (polygons uploaded, join, results read); "
                             "latency from a FIFO queue over the same arrival times"},
         "latency": "arrival (before the polygon upload) to results in host memory",
+        "slots": slots, "clients": clients,
     }
 
 
@@ -772,16 +780,18 @@ def run_gb300(args):
             line["served"] = run_served(rj, h2, cum, args.table_points, args.served_requests, args.served_qps)
             if args.saturate_qps > 0:
                 sat = run_served(rj, h2, cum, args.table_points, args.saturate_requests, args.saturate_qps,
-                                 seed=20261207)
+                                 seed=20261207, slots=args.saturate_slots, clients=args.saturate_clients)
                 line["served_saturated"] = {
                     "offered_qps": args.saturate_qps, "achieved_qps": sat["achieved_qps"],
                     "plain_max_qps": sat["plain"]["max_qps"],
                     "throughput_vs_plain": sat["achieved_qps"] / sat["plain"]["max_qps"],
                     "p50_ms": sat["p50_ms"], "p99_ms": sat["p99_ms"], "mean_batch": sat["mean_batch"],
                     "gpoints_s": sat["gpoints_s"],
-                    "plain_p99_ms": sat["plain"]["p99_ms"],
+                    "plain_p99_ms": sat["plain"]["p99_ms"], "slots": sat["slots"], "clients": sat["clients"],
                     "note": "requests offered faster than either path serves them; achieved_qps is the "
-                            "served path's throughput, plain_max_qps = 1 / mean single-request service time"}
+                            "served path's throughput with `clients` threads submitting (each uploads its "
+                            "requests' polygons), plain_max_qps = 1 / mean single-request service time "
+                            "(polygon upload included)"}
         h2.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

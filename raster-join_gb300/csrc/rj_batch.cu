@@ -841,17 +841,22 @@ int lanes_enqueue(Engine& e, LaneRun& lr, int& launches) {
         e.lane_pin_bytes = bytes;
     }
     char* h = (char*)e.lane_pin;
-    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
-    // the lanes start after the work already queued on the context's stream
-    RJ_CUDA(cudaEventRecord(e.lane_ev, ctx->stream));
-    for (auto& s : e.lane_st) RJ_CUDA(cudaStreamWaitEvent(s, e.lane_ev, 0));
-    cudaStream_t saved_st = ctx->stream;
-    int* saved_err = ctx->d_err;
-    PolySet* saved_ps = ctx->ps;
-    const std::string saved_ns = ctx->scratch_ns;
+    {
+        // the lanes start after the work already queued on the context's stream
+        std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+        RJ_CUDA(cudaEventRecord(e.lane_ev, ctx->stream));
+        for (auto& s : e.lane_st) RJ_CUDA(cudaStreamWaitEvent(s, e.lane_ev, 0));
+    }
     std::map<const PolySet*, int> lane_of;
     int next = 0;
     for (size_t i = 0; i < nq; ++i) {
+        // the context is taken per query, so that other callers (another
+        // serving slot, a submit) interleave with a long batch
+        std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+        cudaStream_t saved_st = ctx->stream;
+        int* saved_err = ctx->d_err;
+        PolySet* saved_ps = ctx->ps;
+        const std::string saved_ns = ctx->scratch_ns;
         QPlan& p = *lr.q[i];
         auto it = lane_of.find(p.ps);
         const int l = it != lane_of.end() ? it->second : (lane_of[p.ps] = (next++) % kLanes);
@@ -883,11 +888,11 @@ int lanes_enqueue(Engine& e, LaneRun& lr, int& launches) {
             cudaStreamSynchronize(ctx->stream);
             p.status = rc;
         }
+        ctx->stream = saved_st;
+        ctx->d_err = saved_err;
+        ctx->ps = saved_ps;
+        ctx->scratch_ns = saved_ns;
     }
-    ctx->stream = saved_st;
-    ctx->d_err = saved_err;
-    ctx->ps = saved_ps;
-    ctx->scratch_ns = saved_ns;
     lr.queued = true;
     return RJ_OK;
 }
@@ -1069,8 +1074,9 @@ struct rj_server {
 
 namespace {
 
-size_t request_need(rj_ctx* ctx, const rj_query* q, const PolySet& ps) {
-    if (q->function_type != RJ_RASTER_JOIN) return 0;
+size_t request_need(rj_ctx* ctx, const rj_query* q, const PolySet& ps, bool lanes) {
+    // the lanes work in the context's scratch, not in the slot's arena
+    if (lanes || q->function_type != RJ_RASTER_JOIN) return 0;
     RasterPlan rp;
     std::lock_guard<std::recursive_mutex> lock(ctx->mu);
     if (plan_raster_bbox(ctx, ps.bbox, q, rp)) return 0;
@@ -1413,7 +1419,7 @@ int rj_submit(rj_server* s, const rj_query* q, rj_polyset* ps, rj_result* res, u
     r->q = *q;
     r->ps = ps;
     r->res = res;
-    r->need = request_need(s->ctx, q, ps ? ps->s : s->ctx->own);
+    r->need = request_need(s->ctx, q, ps ? ps->s : s->ctx->own, !s->engines.empty() && s->engines[0]->lanes);
     r->submit_ms = now_ms();
     {
         std::lock_guard<std::mutex> lk(s->mu);

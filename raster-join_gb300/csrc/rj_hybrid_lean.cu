@@ -317,7 +317,8 @@ struct HybShape {
 };
 // 3 and 6: the register budget of two blocks per SM
 constexpr HybShape kHybShapes[] = {{512, 2, false}, {1024, 2, false}, {256, 4, false}, {512, 2, false},
-                                   {512, 2, true},  {256, 4, true},   {512, 2, true}};
+                                   {512, 2, true},  {256, 4, true},   {512, 2, true},  {1024, 2, true},
+                                   {512, 4, true}};
 constexpr int kNumHybShapes = (int)(sizeof(kHybShapes) / sizeof(kHybShapes[0]));
 
 template <int NCOL, bool AGG>
@@ -329,7 +330,9 @@ HybKernel pick_hyb(int shape) {
         case 3: return k_hybrid_lean_r2<512, 2, NCOL, AGG, false>;
         case 4: return k_hybrid_lean<512, 2, NCOL, AGG, true>;
         case 5: return k_hybrid_lean<256, 4, NCOL, AGG, true>;
-        default: return k_hybrid_lean_r2<512, 2, NCOL, AGG, true>;
+        case 6: return k_hybrid_lean_r2<512, 2, NCOL, AGG, true>;
+        case 7: return k_hybrid_lean<1024, 2, NCOL, AGG, true>;
+        default: return k_hybrid_lean<512, 4, NCOL, AGG, true>;
     }
 }
 

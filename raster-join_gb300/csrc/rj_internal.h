@@ -54,6 +54,9 @@ struct PolySet {
     double bbox[4] = {0, 0, 0, 0};
     float max_abs_coord = 0.f, max_edge_dx = 0.f, max_edge_dy = 0.f;
     double sum_dx = 0, sum_dy = 0;  // sums of |dx|, |dy| over all edges
+    // one device allocation (d_block) holds the vertices, pindex and the
+    // edge -> polygon map; d_verts, d_pindex and d_edge_poly point into it
+    DevBuf d_block;
     DevBuf d_verts, d_pindex, d_edge_poly;
     uint64_t version = 0;
     // Whether two polygons share a pixel centre, per canvas geometry (a set

@@ -1573,10 +1573,20 @@ int load_polyset(rj_ctx* ctx, PolySet& s, const float* xy, const int32_t* pindex
         return fail(ctx, RJ_E_INVALID, "polygon bounds are empty");   // CPUJoin.cpp:51-54
     cudaSetDevice(ctx->device);
     int rc;
-    if ((rc = dev_alloc(ctx, s.d_verts, (size_t)V * 8))) return rc;
-    if ((rc = dev_alloc(ctx, s.d_pindex, (size_t)(npolys + 1) * 4))) return rc;
-    if ((rc = dev_alloc(ctx, s.d_edge_poly, (size_t)V * 4))) return rc;
-    std::vector<int> edge_poly(V);
+    // one allocation and one copy for the three arrays (a served request
+    // brings a new set: fewer driver calls per request)
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t o_pidx = al((size_t)V * 8), o_edge = o_pidx + al((size_t)(npolys + 1) * 4);
+    const size_t total = o_edge + (size_t)V * 4;
+    if ((rc = dev_alloc(ctx, s.d_block, total))) return rc;
+    char* base = (char*)s.d_block.p;
+    s.d_verts = DevBuf{base, (size_t)V * 8};
+    s.d_pindex = DevBuf{base + o_pidx, (size_t)(npolys + 1) * 4};
+    s.d_edge_poly = DevBuf{base + o_edge, (size_t)V * 4};
+    std::vector<char> pack(total);
+    std::memcpy(pack.data(), xy, (size_t)V * 8);
+    std::memcpy(pack.data() + o_pidx, pindex, (size_t)(npolys + 1) * 4);
+    int* edge_poly = reinterpret_cast<int*>(pack.data() + o_edge);
     for (int i = 0; i < npolys; ++i)
         for (int k = pindex[i]; k < pindex[i + 1]; ++k) edge_poly[k] = i;
     s.h_xy.assign(xy, xy + 2 * (size_t)V);
@@ -1590,11 +1600,9 @@ int load_polyset(rj_ctx* ctx, PolySet& s, const float* xy, const int32_t* pindex
         }
         s.h_mbr[i] = make_float4(a, b, c, d);
     }
-    // synchronous copies on the default stream: they do not wait for the
+    // a synchronous copy on the default stream: it does not wait for the
     // context's (non-blocking) streams, so a set can be uploaded while joins run
-    RJ_CUDA(cudaMemcpy(s.d_verts.p, xy, (size_t)V * 8, cudaMemcpyHostToDevice));
-    RJ_CUDA(cudaMemcpy(s.d_pindex.p, pindex, (size_t)(npolys + 1) * 4, cudaMemcpyHostToDevice));
-    RJ_CUDA(cudaMemcpy(s.d_edge_poly.p, edge_poly.data(), (size_t)V * 4, cudaMemcpyHostToDevice));
+    RJ_CUDA(cudaMemcpy(s.d_block.p, pack.data(), total, cudaMemcpyHostToDevice));
     double sdx = 0, sdy = 0;   // total edge extents: bound on the canvas blocks edges cross
     for (int i = 0; i < npolys; ++i) {
         const int v0 = pindex[i], n = pindex[i + 1] - v0;
@@ -1621,9 +1629,8 @@ int load_polyset(rj_ctx* ctx, PolySet& s, const float* xy, const int32_t* pindex
 }
 
 void free_polyset(rj_ctx* ctx, PolySet& s) {
-    dev_free(ctx, s.d_verts);
-    dev_free(ctx, s.d_pindex);
-    dev_free(ctx, s.d_edge_poly);
+    dev_free(ctx, s.d_block);
+    s.d_verts = s.d_pindex = s.d_edge_poly = DevBuf{};
     s.P = s.V = 0;
 }
 
