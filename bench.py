@@ -73,6 +73,8 @@ def parse():
     ap.add_argument("--no-config2", action="store_true")
     ap.add_argument("--c2-points", type=int, default=100_000_000)
     ap.add_argument("--c2-steps", type=int, default=50)
+    ap.add_argument("--c2-shape", type=int, default=-1,
+                    help="pin the lean pass's shape of the config-2 joins (rj_set_tuning; -1: autotuned)")
     ap.add_argument("--table-points", type=int, default=1_000_000_000,
                     help="resident table of the batched and served runs")
     ap.add_argument("--batch-queries", type=int, default=512)
@@ -706,6 +708,8 @@ def run_config2(args, rj, torch, local, join, pts, verts, pidx):
     h.flags = rj.FLAG_NO_CACHE | rj.FLAG_PHASE_TIMING
     fn = fn_of(join)
     h.upload()
+    if args.c2_shape >= 0:
+        h.setTuning(rj.TUNE_COUNT_SHAPE, args.c2_shape)
     q = h.make_query(fn)
     out = {}
     for _ in range(3):

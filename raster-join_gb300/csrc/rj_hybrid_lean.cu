@@ -318,7 +318,7 @@ struct HybShape {
 // 3 and 6: the register budget of two blocks per SM
 constexpr HybShape kHybShapes[] = {{512, 2, false}, {1024, 2, false}, {256, 4, false}, {512, 2, false},
                                    {512, 2, true},  {256, 4, true},   {512, 2, true},  {1024, 2, true},
-                                   {512, 4, true}};
+                                   {512, 1, true}};
 constexpr int kNumHybShapes = (int)(sizeof(kHybShapes) / sizeof(kHybShapes[0]));
 
 template <int NCOL, bool AGG>
@@ -332,7 +332,7 @@ HybKernel pick_hyb(int shape) {
         case 5: return k_hybrid_lean<256, 4, NCOL, AGG, true>;
         case 6: return k_hybrid_lean_r2<512, 2, NCOL, AGG, true>;
         case 7: return k_hybrid_lean<1024, 2, NCOL, AGG, true>;
-        default: return k_hybrid_lean<512, 4, NCOL, AGG, true>;
+        default: return k_hybrid_lean<512, 1, NCOL, AGG, true>;
     }
 }
 

@@ -39,17 +39,18 @@ __device__ __forceinline__ uint32_t bitrange(int a, int b) {
     return (b >= 32 ? 0xFFFFFFFFu : ((1u << b) - 1u)) & ~((1u << a) - 1u);
 }
 
-// Coverage of row j's pixel centres in [i_lo, i_hi] as a bitmap R[0, nw)
-// (bit b of word w = pixel (w_lo + w) * 32 + b).  A pixel is covered when an
-// odd number of the row's crossings lie at or left of it (crossing pixel
-// L = first pixel right of the crossing, exact integer arithmetic), so each
-// crossing toggles one bit and a prefix XOR over the row gives the coverage:
-// no sorting, O(crossings + words) per row.  Crossings left of i_lo act from
-// i_lo; those right of i_hi do not matter.
+// Coverage of row j's pixel centres in [i_lo, i_hi], word by word: f(w, bits)
+// receives word w of the row (bit b = pixel (w_lo + w) * 32 + b), called by
+// lane w % 32.  A pixel is covered when an odd number of the row's crossings
+// lie at or left of it (crossing pixel L = first pixel right of the crossing,
+// exact integer arithmetic), so each crossing toggles one bit of R and a
+// prefix XOR over the row gives the coverage: no sorting, O(crossings + words)
+// per row.  Crossings left of i_lo act from i_lo; those right of i_hi do not
+// matter.  R[0, nw) must be zero on entry and is zero again on return (the
+// scan clears what the toggles set), so consecutive rows need no clearing.
+template <class F>
 __device__ __forceinline__ void row_cover(int j, const int4* edge, int nb, bool overflow, const int2* pv, int n,
-                                          int i_lo, int i_hi, int w_lo, int nw, uint32_t* R, int lane) {
-    for (int w = lane; w < nw; w += 32) R[w] = 0u;
-    __syncwarp();
+                                          int i_lo, int i_hi, int w_lo, int nw, uint32_t* R, int lane, F&& f) {
     const int32_t cy = j * kSub + kSub / 2;
     const int ne = overflow ? n : nb;
     for (int e = lane; e < ne; e += 32) {
@@ -80,13 +81,19 @@ __device__ __forceinline__ void row_cover(int j, const int4* edge, int nb, bool 
         x ^= x << 16;
         if (((unsigned)__popc(odd & ((1u << lane) - 1u)) & 1u) ^ carry) x = ~x;
         if (w < nw) {
+            if (t) R[w] = 0u;
             const int x0 = (w_lo + w) * 32;
             const int a0 = max(i_lo - x0, 0), b0 = min(i_hi + 1 - x0, 32);
-            R[w] = a0 < b0 ? (x & bitrange(a0, b0)) : 0u;
+            f(w, a0 < b0 ? (x & bitrange(a0, b0)) : 0u);
         }
         carry ^= (unsigned)__popc(odd) & 1u;
     }
     __syncwarp();
+}
+
+// the 16-pixel halves of a word whose 16 bits of v are all set, as a mask
+__device__ __forceinline__ uint32_t full_halves(uint32_t v) {
+    return ((v & 0xFFFFu) == 0xFFFFu ? 0xFFFFu : 0u) | ((v >> 16) == 0xFFFFu ? 0xFFFF0000u : 0u);
 }
 
 template <int MODE>
@@ -98,8 +105,10 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
     const int total = a.band_start[TP];
     int4* my_edge = s_tier + (size_t)warp * kTEdgeCap;
     uint32_t* my_I = reinterpret_cast<uint32_t*>(s_tier + (size_t)kTW * kTEdgeCap) + (size_t)warp * 3 * kTWords;
-    uint32_t* my_U = my_I + kTWords;
+    uint32_t* my_U = my_I + kTWords;   // label pass: the mixed blocks' mask instead
     uint32_t* my_R = my_U + kTWords;
+    for (int w = lane; w < kTWords; w += 32) my_R[w] = 0u;   // row_cover keeps it zero between rows
+    __syncwarp();
     for (;;) {
         int item = 0, tp = 0;
         if (lane == 0) {
@@ -167,13 +176,16 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
             for (int r = 0; r < kTBand; ++r) {
                 const int j = jb + r;
                 const bool live = j <= a.resy - 1 && j >= j_lo && j <= j_hi;
-                if (live) row_cover(j, my_edge, nb, overflow, pv, n, i_lo, i_hi, w_lo, nw, my_R, lane);
-                for (int w = lane; w < nw; w += 32) {
-                    const uint32_t v = live ? my_R[w] : 0u;
-                    my_I[w] &= v;
-                    if (MODE == MODE_TIER_CLASSIFY) my_U[w] |= v;
+                if (live) {
+                    row_cover(j, my_edge, nb, overflow, pv, n, i_lo, i_hi, w_lo, nw, my_R, lane,
+                              [&](int w, uint32_t v) {
+                                  my_I[w] &= v;
+                                  if (MODE == MODE_TIER_CLASSIFY) my_U[w] |= v;
+                              });
+                } else {
+                    for (int w = lane; w < nw; w += 32) my_I[w] = 0u;
+                    __syncwarp();
                 }
-                __syncwarp();
             }
         }
         if (MODE == MODE_TIER_CLASSIFY) {
@@ -208,23 +220,30 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
             }
         }
         // covered pixels of the blocks that are not full for p (reduce) or of
-        // the mixed blocks (labels): the pixel slots
+        // the mixed blocks (labels): the pixel slots.  keep[w]: the halves of
+        // word w whose pixels are visited, found once per band (labels: the
+        // mixed blocks; reduce: all but p's full blocks).
+        if (MODE == MODE_TIER_LABEL) {
+            for (int w = lane; w < nw; w += 32) {
+                const int bc = (w_lo + w) * 2;
+                const bool m0 = __ldg(tr.mixed + blk0 + bc) != 0;
+                const bool m1 = bc + 1 < tr.bw && __ldg(tr.mixed + blk0 + bc + 1) != 0;
+                my_U[w] = (m0 ? 0xFFFFu : 0u) | (m1 ? 0xFFFF0000u : 0u);
+            }
+            __syncwarp();
+        }
         for (int r = 0; r < kTBand; ++r) {
             const int j = jb + r;
             if (!(j <= a.resy - 1 && j >= j_lo && j <= j_hi)) continue;
-            row_cover(j, my_edge, nb, overflow, pv, n, i_lo, i_hi, w_lo, nw, my_R, lane);
-            for (int w = lane; w < nw; w += 32) {
-                const uint32_t bits = my_R[w];
-                if (!bits) continue;
+            row_cover(j, my_edge, nb, overflow, pv, n, i_lo, i_hi, w_lo, nw, my_R, lane, [&](int w, uint32_t bits) {
+                bits &= (MODE == MODE_TIER_LABEL) ? my_U[w] : ~full_halves(my_I[w]);
+                if (!bits) return;
                 const int x0 = (w_lo + w) * 32;
                 #pragma unroll
                 for (int half = 0; half < 2; ++half) {
                     uint32_t hb = (bits >> (half * 16)) & 0xFFFFu;
                     if (!hb) continue;
-                    if (MODE == MODE_TIER_REDUCE && ((my_I[w] >> (half * 16)) & 0xFFFFu) == 0xFFFFu) continue;
-                    const int bc = (x0 >> 4) + half;
-                    const size_t b = blk0 + bc;
-                    if (MODE == MODE_TIER_LABEL && !__ldg(tr.mixed + b)) continue;
+                    const size_t b = blk0 + (x0 >> 4) + half;
                     const size_t base = (size_t)__ldg(tr.slot + b) * 256 + (size_t)(j & 15) * 16;
                     while (hb) {
                         const int bit = __ffs(hb) - 1;
@@ -239,8 +258,7 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
                         }
                     }
                 }
-            }
-            __syncwarp();
+            });
         }
         acc_c = warp_sum_u64(acc_c);
         if (MODE == MODE_TIER_LABEL) {
