@@ -288,6 +288,9 @@ RJ_API int rj_column_absmax(const rj_ctx *ctx, int32_t attrib_id, double *out);
  *                            join); RJ_TUNE_COUNT_SHAPE indexes them there
  *                            too (canvas copies in shared memory, or
  *                            atomics into the canvas in global memory)
+ *   RJ_TUNE_HYBRID_SHAPES    (read only) number of shapes of the lean pass
+ *                            of the hybrid and index joins; RJ_TUNE_COUNT_SHAPE
+ *                            indexes them there
  *   RJ_TUNE_WAIT_LIMIT       microseconds a bounded device wait of the
  *                            bulk-copy pipeline (RJ_TUNE_POINT_SHAPE 2) may
  *                            take before it gives up and the call returns
@@ -304,6 +307,7 @@ RJ_API int rj_column_absmax(const rj_ctx *ctx, int32_t attrib_id, double *out);
 #define RJ_TUNE_LEAN_SHAPES        5
 #define RJ_TUNE_WAIT_LIMIT         6
 #define RJ_TUNE_SPLAT_SHAPES       7
+#define RJ_TUNE_HYBRID_SHAPES      8
 RJ_API int rj_set_tuning(rj_ctx *ctx, int32_t knob, int32_t value);
 RJ_API int rj_get_tuning(const rj_ctx *ctx, int32_t knob, int32_t *value);
 

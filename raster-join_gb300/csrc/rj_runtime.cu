@@ -2369,6 +2369,7 @@ int rj_get_tuning(const rj_ctx* ctx, int32_t knob, int32_t* value) {
         case RJ_TUNE_COUNT_SHAPES: *value = label_count_shapes(); return RJ_OK;
         case RJ_TUNE_LEAN_SHAPES: *value = label_lean_shapes(); return RJ_OK;
         case RJ_TUNE_SPLAT_SHAPES: *value = splat_lean_shapes(); return RJ_OK;
+        case RJ_TUNE_HYBRID_SHAPES: *value = hybrid_lean_shapes(); return RJ_OK;
         case RJ_TUNE_WAIT_LIMIT: *value = (int32_t)std::min<uint64_t>(ctx->wait_ns / 1000ull, 0x7FFFFFFFull); return RJ_OK;
         default: return RJ_E_INVALID;
     }

@@ -36,7 +36,7 @@ RJ_PENDING = 1
 SUM_SHIFT_AUTO = -2147483648
 # rj_set_tuning knobs (include/rj.h)
 TUNE_POINT_SHAPE, TUNE_COUNT_SHAPE, TUNE_COUNT_BLOCK_SHIFT, TUNE_HYBRID_EXACT_SCALE = 0, 1, 2, 3
-TUNE_COUNT_SHAPES, TUNE_LEAN_SHAPES, TUNE_WAIT_LIMIT, TUNE_SPLAT_SHAPES = 4, 5, 6, 7
+TUNE_COUNT_SHAPES, TUNE_LEAN_SHAPES, TUNE_WAIT_LIMIT, TUNE_SPLAT_SHAPES, TUNE_HYBRID_SHAPES = 4, 5, 6, 7, 8
 BATCH_AUTOTUNE = 0x1
 BATCH_NO_FUSE = 0x2
 BATCH_FUSE_ALL = 0x4
