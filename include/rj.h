@@ -213,6 +213,16 @@ RJ_API int rj_attach_points_device(rj_ctx *ctx, const rj_column *cols, int32_t n
  * copies overlap the point pass.  Batches run such a table query by query. */
 RJ_API int rj_attach_points_host(rj_ctx *ctx, const rj_column *cols, int32_t ncols,
                                  uint64_t npoints, int32_t loc_attrib, uint64_t chunk_points);
+/* Host-resident table read in place: the data pointers are page-locked host
+ * memory (cudaMallocHost / cudaHostAlloc, or registered with cudaHostRegister;
+ * 16-byte aligned) that the caller keeps alive.  Nothing is copied: every
+ * query's point pass reads the columns over the host link (NVLink-C2C on
+ * Grace systems), so the table crosses the link once per query with no
+ * staging buffers and no copy engine.  RJ_E_INVALID for memory the device
+ * cannot address.  Results equal a resident table's.  No counterpart in the
+ * reference (its memory passes copy chunks, GLFunction.cpp:330-337). */
+RJ_API int rj_attach_points_mapped(rj_ctx *ctx, const rj_column *cols, int32_t ncols,
+                                   uint64_t npoints, int32_t loc_attrib);
 RJ_API int rj_free_points(rj_ctx *ctx);
 
 /* ---- polygons: PolyHandler::addPolygonCollection (PolyHandler.cpp:49-80).

@@ -2037,6 +2037,28 @@ int rj_attach_points_host(rj_ctx* ctx, const rj_column* cols, int32_t ncols, uin
     return load_points_impl(ctx, cols, ncols, npoints, loc_attrib, false, true, chunk_points);
 }
 
+int rj_attach_points_mapped(rj_ctx* ctx, const rj_column* cols, int32_t ncols, uint64_t npoints,
+                            int32_t loc_attrib) {
+    if (!ctx) return RJ_E_INVALID;
+    if (!cols || ncols <= 0 || ncols > RJ_MAX_ATTRIBUTES)
+        return fail(ctx, RJ_E_INVALID, "ncols must be 1..%d", RJ_MAX_ATTRIBUTES);
+    cudaSetDevice(ctx->device);
+    // page-locked host memory is addressable by the device: its device address
+    std::vector<rj_column> dcols(cols, cols + ncols);
+    for (int i = 0; i < ncols; ++i) {
+        if (!npoints) continue;
+        cudaPointerAttributes at{};
+        if (!cols[i].data || cudaPointerGetAttributes(&at, cols[i].data) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(ctx, RJ_E_INVALID, "column %d: not page-locked host memory", i);
+        }
+        if (at.type != cudaMemoryTypeHost || !at.devicePointer)
+            return fail(ctx, RJ_E_INVALID, "column %d: not page-locked host memory the device can address", i);
+        dcols[i].data = at.devicePointer;
+    }
+    return load_points_impl(ctx, dcols.data(), ncols, npoints, loc_attrib, true);
+}
+
 int rj_free_points(rj_ctx* ctx) {
     if (!ctx) return RJ_E_INVALID;
     std::lock_guard<std::recursive_mutex> lock(ctx->mu);

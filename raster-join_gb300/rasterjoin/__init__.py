@@ -143,6 +143,7 @@ def load_library(path=LIB_PATH):
         "rj_attach_points_device": (C.c_int, [C.c_void_p, P(Column), C.c_int32, C.c_uint64, C.c_int32]),
         "rj_free_points": (C.c_int, [C.c_void_p]),
         "rj_attach_points_host": (C.c_int, [C.c_void_p, P(Column), C.c_int32, C.c_uint64, C.c_int32, C.c_uint64]),
+        "rj_attach_points_mapped": (C.c_int, [C.c_void_p, P(Column), C.c_int32, C.c_uint64, C.c_int32]),
         "rj_set_polygons": (C.c_int, [C.c_void_p, P(C.c_float), P(C.c_int32), C.c_int32, P(C.c_double)]),
         "rj_execute": (C.c_int, [C.c_void_p, P(Query), P(Result)]),
         "rj_get_timings": (C.c_int, [C.c_void_p, P(Timings)]),
@@ -599,6 +600,24 @@ class GLHandler:
         self._check(self.lib.rj_attach_points_host(self.ctx, cols, len(columns), npoints, loc_attrib, chunk_points))
         self._host_table = keep
         self._loaded_points = ("host", tuple(id(a) for a in keep), npoints)
+
+    def attachMapped(self, columns, npoints, loc_attrib):
+        """Host table read in place over the host link: columns are
+        (attrib_id, type, array or address) in page-locked host memory (e.g. a
+        pinned torch tensor's numpy view), kept alive by the caller."""
+        cols = (Column * len(columns))()
+        keep = []
+        for i, (aid, typ, arr) in enumerate(columns):
+            cols[i].attrib_id = aid
+            cols[i].type = typ
+            if isinstance(arr, int):
+                cols[i].data = arr
+            else:
+                keep.append(arr)
+                cols[i].data = arr.ctypes.data
+        self._check(self.lib.rj_attach_points_mapped(self.ctx, cols, len(columns), npoints, loc_attrib))
+        self._host_table = keep
+        self._loaded_points = ("device",)
 
     # ---- polygon sets, time index, batches ----
     def polyset(self, xy, pindex, bbox=None):
