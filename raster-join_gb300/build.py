@@ -21,7 +21,8 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "librj.so")
 SOURCES = ["rj_runtime.cu", "rj_point_kernels.cu", "rj_point_exact.cu", "rj_poly_kernels.cu", "rj_noalloc.cu",
            "rj_batch.cu", "rj_batch_kernels.cu", "rj_batch_direct.cu", "rj_tier_kernels.cu",
-           "rj_count_kernels.cu", "rj_lean_kernels.cu", "rj_hybrid_lean.cu", "rj_splat_kernels.cu"]
+           "rj_count_kernels.cu", "rj_lean_kernels.cu", "rj_hybrid_lean.cu", "rj_splat_kernels.cu",
+           "rj_tier_lean.cu"]
 HEADERS = ["rj_device.cuh", "rj_launch.h", "rj_internal.h", "rj_point_map.cuh", "rj_point_core.cuh",
            "rj_batch_common.cuh", "rj_lean.cuh",
            os.path.join("..", "..", "include", "rj.h")]

@@ -278,6 +278,28 @@ struct SplatLeanArgs {
     uint64_t zrow0;
     float4 qbox;
 };
+// Lean point pass over a tiered canvas (rj_tier_lean.cu): one or several
+// canvas tiles, the label form (histogram per polygon) or the canvas form
+// (block and mixed-pixel sums), interval-form filters (LeanCols).
+struct TierLeanArgs {
+    const float4* xy;            // location column as point pairs, 16-byte aligned
+    uint64_t n;
+    const float4* colxf;         // [splitx] (s, t, h, tile extent) per tile column
+    const float4* rowxf;         // [splity]
+    int splitx, splity;
+    int resx, resy;              // tile resolution
+    float lbx, lby;              // canvas lower-left, for the tile guess
+    float inv_tdx, inv_tdy;      // 1 / tile extent, for the tile guess
+    TierArgs tr;
+    int P;
+    unsigned long long* out_count;
+    const float4* zones;         // zone map or null (as LabelCountArgs)
+    uint64_t zrow0;
+    float4 qbox;
+};
+int tier_lean_shapes();
+size_t tier_lean_smem(bool label, int P, bool agg);
+bool launch_tier_lean(int shape, bool label, const TierLeanArgs& a, const LeanCols& lc, int sms, cudaStream_t st);
 int splat_lean_shapes();
 // shared memory of a shape for a canvas (1 for the global-atomic shapes), 0
 // when the canvas does not fit

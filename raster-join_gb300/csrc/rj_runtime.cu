@@ -735,6 +735,9 @@ int poly_pass(rj_ctx* ctx, int mode, PolyPassArgs& a, const TierArgs* tier = nul
 // Tiered canvas of a large raster canvas: classification of 16 x 16 blocks,
 // then the label form (disjoint coverage) or the canvas form.  Results equal
 // the flat canvas's; polygon-side work follows the perimeters.
+int tier_lean_pass(rj_ctx* ctx, const DevFilter& f, const RasterPlan& rp, const CanvasXf& cx, const TierArgs& tr,
+                   bool label, size_t nblk, size_t spx, ExecState& es, bool* done);   // below
+
 int exec_raster_tier(rj_ctx* ctx, const rj_query* q, const RasterPlan& rp, const DevFilter& f, ExecState& es,
                      PolyPassArgs& a, const CanvasXf& cx, uint64_t ckey) {
     int rc;
@@ -782,9 +785,11 @@ int exec_raster_tier(rj_ctx* ctx, const rj_query* q, const RasterPlan& rp, const
     }
     es.ph->mark(2);
     if (label) {
-        if ((rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
-                 launch_tier_label_points(pa, cx, tr, ctx->sms, ctx->stream);
-             })))
+        bool lean = false;
+        if ((rc = tier_lean_pass(ctx, f, rp, cx, tr, true, nblk, spx, es, &lean))) return rc;
+        if (!lean && (rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
+                          launch_tier_label_points(pa, cx, tr, ctx->sms, ctx->stream);
+                      })))
             return rc;
         es.ph->mark(3);
         es.ph->mark(4);
@@ -801,9 +806,11 @@ int exec_raster_tier(rj_ctx* ctx, const rj_query* q, const RasterPlan& rp, const
         RJ_CUDA(cudaMemsetAsync(tr.bsum, 0, nblk * 8, ctx->stream));
         RJ_CUDA(cudaMemsetAsync(tr.psum, 0, spx * 8, ctx->stream));
     }
-    if ((rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
-             launch_tier_splat_points(pa, cx, tr, ctx->sms, ctx->stream);
-         })))
+    bool lean = false;
+    if ((rc = tier_lean_pass(ctx, f, rp, cx, tr, false, nblk, spx, es, &lean))) return rc;
+    if (!lean && (rc = point_pass(ctx, f, es.out_count, es.out_sum, [&](const PointArgs& pa) {
+                      launch_tier_splat_points(pa, cx, tr, ctx->sms, ctx->stream);
+                  })))
         return rc;
     es.ph->mark(3);
     a.canvas_c = nullptr;
@@ -1263,6 +1270,94 @@ int splat_lean_pass(rj_ctx* ctx, const DevFilter& f, const RasterPlan& rp, uint3
     ctx->passes = 1;
     ctx->copy_ms = 0;
     if (!launch_splat_lean(cands[(size_t)pi], a, lc, ctx->sms, ctx->stream)) return RJ_OK;
+    RJ_CUDA(cudaGetLastError());
+    ctx->last_count_shape = cands[(size_t)pi];
+    *done = true;
+    return RJ_OK;
+}
+
+// Lean point pass over the tiered canvas (rj_tier_lean.cu): a resident
+// table, interval-form filters on at most four columns, count or sum; label
+// form into the per-polygon outputs, canvas form into the block and slot
+// sums.  Shapes forced with rj_set_tuning (RJ_TUNE_COUNT_SHAPE), else
+// autotuned per query class; tuning runs of the canvas form write into its
+// sums, which are cleared again after them.  *done = false: the pass does
+// not apply (the caller takes the generic pass).
+int tier_lean_pass(rj_ctx* ctx, const DevFilter& f, const RasterPlan& rp, const CanvasXf& cx, const TierArgs& tr,
+                   bool label, size_t nblk, size_t spx, ExecState& es, bool* done) {
+    *done = false;
+    ctx->last_count_shape = ctx->last_count_bshift = -1;
+    if (ctx->streamed || f.general || f.ncol > label_lean_max_cols()) return RJ_OK;
+    PointArgs pa = make_point_args(ctx, f, es.out_count, es.out_sum);
+    if (((uintptr_t)pa.xy & 15) != 0) return RJ_OK;
+    LeanCols lc{};
+    if (!lean_cols_of(pa, es.out_sum, lc)) return RJ_OK;
+    TierLeanArgs a{};
+    a.xy = reinterpret_cast<const float4*>(pa.xy);
+    a.n = pa.n;
+    a.colxf = cx.colxf;
+    a.rowxf = cx.rowxf;
+    a.splitx = rp.splitx;
+    a.splity = rp.splity;
+    a.resx = rp.resx;
+    a.resy = rp.resy;
+    a.lbx = cx.lbx;
+    a.lby = cx.lby;
+    a.inv_tdx = (float)(1.0 / (double)cx.tdx);
+    a.inv_tdy = (float)(1.0 / (double)cx.tdy);
+    a.tr = tr;
+    a.P = ctx->ps->P;
+    a.out_count = es.out_count;
+    a.zones = pa.zones;
+    a.zrow0 = pa.row0;
+    a.qbox = pa.qbox;
+    const bool agg = lc.aggr != 0;
+    std::vector<int> cands;
+    for (int sh = 0; sh < tier_lean_shapes(); ++sh)
+        if (ctx->count_shape < 0 || ctx->count_shape == sh) cands.push_back(sh);
+    if (cands.empty() || tier_lean_smem(label, a.P, agg) > 200 * 1024) return RJ_OK;
+    char key[200];
+    std::snprintf(key, sizeof key, "tier:%d:%d:%d:%d:%d:%d:%d:%d:%d", label ? 1 : 0, lc.ncol, lc.aggr,
+                  lc.aggr_ci >= 0, rp.splitx * rp.splity, tune_bucket((double)a.P), tune_bucket((double)nblk),
+                  tune_bucket((double)a.n), ctx->count_shape);
+    int tuned_i = -1;
+    const bool have = tuned_get(ctx, key, &tuned_i);
+    const bool small = a.n < kTuneMinPoints;
+    int rc;
+    unsigned long long *tout = nullptr, *tsum = nullptr;
+    double* tnf = nullptr;
+    if (!have && !small && label) {
+        if ((rc = scratch_t(ctx, "tune_count", (size_t)a.P, &tout))) return rc;
+        if ((rc = scratch_t(ctx, "tune_sum", (size_t)a.P, &tsum))) return rc;
+        if ((rc = scratch_t(ctx, "tune_nonfinite", (size_t)a.P, &tnf))) return rc;
+    }
+    bool timed_any = false;
+    const int pi = small && !have ? 0 : tune_pick(ctx, key, cands.size(), [&](size_t i) {
+        timed_any = true;
+        TierLeanArgs b = a;
+        LeanCols tl = lc;
+        if (label) {
+            b.out_count = tout;
+            tl.out_sum = tsum;
+            tl.nonfinite = tnf;
+        }
+        TierLeanArgs w = b;
+        w.n = std::min<uint64_t>(a.n & ~1ULL, 1ULL << 16);   // first launch of a shape loads it
+        if (!launch_tier_lean(cands[i], label, w, tl, ctx->sms, ctx->stream)) return false;
+        b.n = std::min<uint64_t>(a.n & ~1ULL, 1ULL << 27);
+        return launch_tier_lean(cands[i], label, b, tl, ctx->sms, ctx->stream);
+    });
+    RJ_CUDA(cudaGetLastError());
+    if (timed_any && !label) {
+        RJ_CUDA(cudaMemsetAsync(tr.bcnt, 0, nblk * 4, ctx->stream));
+        RJ_CUDA(cudaMemsetAsync(tr.pcnt, 0, spx * 4, ctx->stream));
+        if (tr.bsum) RJ_CUDA(cudaMemsetAsync(tr.bsum, 0, nblk * 8, ctx->stream));
+        if (tr.psum) RJ_CUDA(cudaMemsetAsync(tr.psum, 0, spx * 8, ctx->stream));
+    }
+    if (pi < 0) return RJ_OK;
+    ctx->passes = 1;
+    ctx->copy_ms = 0;
+    if (!launch_tier_lean(cands[(size_t)pi], label, a, lc, ctx->sms, ctx->stream)) return RJ_OK;
     RJ_CUDA(cudaGetLastError());
     ctx->last_count_shape = cands[(size_t)pi];
     *done = true;

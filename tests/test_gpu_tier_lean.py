@@ -1,0 +1,98 @@
+"""Lean point pass over tiered canvases (16 x 16-pixel blocks), label and
+canvas forms, one tile and several: every shape gives the oracle's results
+bit for bit (sums within 1e-6), including points on and around the tile seams
+(which the reference counts in every tile whose window holds them) and points
+off the canvas."""
+import numpy as np
+import pytest
+
+import oracle
+import rasterjoin as rj
+from rasterjoin import synth
+
+pytestmark = pytest.mark.gpu
+
+BOX = 6000.0          # metres: about 6000 x 6000 pixels at 1 m (tiered from 2^24 pixels)
+
+
+def _table(n, seed, seam_x, seam_y):
+    pts = synth.points(n, seed=seed, box=BOX, columns=True)
+    xy = pts["xy"].copy()
+    rng = np.random.default_rng(seed)
+    # points on, just left and just right of every seam line, and off the canvas
+    k = 0
+    offs = np.array([0.0, 1e-3, -1e-3, 0.25, -0.25, 0.5, -0.5, 0.75, -0.75, 1.0, -1.0], np.float32)
+    for sx in seam_x:
+        for o in offs:
+            xy[k] = (sx + o, rng.uniform(0, BOX)); k += 1
+    for sy in seam_y:
+        for o in offs:
+            xy[k] = (rng.uniform(0, BOX), sy + o); k += 1
+    for sx in seam_x:
+        for sy in seam_y:
+            for o in offs[:5]:
+                xy[k] = (sx + o, sy - o); k += 1
+    specials = np.array([[np.nan, 10.0], [10.0, np.nan], [np.inf, 5.0], [-1e30, 3.0], [-0.004, 200.0],
+                         [BOX + 0.004, 300.0], [9000.0, 9000.0]], np.float32)
+    xy[k:k + len(specials)] = specials
+    pts["xy"] = xy
+    return pts
+
+
+@pytest.fixture(scope="module")
+def sets():
+    vor = synth.voronoi_polygons(40, seed=77, box=BOX, verts_per_poly=40, jitter=5.0)
+    stars = synth.star_polygons(25, seed=78, box=BOX, vmin=6, vmax=60, rmin=100, rmax=900)
+    return {"voronoi": vor, "stars": stars}
+
+
+def _dh(pts, verts, pidx, filters):
+    dh = rj.DataHandler()
+    dh.add_column(1, rj.Location, pts["xy"])
+    dh.add_column(2, rj.Uint, pts["t"])
+    dh.add_column(3, rj.Float, pts["a"])
+    dh.add_column(4, rj.Int, pts["f1"])
+    dh.setPolygons(verts, pidx)
+    if filters:
+        dh.setQueryConstraints([(4, rj.GT, 2)])
+        dh.setTimeRange(2, synth.T0, synth.T0 + synth.YEAR // 2)
+        dh.setAggregation(rj.Avg, 3)
+    return dh
+
+
+# one tile (fbo 8192) and 3 x 3 tiles of 2100 pixels
+@pytest.mark.parametrize("fbo", [8192, 2100])
+@pytest.mark.parametrize("name", ["voronoi", "stars"])
+@pytest.mark.parametrize("filters", [False, True])
+def test_every_tier_shape_matches_oracle(handler, sets, fbo, name, filters):
+    verts, pidx = sets[name]
+    bb = (verts[:, 0].min(), verts[:, 1].min())
+    seams_x = [float(bb[0]) + k * fbo * 1.0 for k in (1, 2)] if fbo < 8192 else []
+    seams_y = [float(bb[1]) + k * fbo * 1.0 for k in (1, 2)] if fbo < 8192 else []
+    pts = _table(200_003, 79, seams_x, seams_y)
+    handler.setDataHandler(_dh(pts, verts, pidx, filters))
+    handler.setCellSize(1.0)
+    handler.max_fbo_size = fbo
+    cols = oracle.Columns({2: (oracle.Uint, pts["t"]), 3: (oracle.Float, pts["a"]), 4: (oracle.Int, pts["f1"])})
+    f = cols.filt([(4, oracle.GT, 2)], aggr_attrib=3, time_range=(2, synth.T0, synth.T0 + synth.YEAR // 2)) \
+        if filters else None
+    want = oracle.raster_join(pts["xy"], verts, pidx, 1.0, f=f, max_res=fbo)
+    handler.flags = rj.FLAG_TIERED_CANVAS
+    taken = 0
+    try:
+        for sh in range(3):
+            handler.setTuning(rj.TUNE_COUNT_SHAPE, sh)
+            got = handler.execute(rj.RasterJoinFn)
+            np.testing.assert_array_equal(got.count, want[0], err_msg="shape %d" % sh)
+            if filters:
+                np.testing.assert_allclose(got.sum, want[1], rtol=1e-6, atol=1e-9 * max(1.0, float(np.abs(want[1]).max())))
+            taken += handler.getTuning(rj.TUNE_COUNT_SHAPE) == sh
+        handler.setTuning(rj.TUNE_COUNT_SHAPE, -1)
+        got = handler.execute(rj.RasterJoinFn)                       # autotuned
+        np.testing.assert_array_equal(got.count, want[0])
+    finally:
+        handler.setTuning(rj.TUNE_COUNT_SHAPE, -1)
+        handler.flags = 0
+        handler.max_fbo_size = 8192
+    assert taken == 3
+    assert want[0].sum() > 0
