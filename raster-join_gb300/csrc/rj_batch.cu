@@ -897,6 +897,22 @@ int lanes_enqueue(Engine& e, LaneRun& lr, int& launches) {
     return RJ_OK;
 }
 
+// Frees the lanes' scratch buffers of this engine (their keys carry the
+// engine's lane suffix); the caller holds the context lock and no lane work
+// is in flight.
+void release_lane_scratch(Engine& e) {
+    rj_ctx* ctx = e.ctx;
+    const std::string tag = "#e" + std::to_string(e.id) + ".";
+    for (auto it = ctx->scratch.begin(); it != ctx->scratch.end();) {
+        if (it->first.find(tag) != std::string::npos) {
+            dev_free(ctx, it->second);
+            it = ctx->scratch.erase(it);
+        } else {
+            ++it;
+        }
+    }
+}
+
 int lanes_finish(Engine& e, LaneRun& lr) {
     if (!lr.queued) return RJ_OK;
     int rc = RJ_OK;
@@ -1001,6 +1017,22 @@ int execute_batch(Engine& e, int nq, const rj_query* qs, const rj_query* const* 
     }
     lanes_finish(e, lr);
     bo.fallback += (int)lr.q.size();
+    // A query the lanes could not hold (its lane's scratch beside the other
+    // lanes' exceeded the memory budget) runs again alone once the lanes'
+    // scratch is released.
+    bool retry = false;
+    for (QPlan* p : lr.q) retry = retry || p->status == RJ_E_OOM;
+    if (retry) {
+        {
+            std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+            release_lane_scratch(e);
+        }
+        for (QPlan* p : lr.q) {
+            if (p->status != RJ_E_OOM) continue;
+            p->status = run_plain(ctx, *p);
+            plain_launches += ctx->tm.kernel_launches;
+        }
+    }
     int first = RJ_OK;
     for (QPlan& p : plans) {
         if (status) status[p.idx] = p.status;

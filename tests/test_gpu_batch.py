@@ -341,3 +341,30 @@ def test_lanes_equal_single(setup):
             np.testing.assert_array_equal(r.sum, sm)
             if b is not None:
                 np.testing.assert_array_equal(r.bounds, b)
+
+
+def test_lanes_retry_queries_the_budget_cannot_hold_at_once(built):
+    """Under a device-memory budget too small for several lanes' label maps at
+    once, the queries whose lane ran out of memory run again alone after the
+    lanes' scratch is released: every status is RJ_OK and every result equals
+    the single-query result."""
+    pts = synth.points(500_001, seed=91, columns=True)
+    h = rj.GLHandler(gpu_mem_mb=48)
+    try:
+        dh = rj.DataHandler()
+        dh.add_column(1, rj.Location, pts["xy"])
+        v0, p0 = synth.voronoi_polygons(60, seed=92)
+        dh.setPolygons(v0, p0)
+        h.setDataHandler(dh)
+        h.upload()
+        sets = [h.polyset(*synth.voronoi_polygons(60, seed=93 + k)) for k in range(4)]
+        qs = [make_query(10.0) for _ in range(4)]         # 4000 x 4000 label maps: 32 MB each
+        alone = [single(h, s, q) for s, q in zip(sets, qs)]
+        res, status, stats = h.execute_batch(qs, sets, raise_on_error=False)
+        assert (status == 0).all(), status
+        for (c, sm), r in zip(alone, res):
+            np.testing.assert_array_equal(r.count, c)
+        for s in sets:
+            s.close()
+    finally:
+        h.close()
