@@ -97,6 +97,9 @@ typedef struct {
 #define RJ_FLAG_FLAT_CANVAS        0x80u /* raster: one entry per pixel even for
                                            large canvases (no 16 x 16 block
                                            tiers; same results)              */
+#define RJ_FLAG_COUNT_EDGE_TESTS   0x200u /* index/hybrid: count the exact edge tests
+                                           into rj_timings.edge_tests (one atomic
+                                           per tested point)                  */
 #define RJ_FLAG_TIERED_CANVAS      0x100u /* raster: 16 x 16 block tiers for any
                                            canvas of at least 2^24 pixels,
                                            whatever the rows (same results)  */
@@ -180,6 +183,8 @@ typedef struct {
     double backend_query_ms;  /* always 0: no backend query                */
     int32_t accuracy;         /* accuracy_m for raster joins, else 0       */
     int32_t kernel_launches;  /* kernels this library launched in the call */
+    uint64_t edge_tests;      /* exact edge tests of the index / hybrid join
+                                 (counted with RJ_FLAG_COUNT_EDGE_TESTS, else 0) */
 } rj_timings;
 
 typedef struct rj_ctx rj_ctx;

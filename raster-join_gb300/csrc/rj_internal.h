@@ -160,6 +160,7 @@ struct rj_ctx {
     // refuse (RJ_E_UNSUPPORTED) and the zone map is left out
     uint64_t table_gen = 0;
     uint64_t tix_gen = 0;   // bumped when the time index stops matching the rows
+    unsigned long long* edge_tests_dev = nullptr;   // this query's edge-test counter, or null
     bool capturing = false;
 };
 

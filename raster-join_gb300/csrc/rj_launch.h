@@ -114,6 +114,7 @@ struct ExactIndex {
     const float4* edges;         // (vi.x, vi.y, vj.x, vj.y): nr straddle-only edges, then nf full
     float lbx, lby, csx, csy;    // resolution = query grid resolution * 2^k
     int res;
+    unsigned long long* tests;   // exact edge tests counted here, or null
 };
 
 // Per-axis tile transforms of a raster canvas.

@@ -76,9 +76,11 @@ struct IndexMapper {
 template <class H>
 __device__ __forceinline__ void exact_list(const ExactIndex& ix, int cell, float x, float y, float v, const H& h) {
     const int s = __ldg(ix.cell_start + cell), e = __ldg(ix.cell_start + cell + 1);
+    unsigned ntests = 0;
     for (int k = s; k < e; ++k) {
         const int4 en = __ldg(ix.entries + k);
         if (en.y < 0) { h.add(en.x, v); continue; }
+        ntests += (unsigned)(en.y + en.z);
         const float4* E = ix.edges + en.w;
         bool c = false;
         for (int r = 0; r < en.y; ++r) {
@@ -91,6 +93,7 @@ __device__ __forceinline__ void exact_list(const ExactIndex& ix, int cell, float
         }
         if (c) h.add(en.x, v);
     }
+    if (ix.tests && ntests) atomicAdd(ix.tests, (unsigned long long)ntests);
 }
 
 template <class H>

@@ -1466,6 +1466,18 @@ void exact_qbox(rj_ctx* ctx) {
     ctx->qbox = make_float4((float)(bb[0] - m), (float)(bb[1] - m), (float)(bb[2] + m), (float)(bb[3] + m));
 }
 
+// RJ_FLAG_COUNT_EDGE_TESTS: a zeroed device counter for the exact tests of
+// this query (read back into rj_timings.edge_tests).
+int edge_test_counter(rj_ctx* ctx, const rj_query* q, ExactIndex& ix) {
+    ix.tests = nullptr;
+    if (!(q->flags & RJ_FLAG_COUNT_EDGE_TESTS) || ctx->capturing) return RJ_OK;
+    int rc;
+    if ((rc = scratch_t(ctx, "edge_tests", 1, &ctx->edge_tests_dev))) return rc;
+    RJ_CUDA(cudaMemsetAsync(ctx->edge_tests_dev, 0, sizeof(unsigned long long), ctx->stream));
+    ix.tests = ctx->edge_tests_dev;
+    return RJ_OK;
+}
+
 int exec_index(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     int rc;
     exact_qbox(ctx);
@@ -1485,6 +1497,7 @@ int exec_index(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     } else {
         ExactIndex ix{};
         if ((rc = build_exact(ctx, q->grid_res, ix))) return rc;
+        if ((rc = edge_test_counter(ctx, q, ix))) return rc;
         es.ph->mark(2);
         // the lean pass over the grid's cell labels; else the generic pass
         bool lean = false;
@@ -1520,6 +1533,7 @@ int exec_hybrid(rj_ctx* ctx, const rj_query* q, ExecState& es) {
     ExactIndex ix{};
     // refinement of the query grid for the exact tests (RJ_TUNE_HYBRID_EXACT_SCALE)
     if ((rc = build_exact(ctx, q->grid_res, ix, ctx->hybrid_exact_scale))) return rc;
+    if ((rc = edge_test_counter(ctx, q, ix))) return rc;
 
     // canvas: getResolution(bbox, fboSize) (HybridJoin.cpp:62-66, Utils.h:29-34)
     const double dx = ctx->ps->bbox[2] - ctx->ps->bbox[0], dy = ctx->ps->bbox[3] - ctx->ps->bbox[1];
@@ -1819,6 +1833,7 @@ int enqueue_query(rj_ctx* ctx, const rj_query* q, Phase& ph, unsigned long long*
         ctx->ps->exact.valid = false;
     }
     g_kernel_launches = 0;
+    ctx->edge_tests_dev = nullptr;
     unsigned long long* oc;
     unsigned long long* os;
     double* onf;
@@ -2250,6 +2265,8 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
     t.execute_ms = now_ms() - t0;
     t.accuracy = (q->function_type == RJ_RASTER_JOIN) ? (int)q->accuracy_m : 0;
     t.kernel_launches = g_kernel_launches;
+    if (ctx->edge_tests_dev)
+        RJ_CUDA(cudaMemcpy(&t.edge_tests, ctx->edge_tests_dev, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
     return RJ_OK;
 }
 

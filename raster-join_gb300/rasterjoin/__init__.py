@@ -52,6 +52,7 @@ FLAG_NO_CELL_CLASSIFY = 0x20
 FLAG_NO_CACHE = 0x40
 FLAG_FLAT_CANVAS = 0x80
 FLAG_TIERED_CANVAS = 0x100
+FLAG_COUNT_EDGE_TESTS = 0x200
 
 
 class RJError(RuntimeError):
@@ -98,7 +99,7 @@ class Timings(C.Structure):
                 ("pt_mem_ms", C.c_double), ("pt_render_ms", C.c_double), ("poly_mem_ms", C.c_double),
                 ("poly_render_ms", C.c_double), ("setup_ms", C.c_double), ("triangulation_ms", C.c_double),
                 ("poly_index_ms", C.c_double), ("backend_query_ms", C.c_double), ("accuracy", C.c_int32),
-                ("kernel_launches", C.c_int32)]
+                ("kernel_launches", C.c_int32), ("edge_tests", C.c_uint64)]
 
 
 class BatchStats(C.Structure):

@@ -592,3 +592,22 @@ def test_tiered_multi_tile_matches_flat(handler, c1):
     tier = _raster(handler, 2.5, max_fbo=6000)
     flat = _raster(handler, 2.5, rj.FLAG_FLAT_CANVAS, max_fbo=6000)
     np.testing.assert_array_equal(tier[0], flat[0])
+
+
+@pytest.mark.parametrize("fn", [rj.IndexJoinFn, rj.HybridJoinFn])
+def test_edge_test_counter(handler, c1, fn):
+    """RJ_FLAG_COUNT_EDGE_TESTS counts the exact tests without changing the
+    result; without the flag the count stays 0."""
+    pts, verts, pidx = c1
+    handler.setDataHandler(make_dh(pts, verts, pidx))
+    handler.setPolyIndexResolution(256)
+    base = handler.execute(fn)
+    assert handler.timings()["edge_tests"] == 0
+    handler.flags = rj.FLAG_COUNT_EDGE_TESTS
+    try:
+        got = handler.execute(fn)
+        n = handler.timings()["edge_tests"]
+    finally:
+        handler.flags = 0
+    np.testing.assert_array_equal(got.count, base.count)
+    assert 0 < n < 1000 * len(pts["xy"])
