@@ -356,7 +356,7 @@ def run_batched(rj, h, cum, n, nq):
                     "count or avg" % (nq, n),
         "point_queries": pq, "batched_ms": b_ms, "plain_ms": p_ms, "speedup": p_ms / b_ms,
         "batched_gpoints_s": pq / b_ms / 1e6, "plain_gpoints_s": pq / p_ms / 1e6,
-        "route": "every query on the lanes: rj_execute's device path on 4 streams with their own scratch, "
+        "route": "every query on the lanes: rj_execute's device path on 8 streams with their own scratch, "
                  "queued without host waits, one wait per batch",
         "kernel_launches": stats["kernel_launches"],
         "fused_variant": {"ms": f_ms, "speedup": p_ms / f_ms, "fused_queries": stats_f["fused"],

@@ -413,7 +413,7 @@ RJ_API int rj_cluster_points(rj_ctx *ctx, int32_t time_attrib, int32_t nbuckets,
                                     rows or on multi-tile canvases; the others
                                     take the lanes */
 /* By default every raster query of a batch takes rj_execute's device path on
- * one of four lanes: streams with their own scratch, so that the work of
+ * one of eight lanes: streams with their own scratch, so that the work of
  * several queries overlaps on the GPU (and, with RJ_BATCH_FUSE, with the
  * fused pass); each lane's outputs come back through pinned staging, with one
  * wait for the whole batch.  Queries of one polygon set share a lane.

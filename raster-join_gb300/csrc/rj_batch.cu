@@ -59,7 +59,7 @@ constexpr int kBatchHistCap = 4096;
 // scratch (keys suffixed with the lane) and error word, so that the device
 // work of several such queries -- and of the fused pass on the engine's own
 // stream -- overlaps on the GPU.
-constexpr int kLanes = 4;
+constexpr int kLanes = 8;
 
 struct Engine {
     rj_ctx* ctx = nullptr;

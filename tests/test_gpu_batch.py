@@ -322,7 +322,7 @@ def test_point_heavy_label_queries_leave_the_fused_pass(built):
 
 def test_lanes_equal_single(setup):
     """The default route: every raster query (and the error-bounds query)
-    runs rj_execute's device path on the lanes -- four streams with their own
+    runs rj_execute's device path on the lanes -- eight streams with their own
     scratch -- and gives the single-query results bit for bit, bounds
     included; the other join types still run through rj_execute in turn."""
     h, sets, _ = setup
