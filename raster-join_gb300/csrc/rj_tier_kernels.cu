@@ -48,9 +48,21 @@ __device__ __forceinline__ uint32_t bitrange(int a, int b) {
 // per row.  Crossings left of i_lo act from i_lo; those right of i_hi do not
 // matter.  R[0, nw) must be zero on entry and is zero again on return (the
 // scan clears what the toggles set), so consecutive rows need no clearing.
-template <class F>
+// The words of the row's column range as a mask (bits outside [i_lo, i_hi]
+// cleared): word w's mask.
+__device__ __forceinline__ uint32_t range_mask(int w, int w_lo, int i_lo, int i_hi) {
+    const int x0 = (w_lo + w) * 32;
+    const int a0 = max(i_lo - x0, 0), b0 = min(i_hi + 1 - x0, 32);
+    return a0 < b0 ? bitrange(a0, b0) : 0u;
+}
+
+// fu(w0, carry) takes a whole chunk of 32 words (w0 .. w0 + 31) that no
+// crossing of the row touches: every pixel of it has the coverage `carry`.
+// It is called by every lane (warp-uniform).
+template <class F, class FU>
 __device__ __forceinline__ void row_cover(int j, const int4* edge, int nb, bool overflow, const int2* pv, int n,
-                                          int i_lo, int i_hi, int w_lo, int nw, uint32_t* R, int lane, F&& f) {
+                                          int i_lo, int i_hi, int w_lo, int nw, uint32_t* R, int lane, F&& f,
+                                          FU&& fu) {
     const int32_t cy = j * kSub + kSub / 2;
     const int ne = overflow ? n : nb;
     for (int e = lane; e < ne; e += 32) {
@@ -72,6 +84,10 @@ __device__ __forceinline__ void row_cover(int j, const int4* edge, int nb, bool 
     for (int w0 = 0; w0 < nw; w0 += 32) {
         const int w = w0 + lane;
         const uint32_t t = w < nw ? R[w] : 0u;
+        if (__ballot_sync(0xffffffffu, t != 0u) == 0u) {
+            fu(w0, carry);
+            continue;
+        }
         const unsigned odd = __ballot_sync(0xffffffffu, (__popc(t) & 1) != 0);
         uint32_t x = t;   // inclusive prefix parity inside the word
         x ^= x << 1;
@@ -82,9 +98,7 @@ __device__ __forceinline__ void row_cover(int j, const int4* edge, int nb, bool 
         if (((unsigned)__popc(odd & ((1u << lane) - 1u)) & 1u) ^ carry) x = ~x;
         if (w < nw) {
             if (t) R[w] = 0u;
-            const int x0 = (w_lo + w) * 32;
-            const int a0 = max(i_lo - x0, 0), b0 = min(i_hi + 1 - x0, 32);
-            f(w, a0 < b0 ? (x & bitrange(a0, b0)) : 0u);
+            f(w, x & range_mask(w, w_lo, i_lo, i_hi));
         }
         carry ^= (unsigned)__popc(odd) & 1u;
     }
@@ -173,17 +187,36 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
         }
         __syncwarp();
         if (MODE != MODE_TIER_LABEL) {
+            // per 32-word chunk (warp-uniform): I already zero, U already the
+            // whole range -- both only ever move that way, so a chunk that no
+            // crossing touches needs no update once its flag is set
+            uint32_t izero = rows_ok ? 0u : 0xFFu, ufull = 0u;
             for (int r = 0; r < kTBand; ++r) {
                 const int j = jb + r;
                 const bool live = j <= a.resy - 1 && j >= j_lo && j <= j_hi;
                 if (live) {
-                    row_cover(j, my_edge, nb, overflow, pv, n, i_lo, i_hi, w_lo, nw, my_R, lane,
-                              [&](int w, uint32_t v) {
-                                  my_I[w] &= v;
-                                  if (MODE == MODE_TIER_CLASSIFY) my_U[w] |= v;
-                              });
+                    row_cover(
+                        j, my_edge, nb, overflow, pv, n, i_lo, i_hi, w_lo, nw, my_R, lane,
+                        [&](int w, uint32_t v) {
+                            my_I[w] &= v;
+                            if (MODE == MODE_TIER_CLASSIFY) my_U[w] |= v;
+                        },
+                        [&](int w0, uint32_t carry) {
+                            const uint32_t c = 1u << (w0 >> 5);
+                            const int w = w0 + lane;
+                            if (carry) {
+                                if (MODE == MODE_TIER_CLASSIFY && !(ufull & c)) {
+                                    if (w < nw) my_U[w] |= range_mask(w, w_lo, i_lo, i_hi);
+                                    ufull |= c;
+                                }
+                            } else if (!(izero & c)) {
+                                if (w < nw) my_I[w] = 0u;
+                                izero |= c;
+                            }
+                        });
                 } else {
                     for (int w = lane; w < nw; w += 32) my_I[w] = 0u;
+                    izero = 0xFFu;
                     __syncwarp();
                 }
             }
@@ -235,7 +268,7 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
         for (int r = 0; r < kTBand; ++r) {
             const int j = jb + r;
             if (!(j <= a.resy - 1 && j >= j_lo && j <= j_hi)) continue;
-            row_cover(j, my_edge, nb, overflow, pv, n, i_lo, i_hi, w_lo, nw, my_R, lane, [&](int w, uint32_t bits) {
+            auto visit = [&](int w, uint32_t bits) {
                 bits &= (MODE == MODE_TIER_LABEL) ? my_U[w] : ~full_halves(my_I[w]);
                 if (!bits) return;
                 const int x0 = (w_lo + w) * 32;
@@ -258,7 +291,13 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
                         }
                     }
                 }
-            });
+            };
+            row_cover(j, my_edge, nb, overflow, pv, n, i_lo, i_hi, w_lo, nw, my_R, lane, visit,
+                      [&](int w0, uint32_t carry) {
+                          // an untouched chunk: all covered (visit it) or none
+                          const int w = w0 + lane;
+                          if (carry && w < nw) visit(w, range_mask(w, w_lo, i_lo, i_hi));
+                      });
         }
         acc_c = warp_sum_u64(acc_c);
         if (MODE == MODE_TIER_LABEL) {
