@@ -59,7 +59,7 @@ constexpr int kBatchHistCap = 4096;
 // scratch (keys suffixed with the lane) and error word, so that the device
 // work of several such queries -- and of the fused pass on the engine's own
 // stream -- overlaps on the GPU.
-constexpr int kLanes = 8;
+constexpr int kLanes = 8;   // at most; rj_execute_batch's engine uses 8, a serving slot 4
 
 struct Engine {
     rj_ctx* ctx = nullptr;
@@ -73,6 +73,9 @@ struct Engine {
     BatchShape shape{256, 16384, 1};
     bool tuned = false;
     bool lanes = false;          // may queue queries on the lanes
+    int nlanes = kLanes;         // lanes in use (a serving slot takes fewer: its
+                                 // requests are small, and each lane's scratch is
+                                 // allocated on first use, mid-serving)
     int id = 0;                  // names the lanes' scratch apart from other engines'
     cudaStream_t lane_st[kLanes]{};
     int* lane_err = nullptr;     // device: one error word per lane
@@ -859,7 +862,7 @@ int lanes_enqueue(Engine& e, LaneRun& lr, int& launches) {
         const std::string saved_ns = ctx->scratch_ns;
         QPlan& p = *lr.q[i];
         auto it = lane_of.find(p.ps);
-        const int l = it != lane_of.end() ? it->second : (lane_of[p.ps] = (next++) % kLanes);
+        const int l = it != lane_of.end() ? it->second : (lane_of[p.ps] = (next++) % e.nlanes);
         ctx->stream = e.lane_st[l];
         ctx->d_err = e.lane_err + l;
         ctx->scratch_ns = "#e" + std::to_string(e.id) + "." + std::to_string(l);
@@ -1424,6 +1427,7 @@ int rj_server_create(rj_ctx* ctx, const rj_server_config* cfg, rj_server** out) 
         Engine* e = new Engine();
         int rc = engine_init(ctx, *e, nullptr, cap);
         e->lanes = !(s->cfg.batch_flags & (RJ_BATCH_FUSE | RJ_BATCH_FUSE_ALL | RJ_BATCH_NO_FUSE));
+        e->nlanes = 4;
         // the fused pass works in the slot's fixed arena; the lanes in scratch
         if (!rc && !e->lanes) rc = dev_alloc(ctx, e->ar.buf, cap);
         if (rc) {
