@@ -854,7 +854,8 @@ def run_config3(args):
             if eps == 1.0:
                 # both canvas forms of the 40000 x 40000 canvas: flat (a label
                 # map or count canvas per pixel) and tiered (16 x 16 blocks)
-                forms += [(rj.RasterJoinFn, rj.FLAG_FLAT_CANVAS), (rj.RasterJoinFn, rj.FLAG_TIERED_CANVAS)]
+                forms += [(rj.RasterJoinFn, rj.FLAG_FLAT_CANVAS), (rj.RasterJoinFn, rj.FLAG_TIERED_CANVAS),
+                          (rj.RasterJoinBoundFn, rj.FLAG_FLAT_CANVAS)]
             for fn, form in forms:
                 q = rj.default_query()
                 q.function_type = fn
@@ -877,6 +878,10 @@ def run_config3(args):
                 if fn == rj.RasterJoinBoundFn:
                     b = r.bounds.astype(np.int64)
                     rec["mean_hard_range"] = float(np.mean(b[2 * P:3 * P] + b[3 * P:]))
+                    if form == 0:
+                        eb_default = b
+                    else:                              # the flat canvas's bounds against the default form's
+                        rec["bounds_equal_default"] = bool(np.array_equal(b, eb_default))
                 out.append(rec)
         h.usePolySet(None)
         ps.close()

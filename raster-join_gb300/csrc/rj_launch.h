@@ -27,6 +27,9 @@ struct TierArgs {
     long long* bsum;             // [nblk] block fixed-point sums or null
     uint32_t* pcnt;              // [nslots * 256] pixel counts of mixed blocks
     long long* psum;             // [nslots * 256] or null
+    int outline;                 // classification: also make every block within two
+                                 // pixels of an edge mixed (the error-bound outline
+                                 // pass reads per-pixel counts there)
 };
 
 
@@ -55,6 +58,15 @@ struct PolyPassArgs {
     int2* info_b;                // j_lo, j_hi (rows whose centre can be crossed)
     int* nbands;                 // bands of kBand rows
     const int* band_start;       // exclusive scan of nbands, [T*P + 1]
+    // MODE_BOUNDS over a tiered canvas (with TierArgs::outline): per-pixel
+    // counts from the mixed blocks' slots, no per-pixel reduction (the tier
+    // reduction gives the counts); a lookup outside a mixed block sets err
+    int outline_rows;            // tier classification for error bounds: bands over
+                                 // every row an edge touches (k_poly_info)
+    const uint32_t* tier_code;   // [T][bh][bw] or null (flat canvas)
+    const uint32_t* tier_pcnt;
+    int tier_bw, tier_bh;
+    int* err;
 };
 
 size_t tier_smem_bytes();

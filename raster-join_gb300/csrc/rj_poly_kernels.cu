@@ -193,7 +193,8 @@ __global__ void k_poly_info(PolyPassArgs a) {
             int i_lo = (int)floordiv64((int64_t)xmin - kSub / 2 + kSub - 1, kSub);
             int i_hi = (int)floordiv64((int64_t)xmax - kSub / 2 + kSub - 1, kSub) - 1;
             int r_lo = j_lo, r_hi = j_hi;
-            if (MODE == MODE_BOUNDS) {
+            const bool outline = MODE == MODE_BOUNDS || (MODE == MODE_TIER_CLASSIFY && a.outline_rows);
+            if (outline) {
                 // rows whose pixel rectangle an edge may touch
                 r_lo = min(r_lo, (int)floordiv64((int64_t)ymin, kSub) - 1);
                 r_hi = max(r_hi, (int)floordiv64((int64_t)ymax, kSub) + 1);
@@ -203,7 +204,7 @@ __global__ void k_poly_info(PolyPassArgs a) {
             if (MODE >= MODE_TIER_CLASSIFY) r_lo &= ~15;   // bands on block rows
             i_lo = max(i_lo, 0);
             i_hi = min(i_hi, a.resx - 1);
-            if (r_lo <= r_hi && (MODE == MODE_BOUNDS || i_lo <= i_hi)) {
+            if (r_lo <= r_hi && (outline || i_lo <= i_hi)) {
                 nbands = (r_hi - r_lo + kBand) / kBand;
                 ia = make_int4(i_lo, i_hi, r_lo, r_hi);
                 ib = make_int2(j_lo, j_hi);
@@ -322,6 +323,7 @@ k_poly_pass(PolyPassArgs a) {
                 // pixel i is covered when an odd number of crossings lie at or
                 // left of it: with the crossings sorted, [c0, c1), [c2, c3), ...
                 auto visit = [&](int i) {
+                    if (MODE == MODE_BOUNDS && a.tier_code) return;   // counts: the tier reduction
                     const size_t pix = tile_off + (size_t)j * a.resx + i;
                     if (a.border) {
                         uint32_t w = __ldg(a.border + ((size_t)j * a.border_words + (i >> 5)));
@@ -381,8 +383,19 @@ k_poly_pass(PolyPassArgs a) {
                     int ia0 = max((int)floorf(xa) - 1, 0);
                     int ib0 = min((int)floorf(xb) + 1, a.resx - 1);
                     for (int i = ia0; i <= ib0; ++i) {
-                        const size_t pix = tile_off + (size_t)j * a.resx + i;
-                        uint32_t val = __ldg(a.canvas_c + pix);
+                        uint32_t val;
+                        if (a.tier_code) {
+                            // the pixel's count in its mixed block's slot
+                            const size_t b = (size_t)t * a.tier_bw * a.tier_bh + (size_t)(j >> 4) * a.tier_bw + (i >> 4);
+                            const uint32_t code = __ldg(a.tier_code + b);
+                            if (!(code & kTierMixed) || code >= kTierMulti) {
+                                atomicOr(a.err, 4);   // never: such blocks are made mixed
+                                continue;
+                            }
+                            val = __ldg(a.tier_pcnt + (size_t)(code & ~kTierMixed) * 256 + (size_t)(j & 15) * 16 + (i & 15));
+                        } else {
+                            val = __ldg(a.canvas_c + tile_off + (size_t)j * a.resx + i);
+                        }
                         if (val == 0) continue;
                         if (a.line_filter) {
                             // varying interpolation along the line (projection of

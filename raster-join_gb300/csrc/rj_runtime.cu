@@ -739,7 +739,7 @@ int tier_lean_pass(rj_ctx* ctx, const DevFilter& f, const RasterPlan& rp, const 
                    bool label, size_t nblk, size_t spx, ExecState& es, bool* done);   // below
 
 int exec_raster_tier(rj_ctx* ctx, const rj_query* q, const RasterPlan& rp, const DevFilter& f, ExecState& es,
-                     PolyPassArgs& a, const CanvasXf& cx, uint64_t ckey) {
+                     PolyPassArgs& a, const CanvasXf& cx, uint64_t ckey, bool bounds) {
     int rc;
     TierArgs tr{};
     tr.bw = (rp.resx + 15) / 16;
@@ -756,10 +756,15 @@ int exec_raster_tier(rj_ctx* ctx, const rj_query* q, const RasterPlan& rp, const
     if ((rc = scratch_t(ctx, "tier_tmp", (size_t)scan_tmp_ints((int)nblk), &tmp))) return rc;
     if ((rc = scratch_t(ctx, "tier_cnt", 3, &cnt))) return rc;
     tr.slot = slot;
+    // error bounds: the blocks the outline pass reads are mixed too
+    tr.outline = bounds ? 1 : 0;
     RJ_CUDA(cudaMemsetAsync(tr.full, 0xFF, nblk * 4, ctx->stream));
     RJ_CUDA(cudaMemsetAsync(tr.mixed, 0, nblk * 4, ctx->stream));
     RJ_CUDA(cudaMemsetAsync(cnt, 0, 3 * 8, ctx->stream));
-    if ((rc = poly_pass(ctx, MODE_TIER_CLASSIFY, a, &tr))) return rc;
+    a.outline_rows = tr.outline;
+    rc = poly_pass(ctx, MODE_TIER_CLASSIFY, a, &tr);
+    a.outline_rows = 0;
+    if (rc) return rc;
     if (!launch_exclusive_scan((const int*)tr.mixed, slot, (int)nblk, tmp, ctx->stream))
         return fail(ctx, RJ_E_INVALID, "tier scan failed");
     launch_tier_codes(tr, nblk, cnt, ctx->sms, ctx->stream);
@@ -768,7 +773,8 @@ int exec_raster_tier(rj_ctx* ctx, const rj_query* q, const RasterPlan& rp, const
     RJ_CUDA(cudaMemcpyAsync(&nslots, slot + nblk, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     RJ_CUDA(cudaStreamSynchronize(ctx->stream));
     const size_t spx = (size_t)std::max(nslots, 1) * 256;
-    bool label = !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->ps->overlap_on(ckey) != 1 && ctx->ps->P <= kMaxLabelPolys;
+    bool label = !bounds && !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->ps->overlap_on(ckey) != 1 &&
+                 ctx->ps->P <= kMaxLabelPolys;
     if (label) {
         if ((rc = scratch_t(ctx, "tier_plabel", spx, &tr.plabel))) return rc;
         RJ_CUDA(cudaMemsetAsync(tr.plabel, 0xFF, spx * 2, ctx->stream));
@@ -817,6 +823,18 @@ int exec_raster_tier(rj_ctx* ctx, const rj_query* q, const RasterPlan& rp, const
     a.canvas_s = nullptr;
     a.label = nullptr;
     if ((rc = poly_pass(ctx, MODE_TIER_REDUCE, a, &tr))) return rc;
+    if (bounds) {
+        // the outline pass of the error bounds over the mixed blocks' counts
+        a.tier_code = tr.code;
+        a.tier_pcnt = tr.pcnt;
+        a.tier_bw = tr.bw;
+        a.tier_bh = tr.bh;
+        a.err = ctx->d_err;
+        rc = poly_pass(ctx, MODE_BOUNDS, a);
+        a.tier_code = nullptr;
+        a.tier_pcnt = nullptr;
+        if (rc) return rc;
+    }
     es.ph->mark(4);
     return RJ_OK;
 }
@@ -1406,8 +1424,7 @@ int exec_raster(rj_ctx* ctx, const rj_query* q, ExecState& es, bool bounds) {
 
     const uint64_t ckey = canvas_key(rp.colxf, rp.rowxf, rp.resx, rp.resy);
     const uint64_t rows = std::min(ctx->row1, ctx->npts) - std::min(ctx->row0, ctx->npts);
-    if (!bounds && query_tier(q->flags, npix, rows))
-        return exec_raster_tier(ctx, q, rp, f, es, a, cx, ckey);
+    if (query_tier(q->flags, npix, rows)) return exec_raster_tier(ctx, q, rp, f, es, a, cx, ckey, bounds);
     bool use_label = !bounds && !(q->flags & RJ_FLAG_FORCE_CANVAS) && ctx->ps->overlap_on(ckey) != 1 &&
                      ctx->ps->P <= kMaxLabelPolys;
     if (use_label) {
@@ -2239,6 +2256,7 @@ int rj_execute(rj_ctx* ctx, const rj_query* q, rj_result* res) {
     ph.mark(5);
     RJ_CUDA(cudaStreamSynchronize(ctx->stream));
     RJ_CUDA(cudaGetLastError());
+    if (derr & 4) return fail(ctx, RJ_E_INVALID, "error-bound outline read outside the tiered canvas's slots");
     if (derr) return fail(ctx, RJ_E_TIMEOUT, "a bounded device wait ran out (status 0x%x)", derr);
     decode_result(P, hc.data(), hq.data(), hnf.data(), ctx->sum_shift, hb.empty() ? nullptr : hb.data(), res);
     ctx->last_fixed.assign(hq.begin(), hq.end());

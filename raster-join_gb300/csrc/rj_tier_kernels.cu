@@ -176,6 +176,46 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
         const bool overflow = nb > kTEdgeCap;
         __syncwarp();
 
+        if (MODE == MODE_TIER_CLASSIFY && tr.outline) {
+            // blocks within two pixels of an edge near this band (rows
+            // jb - 2 .. jb + 17) become mixed: the error-bound outline pass
+            // reads per-pixel counts up to a pixel beside each edge, rows one
+            // beyond the polygon's included
+            const float ylo = (float)(jb - 2), yhi = (float)(jb + kTBand + 2);
+            const int ne = overflow ? n : nb;
+            for (int e = lane; e < ne; e += 32) {
+                int4 q;
+                if (!overflow) {
+                    q = my_edge[e];
+                } else {
+                    const int2 A = pv[e];
+                    const int2 B = pv[(e + 1 == n) ? 0 : e + 1];
+                    q = make_int4(A.x, A.y, B.x, B.y);
+                }
+                const float ax = q.x * (1.0f / kSub), ay = q.y * (1.0f / kSub);
+                const float bx = q.z * (1.0f / kSub), by = q.w * (1.0f / kSub);
+                const float y0 = fmaxf(fminf(ay, by), ylo), y1 = fminf(fmaxf(ay, by), yhi);
+                if (!(y0 <= y1)) continue;
+                float x0, x1;
+                if (ay == by) {
+                    x0 = fminf(ax, bx);
+                    x1 = fmaxf(ax, bx);
+                } else {
+                    const float ta = fminf(fmaxf((y0 - ay) / (by - ay), 0.0f), 1.0f);
+                    const float tb = fminf(fmaxf((y1 - ay) / (by - ay), 0.0f), 1.0f);
+                    const float xa = ax + (bx - ax) * ta, xb = ax + (bx - ax) * tb;
+                    x0 = fminf(xa, xb);
+                    x1 = fmaxf(xa, xb);
+                }
+                const int c0 = max((int)floorf(x0) - 2, 0), c1 = min((int)floorf(x1) + 2, a.resx - 1);
+                const int r0 = max((int)floorf(y0) - 2, 0), r1 = min((int)floorf(y1) + 2, a.resy - 1);
+                if (c0 > c1 || r0 > r1) continue;
+                const size_t tile0 = (size_t)t * tr.bw * tr.bh;
+                for (int br2 = r0 >> 4; br2 <= (r1 >> 4); ++br2)
+                    for (int bc = c0 >> 4; bc <= (c1 >> 4); ++bc) tr.mixed[tile0 + (size_t)br2 * tr.bw + bc] = 1u;
+            }
+        }
+
         // I: pixels covered on every row of the block row; U: on some row
         const int nw = w_hi - w_lo + 1;
         const bool rows_ok = jb + kTBand - 1 <= a.resy - 1;

@@ -96,3 +96,34 @@ def test_every_tier_shape_matches_oracle(handler, sets, fbo, name, filters):
         handler.max_fbo_size = 8192
     assert taken == 3
     assert want[0].sum() > 0
+
+
+@pytest.mark.parametrize("fbo", [8192, 2100])
+@pytest.mark.parametrize("name", ["voronoi", "stars"])
+@pytest.mark.parametrize("line_filter", [False, True])
+def test_tiered_error_bounds_match_oracle(handler, sets, fbo, name, line_filter):
+    """The error-bounds join on a tiered canvas: the blocks within two pixels
+    of an edge keep per-pixel counts, so the outline pass reads the same
+    counts as on a flat canvas; counts and bounds equal the oracle's, with and
+    without the reference's 0.5 px fragment filter, on one tile and 3 x 3."""
+    verts, pidx = sets[name]
+    bb = (verts[:, 0].min(), verts[:, 1].min())
+    seams_x = [float(bb[0]) + k * fbo * 1.0 for k in (1, 2)] if fbo < 8192 else []
+    seams_y = [float(bb[1]) + k * fbo * 1.0 for k in (1, 2)] if fbo < 8192 else []
+    pts = _table(200_003, 83, seams_x, seams_y)
+    handler.setDataHandler(_dh(pts, verts, pidx, False))
+    handler.setCellSize(1.0)
+    handler.max_fbo_size = fbo
+    want = oracle.raster_join(pts["xy"], verts, pidx, 1.0, max_res=fbo, bounds=True, line_filter=line_filter)
+    handler.flags = rj.FLAG_TIERED_CANVAS | (rj.FLAG_LINE_FILTER if line_filter else 0)
+    try:
+        got = handler.execute(rj.RasterJoinBoundFn)
+        flat_flags = rj.FLAG_FLAT_CANVAS | (rj.FLAG_LINE_FILTER if line_filter else 0)
+        handler.flags = flat_flags
+        flat = handler.execute(rj.RasterJoinBoundFn)
+    finally:
+        handler.flags = 0
+        handler.max_fbo_size = 8192
+    np.testing.assert_array_equal(got.count, want[0])
+    np.testing.assert_array_equal(got.bounds, want[2])
+    np.testing.assert_array_equal(flat.bounds, want[2])
