@@ -16,10 +16,22 @@
 // polygon areas.
 //
 // One warp per (tile, polygon, band of 16 rows); bands are aligned to block
-// rows.  Per band the warp builds two pixel bitmaps over the polygon's
-// column range: I = pixels covered on all 16 rows, U = pixels covered on any
-// row.  A block column with all 16 bits of I set is full for the polygon;
-// one with bits of U set but not full is mixed.
+// rows.  The work of a band is proportional to the crossings of its rows and
+// to the blocks the polygon's outline passes through (plus one entry per full
+// block), not to the pixels of its area:
+//   * sweep 1 -- every crossing of a live row toggles one bit of a per-row
+//     block bitmap (at the first block whose first pixel lies at or right of
+//     it) and, when it falls strictly inside a block, flags that block; a
+//     prefix XOR over the bitmap gives each block's coverage at its first
+//     pixel, which holds for the whole block row unless the block is flagged.
+//     Over the 16 rows: I = blocks covered throughout (full for the polygon),
+//     U = blocks the polygon covers somewhere.
+//   * the blocks whose pixels matter (labels: U and mixed; reduce: U and not
+//     full) are listed, up to 64 at a time; sweep 2 toggles per-pixel bits of
+//     the listed blocks only, and their 16-bit row masks follow from the
+//     block's first-pixel coverage and a 16-bit prefix XOR;
+//   * the listed blocks' pixel slots are then read or written by the whole
+//     warp, eight pixels a lane with vector loads and stores.
 #include "rj_device.cuh"
 #include "rj_launch.h"
 #include "rj_point_map.cuh"
@@ -31,83 +43,43 @@ namespace {
 constexpr int kTW = 8;            // warps per block
 constexpr int kTBand = 16;        // rows per work item (one block row)
 constexpr int kTEdgeCap = 256;    // staged edges per warp
-constexpr int kTWords = 256;      // bitmap words per warp: 8192 pixel columns
-constexpr size_t kTierSmem = (size_t)kTW * (kTEdgeCap * sizeof(int4) + 3 * kTWords * sizeof(uint32_t));
+constexpr int kTBW = 16;          // block-bitmap words per row: 512 block columns = 8192 pixels
+constexpr int kTList = 64;        // blocks whose pixels one round visits
+
+// Per-warp shared memory.  X, C and M are zero between work items.
+struct TierWarp {
+    int4 edge[kTEdgeCap];               // staged edges of the band
+    uint32_t X[kTBand * kTBW];          // block toggles, then coverage at each block's first pixel
+    uint32_t C[kTBand * kTBW];          // blocks with a crossing inside (pixel offsets 1..15)
+    uint32_t M[kTList * kTBand / 2];    // listed blocks: pixel toggles, then row masks (two rows a word)
+    uint16_t list[kTList];              // listed block columns (relative to bc_lo)
+    uint8_t map[kTBW * 32];             // block column -> list index, 0xFF when not listed
+};
+static_assert(sizeof(TierWarp) % 16 == 0, "TierWarp keeps 16-byte alignment");
+constexpr size_t kTierSmem = (size_t)kTW * sizeof(TierWarp);
 
 // bits [a, b) of a word, 0 <= a < b <= 32
 __device__ __forceinline__ uint32_t bitrange(int a, int b) {
     return (b >= 32 ? 0xFFFFFFFFu : ((1u << b) - 1u)) & ~((1u << a) - 1u);
 }
-
-// Coverage of row j's pixel centres in [i_lo, i_hi], word by word: f(w, bits)
-// receives word w of the row (bit b = pixel (w_lo + w) * 32 + b), called by
-// lane w % 32.  A pixel is covered when an odd number of the row's crossings
-// lie at or left of it (crossing pixel L = first pixel right of the crossing,
-// exact integer arithmetic), so each crossing toggles one bit of R and a
-// prefix XOR over the row gives the coverage: no sorting, O(crossings + words)
-// per row.  Crossings left of i_lo act from i_lo; those right of i_hi do not
-// matter.  R[0, nw) must be zero on entry and is zero again on return (the
-// scan clears what the toggles set), so consecutive rows need no clearing.
-// The words of the row's column range as a mask (bits outside [i_lo, i_hi]
-// cleared): word w's mask.
-__device__ __forceinline__ uint32_t range_mask(int w, int w_lo, int i_lo, int i_hi) {
-    const int x0 = (w_lo + w) * 32;
-    const int a0 = max(i_lo - x0, 0), b0 = min(i_hi + 1 - x0, 32);
-    return a0 < b0 ? bitrange(a0, b0) : 0u;
+// inclusive prefix parity: bit k = XOR of bits 0..k
+__device__ __forceinline__ uint32_t prefix_xor(uint32_t x) {
+    x ^= x << 1;
+    x ^= x << 2;
+    x ^= x << 4;
+    x ^= x << 8;
+    x ^= x << 16;
+    return x;
 }
 
-// fu(w0, carry) takes a whole chunk of 32 words (w0 .. w0 + 31) that no
-// crossing of the row touches: every pixel of it has the coverage `carry`.
-// It is called by every lane (warp-uniform).
-template <class F, class FU>
-__device__ __forceinline__ void row_cover(int j, const int4* edge, int nb, bool overflow, const int2* pv, int n,
-                                          int i_lo, int i_hi, int w_lo, int nw, uint32_t* R, int lane, F&& f,
-                                          FU&& fu) {
-    const int32_t cy = j * kSub + kSub / 2;
-    const int ne = overflow ? n : nb;
-    for (int e = lane; e < ne; e += 32) {
-        int4 q;
-        if (!overflow) {
-            q = edge[e];
-        } else {
-            const int2 A = pv[e];
-            const int2 B = pv[(e + 1 == n) ? 0 : e + 1];
-            q = make_int4(A.x, A.y, B.x, B.y);
-        }
-        if (cross_row(q.y, q.w, cy)) {
-            const int L = max(cross_L(q.x, q.y, q.z, q.w, cy), i_lo);
-            if (L <= i_hi) atomicXor(R + ((L >> 5) - w_lo), 1u << (L & 31));
-        }
-    }
-    __syncwarp();
-    uint32_t carry = 0u;   // parity of the toggles in the words before this chunk
-    for (int w0 = 0; w0 < nw; w0 += 32) {
-        const int w = w0 + lane;
-        const uint32_t t = w < nw ? R[w] : 0u;
-        if (__ballot_sync(0xffffffffu, t != 0u) == 0u) {
-            fu(w0, carry);
-            continue;
-        }
-        const unsigned odd = __ballot_sync(0xffffffffu, (__popc(t) & 1) != 0);
-        uint32_t x = t;   // inclusive prefix parity inside the word
-        x ^= x << 1;
-        x ^= x << 2;
-        x ^= x << 4;
-        x ^= x << 8;
-        x ^= x << 16;
-        if (((unsigned)__popc(odd & ((1u << lane) - 1u)) & 1u) ^ carry) x = ~x;
-        if (w < nw) {
-            if (t) R[w] = 0u;
-            f(w, x & range_mask(w, w_lo, i_lo, i_hi));
-        }
-        carry ^= (unsigned)__popc(odd) & 1u;
-    }
-    __syncwarp();
-}
-
-// the 16-pixel halves of a word whose 16 bits of v are all set, as a mask
-__device__ __forceinline__ uint32_t full_halves(uint32_t v) {
-    return ((v & 0xFFFFu) == 0xFFFFu ? 0xFFFFu : 0u) | ((v >> 16) == 0xFFFFu ? 0xFFFF0000u : 0u);
+// Rows [r0, r1] of the band (relative to jb) whose centre line the edge
+// with fixed-point ends y = ay, by crosses: ylo < cy <= yhi, cy = j * 256 + 128.
+__device__ __forceinline__ void edge_rows(int32_t ay, int32_t by, int jb, int& r0, int& r1) {
+    const int64_t ylo = min(ay, by), yhi = max(ay, by);
+    const int64_t a0 = ((ylo - kSub / 2) >> kSubpixelBits) + 1 - jb;
+    const int64_t a1 = ((yhi - kSub / 2) >> kSubpixelBits) - jb;
+    r0 = (int)(a0 < 0 ? 0 : a0);
+    r1 = (int)(a1 > kTBand - 1 ? kTBand - 1 : a1);
 }
 
 template <int MODE>
@@ -117,12 +89,14 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
     const unsigned FULL = 0xffffffffu;
     const int TP = a.T * a.P;
     const int total = a.band_start[TP];
-    int4* my_edge = s_tier + (size_t)warp * kTEdgeCap;
-    uint32_t* my_I = reinterpret_cast<uint32_t*>(s_tier + (size_t)kTW * kTEdgeCap) + (size_t)warp * 3 * kTWords;
-    uint32_t* my_U = my_I + kTWords;   // label pass: the mixed blocks' mask instead
-    uint32_t* my_R = my_U + kTWords;
-    for (int w = lane; w < kTWords; w += 32) my_R[w] = 0u;   // row_cover keeps it zero between rows
+    TierWarp& S = reinterpret_cast<TierWarp*>(s_tier)[warp];
+    for (int w = lane; w < kTBand * kTBW; w += 32) {
+        S.X[w] = 0u;
+        S.C[w] = 0u;
+    }
+    for (int w = lane; w < kTList * kTBand / 2; w += 32) S.M[w] = 0u;
     __syncwarp();
+    const int hw = lane & 15, half = lane >> 4;   // sweep 1: row 2k + half, block word hw
     for (;;) {
         int item = 0, tp = 0;
         if (lane == 0) {
@@ -150,8 +124,9 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
         const int n = __ldg(a.pindex + p + 1) - v0;
         const int2* pv = a.wv + (size_t)t * a.V + v0;
         const size_t blk0 = (size_t)t * tr.bw * tr.bh + (size_t)br * tr.bw;
-        const int w_lo = i_lo >> 5, w_hi = i_hi >> 5;
-        if (w_hi - w_lo >= kTWords) continue;            // never: resx <= 8192
+        const int bc_lo = i_lo >> 4;
+        const int nbc = (i_hi >> 4) - bc_lo + 1;        // block columns of the range (<= 512)
+        if (nbc > kTBW * 32) continue;                  // never: resx <= 8192
 
         // stage the edges that can cross a row centre of the band
         const int64_t band_lo = (int64_t)jb * kSub - kSub;
@@ -170,28 +145,26 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
             }
             const unsigned m = __ballot_sync(FULL, take);
             const int pos = nb + __popc(m & ((1u << lane) - 1u));
-            if (take && pos < kTEdgeCap) my_edge[pos] = e;
+            if (take && pos < kTEdgeCap) S.edge[pos] = e;
             nb += __popc(m);
         }
         const bool overflow = nb > kTEdgeCap;
+        const int ne = overflow ? n : nb;
         __syncwarp();
-
+        auto edge_at = [&](int e) -> int4 {
+            if (!overflow) return S.edge[e];
+            const int2 A = pv[e];
+            const int2 B = pv[(e + 1 == n) ? 0 : e + 1];
+            return make_int4(A.x, A.y, B.x, B.y);
+        };
         if (MODE == MODE_TIER_CLASSIFY && tr.outline) {
             // blocks within two pixels of an edge near this band (rows
             // jb - 2 .. jb + 17) become mixed: the error-bound outline pass
             // reads per-pixel counts up to a pixel beside each edge, rows one
             // beyond the polygon's included
             const float ylo = (float)(jb - 2), yhi = (float)(jb + kTBand + 2);
-            const int ne = overflow ? n : nb;
             for (int e = lane; e < ne; e += 32) {
-                int4 q;
-                if (!overflow) {
-                    q = my_edge[e];
-                } else {
-                    const int2 A = pv[e];
-                    const int2 B = pv[(e + 1 == n) ? 0 : e + 1];
-                    q = make_int4(A.x, A.y, B.x, B.y);
-                }
+                const int4 q = edge_at(e);
                 const float ax = q.x * (1.0f / kSub), ay = q.y * (1.0f / kSub);
                 const float bx = q.z * (1.0f / kSub), by = q.w * (1.0f / kSub);
                 const float y0 = fmaxf(fminf(ay, by), ylo), y1 = fminf(fmaxf(ay, by), yhi);
@@ -216,129 +189,207 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
             }
         }
 
-        // I: pixels covered on every row of the block row; U: on some row
-        const int nw = w_hi - w_lo + 1;
-        const bool rows_ok = jb + kTBand - 1 <= a.resy - 1;
-        for (int w = lane; w < nw; w += 32) {
-            const int x0 = (w_lo + w) * 32;
-            const int a0 = max(i_lo - x0, 0), b0 = min(i_hi + 1 - x0, 32);
-            my_I[w] = (rows_ok && a0 < b0) ? bitrange(a0, b0) : 0u;
-            my_U[w] = 0u;
-        }
-        __syncwarp();
-        if (MODE != MODE_TIER_LABEL) {
-            // per 32-word chunk (warp-uniform): I already zero, U already the
-            // whole range -- both only ever move that way, so a chunk that no
-            // crossing touches needs no update once its flag is set
-            uint32_t izero = rows_ok ? 0u : 0xFFu, ufull = 0u;
-            for (int r = 0; r < kTBand; ++r) {
-                const int j = jb + r;
-                const bool live = j <= a.resy - 1 && j >= j_lo && j <= j_hi;
-                if (live) {
-                    row_cover(
-                        j, my_edge, nb, overflow, pv, n, i_lo, i_hi, w_lo, nw, my_R, lane,
-                        [&](int w, uint32_t v) {
-                            my_I[w] &= v;
-                            if (MODE == MODE_TIER_CLASSIFY) my_U[w] |= v;
-                        },
-                        [&](int w0, uint32_t carry) {
-                            const uint32_t c = 1u << (w0 >> 5);
-                            const int w = w0 + lane;
-                            if (carry) {
-                                if (MODE == MODE_TIER_CLASSIFY && !(ufull & c)) {
-                                    if (w < nw) my_U[w] |= range_mask(w, w_lo, i_lo, i_hi);
-                                    ufull |= c;
-                                }
-                            } else if (!(izero & c)) {
-                                if (w < nw) my_I[w] = 0u;
-                                izero |= c;
-                            }
-                        });
-                } else {
-                    for (int w = lane; w < nw; w += 32) my_I[w] = 0u;
-                    izero = 0xFFu;
-                    __syncwarp();
+        __syncwarp();                                   // staged edges read; the next item restages them
+        if (nbc <= 0) continue;                         // outline rows only
+
+        // rows of the band inside the polygon's crossing rows and the canvas
+        const int rl = max(j_lo, jb) - jb, rh = min(min(j_hi, a.resy - 1), jb + kTBand - 1) - jb;
+        const uint32_t live = rl <= rh ? bitrange(rl, rh + 1) : 0u;
+        if (!live) continue;
+
+        // sweep 1: block toggles and inside-crossing flags per live row
+        for (int e = lane; e < ne; e += 32) {
+            const int4 q = edge_at(e);
+            int r0, r1;
+            edge_rows(q.y, q.w, jb, r0, r1);
+            for (int r = r0; r <= r1; ++r) {
+                const int32_t cy = (jb + r) * kSub + kSub / 2;
+                if (!((live >> r) & 1u) || !cross_row(q.y, q.w, cy)) continue;
+                const int L = max(cross_L(q.x, q.y, q.z, q.w, cy), i_lo);
+                if (L > i_hi) continue;
+                const int rb = ((L + 15) >> 4) - bc_lo;
+                if (rb < nbc) atomicXor(&S.X[r * kTBW + (rb >> 5)], 1u << (rb & 31));
+                if (L & 15) {
+                    const int cb = (L >> 4) - bc_lo;
+                    atomicOr(&S.C[r * kTBW + (cb >> 5)], 1u << (cb & 31));
                 }
             }
         }
+        __syncwarp();
+        // block columns [fb, lb] lie wholly inside [i_lo, i_hi]; word hw's valid blocks
+        const int fb = ((i_lo + 15) >> 4) - bc_lo, lb = ((i_hi + 1) >> 4) - 1 - bc_lo;
+        const int wa = max(fb - hw * 32, 0), wb = min(lb - hw * 32 + 1, 32);
+        const int va = min(nbc - hw * 32, 32);
+        const uint32_t valid = va > 0 ? bitrange(0, va) : 0u;
+        uint32_t I = (live == 0xFFFFu && wa < wb) ? bitrange(wa, wb) : 0u, U = 0u;
+        #pragma unroll 2
+        for (int r2 = 0; r2 < kTBand; r2 += 2) {
+            const int r = r2 + half;
+            const int idx = r * kTBW + hw;
+            const uint32_t tg = S.X[idx], c = S.C[idx];
+            uint32_t x = prefix_xor(tg);
+            const unsigned odd = __ballot_sync(FULL, (__popc(tg) & 1) != 0);
+            if (__popc((odd >> (half * 16)) & ((1u << hw) - 1u)) & 1) x = ~x;
+            S.X[idx] = x;
+            S.C[idx] = 0u;
+            if ((live >> r) & 1u) {
+                I &= x & ~c;
+                U |= (x | c) & valid;
+            }
+        }
+        I &= __shfl_xor_sync(FULL, I, 16);
+        U |= __shfl_xor_sync(FULL, U, 16);
+        const int nbw = (nbc + 31) >> 5;
+
         if (MODE == MODE_TIER_CLASSIFY) {
             // block columns: full for p, or touched (mixed)
-            const int bc_lo = i_lo >> 4, bc_hi = i_hi >> 4;
-            for (int bc = bc_lo + lane; bc <= bc_hi; bc += 32) {
-                const int w = (bc >> 1) - w_lo;
-                const int sh = (bc & 1) * 16;
-                const uint32_t iv = (my_I[w] >> sh) & 0xFFFFu, uv = (my_U[w] >> sh) & 0xFFFFu;
-                const size_t b = blk0 + bc;
-                if (iv == 0xFFFFu) {
+            for (int k = 0; k < nbw; ++k) {
+                const uint32_t Iw = __shfl_sync(FULL, I, k), Uw = __shfl_sync(FULL, U, k);
+                if (!Uw) continue;
+                const int rel = k * 32 + lane;
+                if (!((Uw >> lane) & 1u)) continue;
+                const size_t b = blk0 + bc_lo + rel;
+                if ((Iw >> lane) & 1u) {
                     if (atomicCAS(tr.full + b, kTierEmpty, (uint32_t)p) != kTierEmpty) atomicExch(tr.full + b, kTierMulti);
-                } else if (uv) {
+                } else {
                     tr.mixed[b] = 1u;
                 }
             }
+            for (int w = lane; w < kTBand * kTBW; w += 32) S.X[w] = 0u;
+            __syncwarp();
             continue;
         }
 
-        // ---- canvas modes
         unsigned long long acc_c = 0;
         long long acc_s = 0;
-        if (MODE == MODE_TIER_REDUCE) {
-            // full blocks of p: one block sum each
-            const int bc_lo = i_lo >> 4, bc_hi = i_hi >> 4;
-            for (int bc = bc_lo + lane; bc <= bc_hi; bc += 32) {
-                const int w = (bc >> 1) - w_lo;
-                if (((my_I[w] >> ((bc & 1) * 16)) & 0xFFFFu) == 0xFFFFu) {
-                    acc_c += __ldg(tr.bcnt + blk0 + bc);
-                    if (tr.bsum) acc_s += __ldg(tr.bsum + blk0 + bc);
+        // listed blocks: reduce -- covered, not full (full ones take the
+        // block sums); labels -- covered and mixed
+        uint32_t Lw = 0u;   // lane k < nbw: listed blocks of word k
+        for (int k = 0; k < nbw; ++k) {
+            const uint32_t Iw = __shfl_sync(FULL, I, k), Uw = __shfl_sync(FULL, U, k);
+            if (!Uw) continue;
+            const int rel = k * 32 + lane;
+            const size_t b = blk0 + bc_lo + rel;
+            bool take = false;
+            if (MODE == MODE_TIER_REDUCE) {
+                if ((Iw >> lane) & 1u) {
+                    acc_c += __ldg(tr.bcnt + b);
+                    if (tr.bsum) acc_s += __ldg(tr.bsum + b);
+                }
+                take = ((Uw & ~Iw) >> lane) & 1u;
+            } else {
+                take = ((Uw >> lane) & 1u) && __ldg(tr.mixed + b) != 0u;
+            }
+            const uint32_t m = __ballot_sync(FULL, take);
+            if (lane == k) Lw = m;
+        }
+        // list positions: exclusive prefix of the words' counts
+        const int cnt = lane < nbw ? __popc(Lw) : 0;
+        int pre = cnt;
+        #pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(FULL, pre, o);
+            if (lane >= o) pre += v;
+        }
+        const int nlist = __shfl_sync(FULL, pre, 31);
+        pre -= cnt;
+        for (int start = 0; start < nlist; start += kTList) {
+            const int nk = min(kTList, nlist - start);
+            for (int w = lane; w < kTBW * 32 / 4; w += 32) reinterpret_cast<uint32_t*>(S.map)[w] = 0xFFFFFFFFu;
+            __syncwarp();
+            if (lane < nbw && pre < start + nk && pre + cnt > start) {
+                uint32_t m = Lw;
+                int g = pre;
+                while (m && g < start + nk) {
+                    const int bit = __ffs(m) - 1;
+                    m &= m - 1u;
+                    if (g >= start) {
+                        S.map[lane * 32 + bit] = (uint8_t)(g - start);
+                        S.list[g - start] = (uint16_t)(lane * 32 + bit);
+                    }
+                    ++g;
                 }
             }
-        }
-        // covered pixels of the blocks that are not full for p (reduce) or of
-        // the mixed blocks (labels): the pixel slots.  keep[w]: the halves of
-        // word w whose pixels are visited, found once per band (labels: the
-        // mixed blocks; reduce: all but p's full blocks).
-        if (MODE == MODE_TIER_LABEL) {
-            for (int w = lane; w < nw; w += 32) {
-                const int bc = (w_lo + w) * 2;
-                const bool m0 = __ldg(tr.mixed + blk0 + bc) != 0;
-                const bool m1 = bc + 1 < tr.bw && __ldg(tr.mixed + blk0 + bc + 1) != 0;
-                my_U[w] = (m0 ? 0xFFFFu : 0u) | (m1 ? 0xFFFF0000u : 0u);
+            __syncwarp();
+            // sweep 2: pixel toggles of the listed blocks (crossings inside a
+            // block only; one at a block's first pixel is in X already)
+            for (int e = lane; e < ne; e += 32) {
+                const int4 q = edge_at(e);
+                int r0, r1;
+                edge_rows(q.y, q.w, jb, r0, r1);
+                for (int r = r0; r <= r1; ++r) {
+                    const int32_t cy = (jb + r) * kSub + kSub / 2;
+                    if (!((live >> r) & 1u) || !cross_row(q.y, q.w, cy)) continue;
+                    const int L = max(cross_L(q.x, q.y, q.z, q.w, cy), i_lo);
+                    if (L > i_hi || !(L & 15)) continue;
+                    const int k = S.map[(L >> 4) - bc_lo];
+                    if (k != 0xFF) atomicXor(&S.M[k * 8 + (r >> 1)], (1u << (L & 15)) << ((r & 1) * 16));
+                }
             }
             __syncwarp();
-        }
-        for (int r = 0; r < kTBand; ++r) {
-            const int j = jb + r;
-            if (!(j <= a.resy - 1 && j >= j_lo && j <= j_hi)) continue;
-            auto visit = [&](int w, uint32_t bits) {
-                bits &= (MODE == MODE_TIER_LABEL) ? my_U[w] : ~full_halves(my_I[w]);
-                if (!bits) return;
-                const int x0 = (w_lo + w) * 32;
+            // row masks: coverage at the block's first pixel, then the block's
+            // own crossings, clipped to [i_lo, i_hi]
+            for (int w = lane; w < nk * 8; w += 32) {
+                const int k = w >> 3, rp = (w & 7) * 2;
+                const int rel = S.list[k];
+                const int x0 = (bc_lo + rel) * 16;
+                const int ka = max(i_lo - x0, 0), kb = min(i_hi - x0, 15);
+                const uint32_t rng = bitrange(ka, kb + 1);
+                const uint32_t tg = S.M[w];
+                uint32_t out = 0u;
                 #pragma unroll
-                for (int half = 0; half < 2; ++half) {
-                    uint32_t hb = (bits >> (half * 16)) & 0xFFFFu;
-                    if (!hb) continue;
-                    const size_t b = blk0 + (x0 >> 4) + half;
-                    const size_t base = (size_t)__ldg(tr.slot + b) * 256 + (size_t)(j & 15) * 16;
-                    while (hb) {
-                        const int bit = __ffs(hb) - 1;
-                        hb &= hb - 1u;
-                        const size_t q = base + bit;   // (x0 + 16 * half + bit) & 15 == bit
-                        if (MODE == MODE_TIER_LABEL) {
-                            tr.plabel[q] = (uint16_t)p;
-                            ++acc_c;
-                        } else {
-                            acc_c += __ldg(tr.pcnt + q);
-                            if (tr.psum) acc_s += __ldg(tr.psum + q);
+                for (int h = 0; h < 2; ++h) {
+                    const int r = rp + h;
+                    if (!((live >> r) & 1u)) continue;
+                    uint32_t x = prefix_xor((tg >> (h * 16)) & 0xFFFFu) & 0xFFFFu;
+                    if ((S.X[r * kTBW + (rel >> 5)] >> (rel & 31)) & 1u) x ^= 0xFFFFu;
+                    out |= (x & rng) << (h * 16);
+                }
+                S.M[w] = out;
+            }
+            __syncwarp();
+            // the listed blocks' pixels: lane = (row, half row of 8 pixels)
+            const int pr = lane >> 1, ph = (lane & 1) * 8;
+            #pragma unroll 4
+            for (int k = 0; k < nk; ++k) {
+                const uint32_t m8 = (S.M[k * 8 + (pr >> 1)] >> ((pr & 1) * 16 + ph)) & 0xFFu;
+                if (!m8) continue;
+                const size_t b = blk0 + bc_lo + S.list[k];
+                const size_t q = (size_t)__ldg(tr.slot + b) * 256 + (size_t)pr * 16 + ph;
+                if (MODE == MODE_TIER_LABEL) {
+                    uint16_t* dst = tr.plabel + q;
+                    if (m8 == 0xFFu) {
+                        const uint32_t pp = (uint32_t)p | ((uint32_t)p << 16);
+                        *reinterpret_cast<uint4*>(dst) = make_uint4(pp, pp, pp, pp);
+                    } else {
+                        #pragma unroll
+                        for (int i = 0; i < 8; ++i)
+                            if ((m8 >> i) & 1u) dst[i] = (uint16_t)p;
+                    }
+                    acc_c += (unsigned)__popc(m8);
+                } else {
+                    const uint4 c0 = __ldg(reinterpret_cast<const uint4*>(tr.pcnt + q));
+                    const uint4 c1 = __ldg(reinterpret_cast<const uint4*>(tr.pcnt + q + 4));
+                    acc_c += (unsigned long long)((m8 & 1u) ? c0.x : 0u) + ((m8 & 2u) ? c0.y : 0u) +
+                             ((m8 & 4u) ? c0.z : 0u) + ((m8 & 8u) ? c0.w : 0u) + ((m8 & 16u) ? c1.x : 0u) +
+                             ((m8 & 32u) ? c1.y : 0u) + ((m8 & 64u) ? c1.z : 0u) + ((m8 & 128u) ? c1.w : 0u);
+                    if (tr.psum) {
+                        const longlong2* ps = reinterpret_cast<const longlong2*>(tr.psum + q);
+                        #pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            const longlong2 v = __ldg(ps + i);
+                            if ((m8 >> (2 * i)) & 1u) acc_s += v.x;
+                            if ((m8 >> (2 * i + 1)) & 1u) acc_s += v.y;
                         }
                     }
                 }
-            };
-            row_cover(j, my_edge, nb, overflow, pv, n, i_lo, i_hi, w_lo, nw, my_R, lane, visit,
-                      [&](int w0, uint32_t carry) {
-                          // an untouched chunk: all covered (visit it) or none
-                          const int w = w0 + lane;
-                          if (carry && w < nw) visit(w, range_mask(w, w_lo, i_lo, i_hi));
-                      });
+            }
+            __syncwarp();   // every lane has read its masks
+            for (int w = lane; w < nk * 8; w += 32) S.M[w] = 0u;
+            __syncwarp();
         }
+        for (int w = lane; w < kTBand * kTBW; w += 32) S.X[w] = 0u;
+        __syncwarp();
         acc_c = warp_sum_u64(acc_c);
         if (MODE == MODE_TIER_LABEL) {
             if (lane == 0 && acc_c) atomicAdd(a.covered, acc_c);
