@@ -23,7 +23,7 @@ struct TierArgs {
     const int* slot;             // [nblk] exclusive scan of mixed
     uint32_t* code;              // [nblk] lookup code (full polygon / empty / multi / mixed | slot)
     uint16_t* plabel;            // [nslots * 256] pixel labels of mixed blocks
-    uint32_t* bcnt;              // [nblk] block point counts (canvas form)
+    uint32_t* bcnt;              // [nblk] point counts of the blocks neither mixed nor empty (canvas form)
     long long* bsum;             // [nblk] block fixed-point sums or null
     uint32_t* pcnt;              // [nslots * 256] pixel counts of mixed blocks
     long long* psum;             // [nslots * 256] or null

@@ -332,31 +332,42 @@ struct TierSplatMapper {
         if (px < 0 || px >= cx.resx || py < 0 || py >= cx.resy) return kNone;
         return (Key)py * (Key)cx.resx + (Key)px;
     }
-    __device__ __forceinline__ void pixel_add(size_t blk0, int px, int py, long long q) const {
-        const uint32_t code = __ldg(tr.code + blk0 + (size_t)(py >> 4) * tr.bw + (px >> 4));
-        if ((code & kTierMixed) && code < kTierMulti) {
-            const size_t at = (size_t)(code & ~kTierMixed) * 256 + (size_t)(py & 15) * 16 + (px & 15);
-            atomicAdd(tr.pcnt + at, 1u);
-            if (tr.psum) atomicAdd(reinterpret_cast<unsigned long long*>(tr.psum + at), (unsigned long long)q);
-        }
+    // A point's count (and sum) goes to the pixel slot of a mixed block, else
+    // to the block's total; a block no polygon reaches keeps nothing (no
+    // polygon reads it).
+    __device__ static __forceinline__ bool tier_mixed(uint32_t code) {
+        return (code & kTierMixed) && code < kTierMulti;
+    }
+    __device__ __forceinline__ void pixel_add(uint32_t code, int px, int py, long long q) const {
+        const size_t at = (size_t)(code & ~kTierMixed) * 256 + (size_t)(py & 15) * 16 + (px & 15);
+        atomicAdd(tr.pcnt + at, 1u);
+        if (tr.psum) atomicAdd(reinterpret_cast<unsigned long long*>(tr.psum + at), (unsigned long long)q);
     }
     template <class H>
     __device__ __forceinline__ void consume(bool valid, Key k, float x, float y, float v, const H& h,
                                             const DeferQ& dq) const {
         const bool one = valid && k < kMulti;
-        const unsigned active = __ballot_sync(0xffffffffu, one);
+        int px = 0, py = 0;
+        uint32_t b = 0, code = kTierEmpty;
         if (one) {
-            const long long q = (tr.bsum && isfinite(v)) ? fixed_value(v, scale) : 0ll;
-            const int px = (int)(k % (Key)cx.resx), py = (int)(k / (Key)cx.resx);
-            const uint32_t b = (uint32_t)((py >> 4) * tr.bw + (px >> 4));
+            px = (int)(k % (Key)cx.resx);
+            py = (int)(k / (Key)cx.resx);
+            b = (uint32_t)((py >> 4) * tr.bw + (px >> 4));
+            code = __ldg(tr.code + b);
+        }
+        const bool mixed = tier_mixed(code);
+        const bool blk = !mixed && code != kTierEmpty;
+        const long long q = ((mixed || blk) && tr.bsum && isfinite(v)) ? fixed_value(v, scale) : 0ll;
+        const unsigned active = __ballot_sync(0xffffffffu, blk);
+        if (blk) {
             const unsigned peers = __match_any_sync(active, b);
             const long long sum = group_sum(active, peers, q);
             if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) {
                 atomicAdd(tr.bcnt + b, (unsigned)__popc(peers));
                 if (tr.bsum) atomicAdd(reinterpret_cast<unsigned long long*>(tr.bsum + b), (unsigned long long)sum);
             }
-            pixel_add(0, px, py, q);
         }
+        if (mixed) pixel_add(code, px, py, q);
         if (valid && k == kMulti) map(x, y, v, h, dq);
     }
     template <class H>
@@ -364,11 +375,14 @@ struct TierSplatMapper {
         const size_t tile_blk = (size_t)tr.bw * tr.bh;
         const long long q = (tr.bsum && isfinite(v)) ? fixed_value(v, scale) : 0ll;
         canvas_visit(cx, x, y, [&](int t, int px, int py) {
-            const size_t blk0 = (size_t)t * tile_blk;
-            const size_t b = blk0 + (size_t)(py >> 4) * tr.bw + (px >> 4);
-            atomicAdd(tr.bcnt + b, 1u);
-            if (tr.bsum) atomicAdd(reinterpret_cast<unsigned long long*>(tr.bsum + b), (unsigned long long)q);
-            pixel_add(blk0, px, py, q);
+            const size_t b = (size_t)t * tile_blk + (size_t)(py >> 4) * tr.bw + (px >> 4);
+            const uint32_t code = __ldg(tr.code + b);
+            if (tier_mixed(code)) {
+                pixel_add(code, px, py, q);
+            } else if (code != kTierEmpty) {
+                atomicAdd(tr.bcnt + b, 1u);
+                if (tr.bsum) atomicAdd(reinterpret_cast<unsigned long long*>(tr.bsum + b), (unsigned long long)q);
+            }
         });
     }
     template <class H>

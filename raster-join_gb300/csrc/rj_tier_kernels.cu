@@ -262,8 +262,9 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
 
         unsigned long long acc_c = 0;
         long long acc_s = 0;
-        // listed blocks: reduce -- covered, not full (full ones take the
-        // block sums); labels -- covered and mixed
+        // listed blocks: reduce -- covered and not full, or full and mixed
+        // (a mixed block's points are in its pixel slot only; the other full
+        // blocks take their block totals); labels -- covered and mixed
         uint32_t Lw = 0u;   // lane k < nbw: listed blocks of word k
         for (int k = 0; k < nbw; ++k) {
             const uint32_t Iw = __shfl_sync(FULL, I, k), Uw = __shfl_sync(FULL, U, k);
@@ -273,10 +274,15 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
             bool take = false;
             if (MODE == MODE_TIER_REDUCE) {
                 if ((Iw >> lane) & 1u) {
-                    acc_c += __ldg(tr.bcnt + b);
-                    if (tr.bsum) acc_s += __ldg(tr.bsum + b);
+                    if (__ldg(tr.mixed + b) != 0u) {
+                        take = true;
+                    } else {
+                        acc_c += __ldg(tr.bcnt + b);
+                        if (tr.bsum) acc_s += __ldg(tr.bsum + b);
+                    }
+                } else {
+                    take = (Uw >> lane) & 1u;
                 }
-                take = ((Uw & ~Iw) >> lane) & 1u;
             } else {
                 take = ((Uw >> lane) & 1u) && __ldg(tr.mixed + b) != 0u;
             }

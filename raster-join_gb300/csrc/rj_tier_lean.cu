@@ -103,13 +103,16 @@ __device__ __forceinline__ void tl_visit(const TierLeanArgs& a, uint32_t* h_cnt,
         else lab = code;
         if (lab < (uint32_t)a.P) tl_hist_add<AGG>(h_cnt, (uint32_t)a.P, lc, lab, v);
     } else {
+        // the pixel slot of a mixed block, else the block total (an empty
+        // block keeps nothing: no polygon reads it)
         const bool fin = AGG && isfinite(v);
         const unsigned long long q = fin ? (unsigned long long)fixed_value(v, lc.scale) : 0ull;
-        atomicAdd(a.tr.bcnt + b, 1u);
-        if (fin) atomicAdd(reinterpret_cast<unsigned long long*>(a.tr.bsum + b), q);
         if ((code & kTierMixed) && code < kTierMulti) {
             atomicAdd(a.tr.pcnt + at, 1u);
             if (fin) atomicAdd(reinterpret_cast<unsigned long long*>(a.tr.psum + at), q);
+        } else if (code != kTierEmpty) {
+            atomicAdd(a.tr.bcnt + b, 1u);
+            if (fin) atomicAdd(reinterpret_cast<unsigned long long*>(a.tr.bsum + b), q);
         }
     }
 }
