@@ -338,7 +338,8 @@ k_poly_pass(PolyPassArgs a) {
                     }
                 };
                 if (!cover_slow) {
-                    warp_sort_ints(my_cross, m, lane);
+                    warp_sort_ints(my_cross, m, lane);   // the outline's inside test searches them too
+                    if (!(MODE == MODE_BOUNDS && a.tier_code))
                     for (int s2 = 0; s2 + 1 < m; s2 += 2) {
                         const int L = max(my_cross[s2], i_lo), R = min(my_cross[s2 + 1], i_hi + 1);
                         for (int i = L + lane; i < R; i += 32) visit(i);
@@ -413,9 +414,16 @@ k_poly_pass(PolyPassArgs a) {
                         float frac;
                         if (!compute_fraction(P0.x, P0.y, P1.x, P1.y, (float)i, ylo, (float)(i + 1), yhi, frac)) continue;
                         // inside test of the pixel centre: the same coverage rule
+                        // (an odd number of the row's crossings right of i; the
+                        // crossings are sorted, so a binary search counts them)
                         bool inside = false;
                         if (!cover_slow && centre_row) {
-                            for (int kk = 0; kk < m; ++kk) inside ^= (i < my_cross[kk]);
+                            int lo = 0, hi = m;   // first crossing right of i
+                            while (lo < hi) {
+                                const int mid = (lo + hi) >> 1;
+                                if (my_cross[mid] <= i) lo = mid + 1; else hi = mid;
+                            }
+                            inside = ((m - lo) & 1) != 0;
                         } else if (centre_row) {
                             for (int kk = 0; kk < n; ++kk) {
                                 int2 A = pv[kk];
