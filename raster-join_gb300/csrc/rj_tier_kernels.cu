@@ -82,6 +82,46 @@ __device__ __forceinline__ void edge_rows(int32_t ay, int32_t by, int jb, int& r
     r1 = (int)(a1 > kTBand - 1 ? kTBand - 1 : a1);
 }
 
+// f(q, r) for every (edge, band row) pair whose row centre line the edge's
+// y range spans, spread over the lanes: an edge crossing 16 rows gives 16
+// lanes work instead of one lane 16 exact divisions.  Every lane calls this
+// (warp-uniform loops); edge(e) returns staged edge e < ne.
+template <class E, class F>
+__device__ __forceinline__ void for_edge_rows(int ne, int jb, int lane, E&& edge, F&& f) {
+    const unsigned FULL = 0xffffffffu;
+    for (int e0 = 0; e0 < ne; e0 += 32) {
+        const int e = e0 + lane;
+        int4 q = make_int4(0, 0, 0, 0);
+        int r0 = 0, cnt = 0;
+        if (e < ne) {
+            q = edge(e);
+            int r1;
+            edge_rows(q.y, q.w, jb, r0, r1);
+            cnt = max(r1 - r0 + 1, 0);
+        }
+        int incl = cnt;
+        #pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(FULL, incl, 31);
+        for (int base = 0; base < total; base += 32) {
+            const int idx = base + lane;
+            int lo = 0, hi = 31;   // the first lane whose inclusive count exceeds idx
+            #pragma unroll
+            for (int s = 0; s < 5; ++s) {
+                const int mid = (lo + hi) >> 1;
+                if (__shfl_sync(FULL, incl, mid) > idx) hi = mid; else lo = mid + 1;
+            }
+            const int4 qe = make_int4(__shfl_sync(FULL, q.x, lo), __shfl_sync(FULL, q.y, lo),
+                                      __shfl_sync(FULL, q.z, lo), __shfl_sync(FULL, q.w, lo));
+            const int first = __shfl_sync(FULL, r0, lo) + idx - (__shfl_sync(FULL, incl, lo) - __shfl_sync(FULL, cnt, lo));
+            if (idx < total) f(qe, first);
+        }
+    }
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs tr) {
     extern __shared__ int4 s_tier[];
@@ -198,23 +238,18 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
         if (!live) continue;
 
         // sweep 1: block toggles and inside-crossing flags per live row
-        for (int e = lane; e < ne; e += 32) {
-            const int4 q = edge_at(e);
-            int r0, r1;
-            edge_rows(q.y, q.w, jb, r0, r1);
-            for (int r = r0; r <= r1; ++r) {
-                const int32_t cy = (jb + r) * kSub + kSub / 2;
-                if (!((live >> r) & 1u) || !cross_row(q.y, q.w, cy)) continue;
-                const int L = max(cross_L(q.x, q.y, q.z, q.w, cy), i_lo);
-                if (L > i_hi) continue;
-                const int rb = ((L + 15) >> 4) - bc_lo;
-                if (rb < nbc) atomicXor(&S.X[r * kTBW + (rb >> 5)], 1u << (rb & 31));
-                if (L & 15) {
-                    const int cb = (L >> 4) - bc_lo;
-                    atomicOr(&S.C[r * kTBW + (cb >> 5)], 1u << (cb & 31));
-                }
+        for_edge_rows(ne, jb, lane, edge_at, [&](const int4& q, int r) {
+            const int32_t cy = (jb + r) * kSub + kSub / 2;
+            if (!((live >> r) & 1u) || !cross_row(q.y, q.w, cy)) return;
+            const int L = max(cross_L(q.x, q.y, q.z, q.w, cy), i_lo);
+            if (L > i_hi) return;
+            const int rb = ((L + 15) >> 4) - bc_lo;
+            if (rb < nbc) atomicXor(&S.X[r * kTBW + (rb >> 5)], 1u << (rb & 31));
+            if (L & 15) {
+                const int cb = (L >> 4) - bc_lo;
+                atomicOr(&S.C[r * kTBW + (cb >> 5)], 1u << (cb & 31));
             }
-        }
+        });
         __syncwarp();
         // block columns [fb, lb] lie wholly inside [i_lo, i_hi]; word hw's valid blocks
         const int fb = ((i_lo + 15) >> 4) - bc_lo, lb = ((i_hi + 1) >> 4) - 1 - bc_lo;
@@ -319,19 +354,14 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
             __syncwarp();
             // sweep 2: pixel toggles of the listed blocks (crossings inside a
             // block only; one at a block's first pixel is in X already)
-            for (int e = lane; e < ne; e += 32) {
-                const int4 q = edge_at(e);
-                int r0, r1;
-                edge_rows(q.y, q.w, jb, r0, r1);
-                for (int r = r0; r <= r1; ++r) {
-                    const int32_t cy = (jb + r) * kSub + kSub / 2;
-                    if (!((live >> r) & 1u) || !cross_row(q.y, q.w, cy)) continue;
-                    const int L = max(cross_L(q.x, q.y, q.z, q.w, cy), i_lo);
-                    if (L > i_hi || !(L & 15)) continue;
-                    const int k = S.map[(L >> 4) - bc_lo];
-                    if (k != 0xFF) atomicXor(&S.M[k * 8 + (r >> 1)], (1u << (L & 15)) << ((r & 1) * 16));
-                }
-            }
+            for_edge_rows(ne, jb, lane, edge_at, [&](const int4& q, int r) {
+                const int32_t cy = (jb + r) * kSub + kSub / 2;
+                if (!((live >> r) & 1u) || !cross_row(q.y, q.w, cy)) return;
+                const int L = max(cross_L(q.x, q.y, q.z, q.w, cy), i_lo);
+                if (L > i_hi || !(L & 15)) return;
+                const int k = S.map[(L >> 4) - bc_lo];
+                if (k != 0xFF) atomicXor(&S.M[k * 8 + (r >> 1)], (1u << (L & 15)) << ((r & 1) * 16));
+            });
             __syncwarp();
             // row masks: coverage at the block's first pixel, then the block's
             // own crossings, clipped to [i_lo, i_hi]
