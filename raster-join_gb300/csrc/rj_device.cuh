@@ -318,6 +318,26 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+// The work item's owner: the last index tp in [0, n) with start[tp] <= item,
+// for a nondecreasing start[] with start[0] == 0 <= item.  Called by the whole
+// warp: each round the 32 lanes probe evenly spaced entries and the range
+// shrinks to the gap between the last probe at or below item and the next,
+// so a search over n entries takes ceil(log32 n) dependent loads instead of
+// log2 n.
+__device__ __forceinline__ int warp_find_owner(const int* __restrict__ start, int n, int item, int lane) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int step = (hi - lo + 32) >> 5;   // ceil((hi - lo + 1) / 32)
+        const int pos = min(lo + lane * step, hi);
+        const unsigned le = __ballot_sync(0xffffffffu, __ldg(start + pos) <= item);
+        const int last = 31 - __clz(le);          // lane 0 probes lo: le != 0
+        const int plast = min(lo + last * step, hi);
+        const int pnext = last < 31 ? min(lo + (last + 1) * step, hi) : hi + 1;
+        lo = plast;
+        hi = (pnext > plast) ? min(pnext - 1, hi) : hi;
+    }
+    return lo;
+}
 __device__ __forceinline__ double warp_sum_f64(double v) {
     #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -234,22 +234,11 @@ k_poly_pass(PolyPassArgs a) {
                     (size_t)warp * kCrossCap;
 
     for (;;) {
-        int item = 0, tp = 0;
-        if (lane == 0) {
-            item = (int)atomicAdd(a.work_ctr, 1u);
-            if (item < total) {
-                // last tp with band_start[tp] <= item
-                int lo = 0, hi = TP - 1;
-                while (lo < hi) {
-                    int mid = (lo + hi + 1) >> 1;
-                    if (a.band_start[mid] <= item) lo = mid; else hi = mid - 1;
-                }
-                tp = lo;
-            }
-        }
+        int item = 0;
+        if (lane == 0) item = (int)atomicAdd(a.work_ctr, 1u);
         item = __shfl_sync(FULL, item, 0);
-        tp = __shfl_sync(FULL, tp, 0);
         if (item >= total) break;
+        const int tp = warp_find_owner(a.band_start, TP, item, lane);
         const int t = tp / a.P, p = tp - t * a.P;
         const int band = item - a.band_start[tp];
         const int4 ia = a.info_a[tp];

@@ -138,21 +138,11 @@ __global__ void __launch_bounds__(kTW * 32) k_tier_pass(PolyPassArgs a, TierArgs
     __syncwarp();
     const int hw = lane & 15, half = lane >> 4;   // sweep 1: row 2k + half, block word hw
     for (;;) {
-        int item = 0, tp = 0;
-        if (lane == 0) {
-            item = (int)atomicAdd(a.work_ctr, 1u);
-            if (item < total) {
-                int lo = 0, hi = TP - 1;
-                while (lo < hi) {
-                    int mid = (lo + hi + 1) >> 1;
-                    if (a.band_start[mid] <= item) lo = mid; else hi = mid - 1;
-                }
-                tp = lo;
-            }
-        }
+        int item = 0;
+        if (lane == 0) item = (int)atomicAdd(a.work_ctr, 1u);
         item = __shfl_sync(FULL, item, 0);
-        tp = __shfl_sync(FULL, tp, 0);
         if (item >= total) break;
+        const int tp = warp_find_owner(a.band_start, TP, item, lane);
         const int t = tp / a.P, p = tp - t * a.P;
         const int band = item - a.band_start[tp];
         const int4 ia = a.info_a[tp];
