@@ -204,8 +204,8 @@ constexpr size_t kTierMinPixels = (size_t)1 << 24;
 // pixel, tiered point lookups ~3.1 ps per point more while the flat canvas
 // stays in L2).  Beyond kTierFlatMaxPixels a flat canvas no longer stays in
 // L2 and every point's lookup goes to DRAM: 2B points on a 40000 x 40000
-// canvas took 52.7 ms flat against 21.5 ms tiered (260 Voronoi cells; 2000
-// overlapping stars: 97.3 against 56.7 ms).
+// canvas took 53.2 ms flat against 12.5 ms tiered (260 Voronoi cells; 2000
+// overlapping stars: 97.7 against 44.2 ms).
 constexpr size_t kTierFlatMaxPixels = (size_t)1 << 25;
 inline bool use_tier(size_t npix, uint64_t rows) {
     return npix >= kTierMinPixels && (npix > 2 * rows || npix > kTierFlatMaxPixels);
