@@ -127,3 +127,59 @@ def test_tiered_error_bounds_match_oracle(handler, sets, fbo, name, line_filter)
     np.testing.assert_array_equal(got.count, want[0])
     np.testing.assert_array_equal(got.bounds, want[2])
     np.testing.assert_array_equal(flat.bounds, want[2])
+
+
+def _crowded_sets():
+    """Polygons that crowd one band of 16 rows: a sawtooth 4000 px long whose
+    teeth (8 px wide, 8 px high) put a crossing inside every block of its band
+    (250 listed blocks: four rounds of 64), and a star of 1,200 vertices 120 px
+    across (more than 256 edges in a band: the edges are read from global
+    memory).  Two small triangles stretch the canvas past 2^24 pixels.  Set
+    "apart" has no overlaps (label form); "frame" adds a square over most of
+    the canvas (canvas form)."""
+    k = np.arange(501)
+    teeth = np.c_[1000.0 + 8.0 * k, 3000.0 + np.where(k % 2 == 1, 4.0, -4.0) + 0.37]
+    saw = np.r_[teeth, [[5000.0, 2900.25], [1000.0, 2900.25]]]
+    n = 1200
+    ang = 2 * np.pi * np.arange(n) / n
+    rad = np.where(np.arange(n) % 2 == 0, 60.0, 20.0)
+    star = np.c_[3000.3 + rad * np.cos(ang), 4500.6 + rad * np.sin(ang)]
+    t1 = np.array([[5900.0, 100.0], [5990.0, 100.0], [5950.0, 150.0]])
+    t2 = np.array([[100.0, 5900.0], [150.0, 5950.0], [100.0, 5950.0]])
+    frame = np.array([[500.0, 500.0], [5500.0, 500.0], [5500.0, 5500.0], [500.0, 5500.0]])
+
+    def pack(polys):
+        v = np.concatenate(polys).astype(np.float32)
+        pidx = np.r_[0, np.cumsum([len(q) for q in polys])].astype(np.int32)
+        return v, pidx
+    return {"apart": pack([saw, star, t1, t2]), "frame": pack([saw, star, t1, t2, frame])}
+
+
+@pytest.mark.parametrize("fbo", [8192, 2100])
+@pytest.mark.parametrize("name", ["apart", "frame"])
+def test_crowded_bands_match_oracle(handler, fbo, name):
+    verts, pidx = _crowded_sets()[name]
+    rng = np.random.default_rng(91)
+    xy = np.r_[rng.uniform(0, BOX, (300_000, 2)),
+               np.c_[rng.uniform(990, 5010, 200_000), rng.uniform(2890, 3012, 200_000)],
+               np.c_[rng.normal(3000.3, 40, 100_000), rng.normal(4500.6, 40, 100_000)]].astype(np.float32)
+    pts = synth.points(len(xy), seed=92, box=BOX, columns=True)
+    pts["xy"] = xy
+    handler.setDataHandler(_dh(pts, verts, pidx, False))
+    handler.setCellSize(1.0)
+    handler.max_fbo_size = fbo
+    want = oracle.raster_join(xy, verts, pidx, 1.0, max_res=fbo, bounds=True)
+    try:
+        handler.flags = rj.FLAG_TIERED_CANVAS
+        got = handler.execute(rj.RasterJoinFn)
+        bnd = handler.execute(rj.RasterJoinBoundFn)
+        handler.flags = rj.FLAG_FLAT_CANVAS
+        flat = handler.execute(rj.RasterJoinFn)
+    finally:
+        handler.flags = 0
+        handler.max_fbo_size = 8192
+    np.testing.assert_array_equal(got.count, want[0])
+    np.testing.assert_array_equal(flat.count, want[0])
+    np.testing.assert_array_equal(bnd.count, want[0])
+    np.testing.assert_array_equal(bnd.bounds, want[2])
+    assert want[0][:2].min() > 0
