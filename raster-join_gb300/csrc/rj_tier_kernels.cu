@@ -19,6 +19,8 @@
 // rows.  The work of a band is proportional to the crossings of its rows and
 // to the blocks the polygon's outline passes through (plus one entry per full
 // block), not to the pixels of its area:
+//   * the band's (edge, row) crossing pairs are spread over the lanes, one
+//     exact division each;
 //   * sweep 1 -- every crossing of a live row toggles one bit of a per-row
 //     block bitmap (at the first block whose first pixel lies at or right of
 //     it) and, when it falls strictly inside a block, flags that block; a
@@ -27,7 +29,8 @@
 //     Over the 16 rows: I = blocks covered throughout (full for the polygon),
 //     U = blocks the polygon covers somewhere.
 //   * the blocks whose pixels matter (labels: U and mixed; reduce: U and not
-//     full) are listed, up to 64 at a time; sweep 2 toggles per-pixel bits of
+//     full, or full and mixed -- a mixed block's points are in its pixel slot
+//     only) are listed, up to 64 at a time; sweep 2 toggles per-pixel bits of
 //     the listed blocks only, and their 16-bit row masks follow from the
 //     block's first-pixel coverage and a 16-bit prefix XOR;
 //   * the listed blocks' pixel slots are then read or written by the whole
