@@ -347,32 +347,58 @@ k_poly_pass(PolyPassArgs a) {
             }
             if (MODE == MODE_BOUNDS) {
                 // Outline pass: every edge of the polygon touching this pixel
-                // row, every pixel of the row the edge clips.
+                // row, every pixel of the row the edge clips.  The (edge,
+                // pixel) pairs of 32 edges at a time are spread over the
+                // lanes, so a long edge does not leave the others idle.
                 const float ylo = (float)j, yhi = (float)(j + 1);
                 for (int e0 = 0; e0 < ne; e0 += 32) {
-                    int e = e0 + lane;
-                    if (e >= ne) continue;
-                    int k = overflow ? e : my_eidx[e];
-                    float2 P0 = pf[k];
-                    float2 P1 = pf[(k + 1 == n) ? 0 : k + 1];
-                    float eylo = fminf(P0.y, P1.y), eyhi = fmaxf(P0.y, P1.y);
-                    if (eyhi < ylo - 0.01f || eylo > yhi + 0.01f) continue;
-                    // x range of the edge inside the slab (conservative, +-1 px)
-                    float xa, xb;
-                    if (P0.y == P1.y) {
-                        xa = fminf(P0.x, P1.x); xb = fmaxf(P0.x, P1.x);
-                    } else {
-                        float ta = (ylo - P0.y) / (P1.y - P0.y);
-                        float tb = (yhi - P0.y) / (P1.y - P0.y);
-                        ta = fminf(fmaxf(ta, 0.0f), 1.0f);
-                        tb = fminf(fmaxf(tb, 0.0f), 1.0f);
-                        float x_a = P0.x + (P1.x - P0.x) * ta;
-                        float x_b = P0.x + (P1.x - P0.x) * tb;
-                        xa = fminf(x_a, x_b); xb = fmaxf(x_a, x_b);
+                    const int e = e0 + lane;
+                    int k = 0, ia0 = 0, cnt = 0;
+                    if (e < ne) {
+                        k = overflow ? e : my_eidx[e];
+                        const float2 P0 = pf[k];
+                        const float2 P1 = pf[(k + 1 == n) ? 0 : k + 1];
+                        const float eylo = fminf(P0.y, P1.y), eyhi = fmaxf(P0.y, P1.y);
+                        if (!(eyhi < ylo - 0.01f || eylo > yhi + 0.01f)) {
+                            // x range of the edge inside the slab (conservative, +-1 px)
+                            float xa, xb;
+                            if (P0.y == P1.y) {
+                                xa = fminf(P0.x, P1.x); xb = fmaxf(P0.x, P1.x);
+                            } else {
+                                float ta = (ylo - P0.y) / (P1.y - P0.y);
+                                float tb = (yhi - P0.y) / (P1.y - P0.y);
+                                ta = fminf(fmaxf(ta, 0.0f), 1.0f);
+                                tb = fminf(fmaxf(tb, 0.0f), 1.0f);
+                                float x_a = P0.x + (P1.x - P0.x) * ta;
+                                float x_b = P0.x + (P1.x - P0.x) * tb;
+                                xa = fminf(x_a, x_b); xb = fmaxf(x_a, x_b);
+                            }
+                            ia0 = max((int)floorf(xa) - 1, 0);
+                            const int ib0 = min((int)floorf(xb) + 1, a.resx - 1);
+                            cnt = max(ib0 - ia0 + 1, 0);
+                        }
                     }
-                    int ia0 = max((int)floorf(xa) - 1, 0);
-                    int ib0 = min((int)floorf(xb) + 1, a.resx - 1);
-                    for (int i = ia0; i <= ib0; ++i) {
+                    int incl = cnt;
+                    #pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int v = __shfl_up_sync(FULL, incl, o);
+                        if (lane >= o) incl += v;
+                    }
+                    const int npairs = __shfl_sync(FULL, incl, 31);
+                    for (int base = 0; base < npairs; base += 32) {
+                        const int idx = base + lane;
+                        int lo = 0, hi = 31;   // the lane whose edge holds pair idx
+                        #pragma unroll
+                        for (int st = 0; st < 5; ++st) {
+                            const int mid = (lo + hi) >> 1;
+                            if (__shfl_sync(FULL, incl, mid) > idx) hi = mid; else lo = mid + 1;
+                        }
+                        const int ke = __shfl_sync(FULL, k, lo);
+                        const int i = __shfl_sync(FULL, ia0, lo) + idx -
+                                      (__shfl_sync(FULL, incl, lo) - __shfl_sync(FULL, cnt, lo));
+                        if (idx >= npairs) continue;
+                        const float2 P0 = pf[ke];
+                        const float2 P1 = pf[(ke + 1 == n) ? 0 : ke + 1];
                         uint32_t val;
                         if (a.tier_code) {
                             // the pixel's count in its mixed block's slot
@@ -389,7 +415,7 @@ k_poly_pass(PolyPassArgs a) {
                         if (val == 0) continue;
                         if (a.line_filter) {
                             // varying interpolation along the line (projection of
-                            // the pixel centre), kept within 0.5 px: line-bound.frag:245
+                            // the pixel centre), kept within 0.5 px: line-bound.frag:221
                             float cxp = (float)i + 0.5f, cyp = (float)j + 0.5f;
                             float dx = __fsub_rn(P1.x, P0.x), dy = __fsub_rn(P1.y, P0.y);
                             float l2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
@@ -407,12 +433,12 @@ k_poly_pass(PolyPassArgs a) {
                         // crossings are sorted, so a binary search counts them)
                         bool inside = false;
                         if (!cover_slow && centre_row) {
-                            int lo = 0, hi = m;   // first crossing right of i
-                            while (lo < hi) {
-                                const int mid = (lo + hi) >> 1;
-                                if (my_cross[mid] <= i) lo = mid + 1; else hi = mid;
+                            int clo = 0, chi = m;   // first crossing right of i
+                            while (clo < chi) {
+                                const int mid = (clo + chi) >> 1;
+                                if (my_cross[mid] <= i) clo = mid + 1; else chi = mid;
                             }
-                            inside = ((m - lo) & 1) != 0;
+                            inside = ((m - clo) & 1) != 0;
                         } else if (centre_row) {
                             for (int kk = 0; kk < n; ++kk) {
                                 int2 A = pv[kk];
