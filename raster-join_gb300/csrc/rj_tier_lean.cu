@@ -17,8 +17,9 @@
 //   LABEL: the block code (full polygon, empty, or mixed | slot) and, for a
 //          mixed block, the pixel's label give the polygon; one count (and
 //          the fixed-point value) into the block's shared histogram.
-//   splat: the block's count / sum and, for a mixed block, the pixel's,
-//          with plain global atomics (the polygon pass reduces them).
+//   splat: one count (and sum) per point with plain global atomics: into
+//          the pixel slot of a mixed block, else into the block's total (an
+//          empty block keeps nothing); the polygon pass reduces them.
 #include "rj_lean.cuh"
 
 namespace rj {
