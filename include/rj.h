@@ -121,7 +121,7 @@ typedef struct {
     double ground_resolution;       /* metres per world unit (1 for metric
                                        coordinates; UsefulFuncs.cpp:625)   */
     int32_t grid_res;               /* polygon grid index resolution       */
-    int32_t max_fbo_size;           /* canvas tile side (0 = 8192)         */
+    int32_t max_fbo_size;           /* canvas tile side (0 = 8192), <= 8192 */
     int32_t time_attrib;            /* uint32 column of the time range, or -1 */
     uint32_t t_start, t_end;        /* inclusive range, DataHandler.cpp:107-109 */
     int32_t hybrid_canvas;          /* hybrid canvas long side (0 = 8192,

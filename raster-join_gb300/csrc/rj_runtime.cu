@@ -123,6 +123,10 @@ double now_ms() {
 }
 
 int plan_raster_bbox(rj_ctx* ctx, const double* bbox, const rj_query* q, RasterPlan& rp) {
+    // tiles up to the reference's framebuffer side (GLFunction.hpp:14); the
+    // tiered canvas's kernels hold a tile row of at most 8192 pixels
+    if (q->max_fbo_size > RJ_MAX_FBO_SIZE)
+        return fail(ctx, RJ_E_INVALID, "canvas tile side %d above %d", q->max_fbo_size, RJ_MAX_FBO_SIZE);
     double ground = q->ground_resolution > 0 ? q->ground_resolution : 1.0;
     double cell = q->cell_size > 0 ? q->cell_size : (q->accuracy_m / std::sqrt(2.0)) / ground;
     if (!(cell > 0) || !std::isfinite(cell)) return fail(ctx, RJ_E_INVALID, "invalid cell size %g", cell);

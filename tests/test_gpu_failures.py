@@ -101,6 +101,12 @@ def test_bad_arguments_refused(handler, small):
     assert lib.rj_set_tuning(handler.ctx, 99, 0) == -1
     assert lib.rj_set_tuning(handler.ctx, rj.TUNE_COUNT_BLOCK_SHIFT, 2) == -1
     assert b"block shift" in lib.rj_last_error(handler.ctx)
+    # canvas tiles above the reference's 8192-pixel framebuffer (GLFunction.hpp:14)
+    q = handler.make_query(rj.RasterJoinFn)
+    q.max_fbo_size = 16384
+    res = rj.Result()
+    assert lib.rj_execute(handler.ctx, C.byref(q), C.byref(res)) == -1
+    assert b"tile side" in lib.rj_last_error(handler.ctx)
     handler._loaded_points = None
     got = _join(handler, xy, verts, pidx)
     np.testing.assert_array_equal(got.count, oracle.raster_join(xy, verts, pidx, 50.0)[0])
