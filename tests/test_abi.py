@@ -100,3 +100,23 @@ def test_create_without_gpu_returns_status(built):
     assert lib.rj_poll(None, 0, 0, None) == -1
     with pytest.raises(rj.RJError):
         rj.GLHandler()
+
+
+def header_constants(prefixes):
+    """Integer #defines of include/rj.h whose names start with one of prefixes."""
+    out = {}
+    for name, val in re.findall(r"^#define\s+(RJ_\w+)\s+(-?(?:0x[0-9A-Fa-f]+|\d+))u?\b", open(HEADER).read(), re.M):
+        if name.startswith(prefixes):
+            out[name] = int(val, 0)
+    return out
+
+
+def test_binding_constants_match_header():
+    """Every flag, tuning knob and batch flag of the header has the binding's
+    constant of the same name and value, and the status names agree."""
+    consts = header_constants(("RJ_FLAG_", "RJ_TUNE_", "RJ_BATCH_"))
+    assert len(consts) >= 20
+    for name, val in consts.items():
+        assert getattr(rj, name[3:]) == val, name
+    status = header_constants(("RJ_OK", "RJ_E_", "RJ_PENDING"))
+    assert status and all(rj.STATUS[v] == name for name, v in status.items())
