@@ -108,7 +108,7 @@ def test_filters_and_time_range(lite):
 
 
 @pytest.mark.parametrize("cell,expect", [
-    (10.0, (1, 1, 4000, 4000)),                       # BASELINE's "eps = 10 m (4000^2 canvas)"
+    (10.0, (1, 1, 4000, 4000)),                       # eps = 10 m as the pixel side: a 4000^2 canvas
     (10.0 / np.sqrt(2.0), (1, 1, 5657, 5657)),        # accuracy 10 m, GLFunction.cpp:26-30
     (1.0, (5, 5, 8000, 8000)),
     (1.0 / np.sqrt(2.0), (7, 7, 8082, 8082)),         # accuracy 1 m: 7x7 tiles of 8082^2 (RasterJoin.cpp:59-63)
